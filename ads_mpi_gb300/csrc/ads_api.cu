@@ -1,0 +1,1060 @@
+// ads_api.cu — the C-ABI (include/ads_gpu.h): handle, device memory, step
+// orchestration, refinement control, adjoint driver, timing.
+//
+// One handle = one configuration on one GPU (the reference's ADS_setup +
+// ADS_compute_data, src/Setup.F90:29-140, for one rank).  Device layouts:
+//   L0: x fastest, pitch PX  (coefficients u, assembled F, residual r)
+//   L1: y fastest, pitch PY  (after the x sweep; the reference's F2)
+//   L2: z fastest, pitch PZ  (after the y sweep; the reference's F3)
+// Pitches are rounded up to 8 entries so every TMA stride is a multiple of 16 B.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ads_internal.cuh"
+#include "setup.h"
+
+using namespace ads;
+
+namespace {
+
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+PFN_encodeTiled get_encode() {
+  static PFN_encodeTiled fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_encodeTiled>(p);
+  }
+  return fn;
+}
+
+long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
+
+}  // namespace
+
+struct ads_handle {
+  int n[3] = {0, 0, 0}, p[3] = {0, 0, 0};
+  int P = 0, Q = 0;
+  ads_opts opts{};
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+
+  AxisHost ax[3];
+  Geometry g{};
+  size_t n0 = 0, n1 = 0, n2 = 0;  // padded element counts of L0/L1/L2
+  long long nqp = 0;
+
+  // device tables
+  double* d_nn64[3] = {nullptr, nullptr, nullptr};
+  double* d_jw64[3] = {nullptr, nullptr, nullptr};
+  float* d_nn32[3] = {nullptr, nullptr, nullptr};
+  float* d_jw32[3] = {nullptr, nullptr, nullptr};
+  double* d_fac64[3] = {nullptr, nullptr, nullptr};
+  double* d_tfac64[3] = {nullptr, nullptr, nullptr};
+  float* d_fac32[3] = {nullptr, nullptr, nullptr};
+  double* d_band[3] = {nullptr, nullptr, nullptr};
+
+  // device buffers
+  double* d_u = nullptr;
+  double* d_F = nullptr;
+  double* d_r = nullptr;
+  double* d_wA = nullptr;  // L1 (double-sized; float view uses the same memory)
+  double* d_wB = nullptr;  // L2
+  double* d_shadow = nullptr;
+  double* d_fqp = nullptr;
+  double* d_kqp = nullptr;
+  double* d_l2part = nullptr;
+  double* d_part = nullptr;
+  double* d_scal = nullptr;
+  int* d_flags = nullptr;
+  double* d_hist = nullptr;
+  int hist_cap = 0;
+  int npart = 0;
+
+  // launch geometry
+  int asm_grid = 0, asm_zc = 0, asm_nix = 0, asm_niy = 0, asm_niz = 0;
+  int res_grid = 0, res_zc = 0, res_nix = 0, res_niy = 0, res_niz = 0;
+  int norm_parts = 0;
+
+  // tensor maps
+  CUtensorMap tm_F_in64{}, tm_r_in64{}, tm_u_out64{}, tm_r_out64{};
+  CUtensorMap tm_wA_out64{}, tm_wA_in64{}, tm_wB_out64{}, tm_wB_in64{};
+  CUtensorMap tm_wA_out32{}, tm_wA_in32{}, tm_wB_out32{}, tm_wB_in32{};
+
+  // form
+  bool has_form = false;
+  int form = ADS_FORM_PROJECT;
+  double kappa = 1.0, dt = 0.0;
+  bool has_f = false, has_k = false;
+
+  ads_stats last{};
+
+  // timing: one event pair per timed launch, resolved when the totals are read
+  bool timing = false;
+  std::vector<std::string> tnames;
+  std::vector<double> tms;
+  std::vector<int> tcount;
+  std::vector<cudaEvent_t> evpool;
+  std::vector<int> pending;  // kernel index of each recorded event pair
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  long long launches = 0;
+
+  // graph of one step
+  cudaGraphExec_t gexec = nullptr;
+  bool graph_valid = false;
+  long long graph_launches = 0;
+};
+
+namespace {
+
+int fail(ads_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int cuda_fail(ads_handle* h, cudaError_t e, const char* where) {
+  return fail(h, ADS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define ADS_CUDA(h, call)                               \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+  } while (0)
+
+// resolve recorded event pairs into the per-kernel totals
+void resolve_timing(ads_handle* h) {
+  if (h->pending.empty()) return;
+  cudaStreamSynchronize(h->stream);
+  for (size_t i = 0; i < h->pending.size(); ++i) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->evpool[2 * i], h->evpool[2 * i + 1]) == cudaSuccess) {
+      h->tms[h->pending[i]] += ms;
+      h->tcount[h->pending[i]] += 1;
+    }
+  }
+  h->pending.clear();
+}
+
+template <typename F>
+int run_kernel(ads_handle* h, const char* name, int nlaunch, F&& f) {
+  cudaError_t e;
+  if (h->timing) {
+    size_t k = 0;
+    for (; k < h->tnames.size(); ++k)
+      if (h->tnames[k] == name) break;
+    if (k == h->tnames.size()) {
+      h->tnames.push_back(name);
+      h->tms.push_back(0.0);
+      h->tcount.push_back(0);
+    }
+    if (h->pending.size() >= 4096) resolve_timing(h);
+    const size_t i = h->pending.size();
+    while (h->evpool.size() < 2 * (i + 1)) {
+      cudaEvent_t ev;
+      if (cudaEventCreate(&ev) != cudaSuccess) break;
+      h->evpool.push_back(ev);
+    }
+    const bool have = h->evpool.size() >= 2 * (i + 1);
+    if (have) cudaEventRecord(h->evpool[2 * i], h->stream);
+    e = f();
+    if (have) {
+      cudaEventRecord(h->evpool[2 * i + 1], h->stream);
+      h->pending.push_back((int)k);
+    }
+  } else {
+    e = f();
+  }
+  h->launches += nlaunch;
+  if (e != cudaSuccess) return cuda_fail(h, e, name);
+  return ADS_OK;
+}
+
+#define RUN(h, name, n, expr)                                               \
+  do {                                                                      \
+    int st_ = run_kernel(h, name, n, [&]() -> cudaError_t { return (expr); }); \
+    if (st_ != ADS_OK) return st_;                                          \
+  } while (0)
+
+template <typename T>
+int upload(ads_handle* h, T** d, const std::vector<T>& v) {
+  ADS_CUDA(h, cudaMalloc((void**)d, sizeof(T) * std::max<size_t>(v.size(), 1)));
+  ADS_CUDA(h, cudaMemcpy(*d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  return ADS_OK;
+}
+
+bool encode(CUtensorMap* m, void* base, bool fp32, cuuint64_t d0, cuuint64_t d1, cuuint64_t d2,
+            long long pitch, cuuint32_t b0, cuuint32_t b1, cuuint32_t b2) {
+  PFN_encodeTiled fn = get_encode();
+  if (!fn) return false;
+  const size_t es = fp32 ? 4 : 8;
+  cuuint64_t dims[3] = {d0, d1, d2};
+  cuuint64_t strides[2] = {(cuuint64_t)(pitch * es), (cuuint64_t)(pitch * d1 * es)};
+  cuuint32_t box[3] = {b0, b1, b2};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(m, fp32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, base, dims,
+                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// Layout maps: L0 dims (Nx,Ny,Nz) pitch PX; L1 (Ny,Nx,Nz) pitch PY; L2 (Nz,Nx,Ny) pitch PZ.
+// Sweep input boxes are (CH, lanes...) and output boxes (32 lanes, line...).
+bool make_l0_in(const ads_handle* h, CUtensorMap* m, void* base, bool f32) {
+  return encode(m, base, f32, h->g.N[0], h->g.N[1], h->g.N[2], h->g.PX, SW_CH, SW_LANES, 1);
+}
+bool make_l0_out(const ads_handle* h, CUtensorMap* m, void* base, bool f32) {
+  return encode(m, base, f32, h->g.N[0], h->g.N[1], h->g.N[2], h->g.PX, SW_LANES, 1, SW_CH);
+}
+bool make_l1_out(const ads_handle* h, CUtensorMap* m, void* base, bool f32) {
+  return encode(m, base, f32, h->g.N[1], h->g.N[0], h->g.N[2], h->g.PY, SW_LANES, SW_CH, 1);
+}
+bool make_l1_in(const ads_handle* h, CUtensorMap* m, void* base, bool f32) {
+  return encode(m, base, f32, h->g.N[1], h->g.N[0], h->g.N[2], h->g.PY, SW_CH, 1, SW_LANES);
+}
+bool make_l2_out(const ads_handle* h, CUtensorMap* m, void* base, bool f32) {
+  return encode(m, base, f32, h->g.N[2], h->g.N[0], h->g.N[1], h->g.PZ, SW_LANES, 1, SW_CH);
+}
+bool make_l2_in(const ads_handle* h, CUtensorMap* m, void* base, bool f32) {
+  return encode(m, base, f32, h->g.N[2], h->g.N[0], h->g.N[1], h->g.PZ, SW_CH, SW_LANES, 1);
+}
+
+// sweep along `axis` (0: x, L0->L1; 1: y, L1->L2; 2: z, L2->L0)
+SweepArgs sweep_args(const ads_handle* h, int axis, const void* fac) {
+  SweepArgs a{};
+  const int* N = h->g.N;
+  a.L = N[axis];
+  a.nchunk = (a.L + SW_CH - 1) / SW_CH;
+  if (axis == 0) { a.lanes_total = N[1]; a.lane_dim = 1; a.out_line_dim = 1; }
+  if (axis == 1) { a.lanes_total = N[2]; a.lane_dim = 2; a.out_line_dim = 2; }
+  if (axis == 2) { a.lanes_total = N[0]; a.lane_dim = 1; a.out_line_dim = 2; }
+  a.tiles_lane = (a.lanes_total + SW_LANES - 1) / SW_LANES;
+  a.fac = fac;
+  a.in_scale = 1.0;
+  a.out_scale = 1.0;
+  a.out = h->d_u;
+  a.out_pitch = h->g.PX;
+  a.out_slice = h->g.PX * (long long)N[1];
+  a.err = h->d_flags + FL_ERR;
+  return a;
+}
+int sweep_grid(const ads_handle* h, int axis) {
+  const int* N = h->g.N;
+  if (axis == 0) return ((N[1] + SW_LANES - 1) / SW_LANES) * N[2];
+  if (axis == 1) return ((N[2] + SW_LANES - 1) / SW_LANES) * N[0];
+  return ((N[0] + SW_LANES - 1) / SW_LANES) * N[1];
+}
+
+AssembleArgs assemble_args(const ads_handle* h, const double* u, double* F, bool with_f) {
+  AssembleArgs a{};
+  a.g = h->g;
+  a.form = h->form;
+  a.zc = h->asm_zc;
+  a.nix = h->asm_nix; a.niy = h->asm_niy; a.niz = h->asm_niz;
+  a.dt = h->dt;
+  a.kappa = h->kappa;
+  a.u = u;
+  a.F = F;
+  a.shadow = h->d_shadow;
+  a.shadow_stride = (long long)h->n0;
+  a.fqp = (with_f && h->has_f) ? h->d_fqp : nullptr;
+  a.kqp = h->has_k ? h->d_kqp : nullptr;
+  a.l2part = h->d_l2part;
+  a.err = h->d_flags + FL_ERR;
+  return a;
+}
+
+FixupArgs fixup_args(const ads_handle* h, double* F) {
+  FixupArgs f{};
+  f.g = h->g;
+  f.zc = h->asm_zc;
+  f.nix = h->asm_nix; f.niy = h->asm_niy; f.niz = h->asm_niz;
+  f.F = F;
+  f.shadow = h->d_shadow;
+  f.shadow_stride = (long long)h->n0;
+  f.l2part = h->d_l2part;
+  f.nl2 = h->asm_grid;
+  f.l2out = h->d_scal + SC_L2;
+  return f;
+}
+
+ResidualArgs residual_args(const ads_handle* h, const double* u, const double* F, double* r) {
+  ResidualArgs a{};
+  a.g = h->g;
+  a.zc = h->res_zc;
+  a.nix = h->res_nix; a.niy = h->res_niy; a.niz = h->res_niz;
+  a.u = u; a.F = F; a.r = r;
+  for (int d = 0; d < 3; ++d) a.band[d] = h->d_band[d];
+  a.part = h->d_part;
+  a.err = h->d_flags + FL_ERR;
+  return a;
+}
+
+// assembly (+ fixup) of F from coefficients u with the handle's form
+int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool with_f) {
+  AssembleArgs a = assemble_args(h, u, F, with_f);
+  AxisTab<double> t64[3];
+  AxisTab<float> t32[3];
+  for (int d = 0; d < 3; ++d) {
+    t64[d].nn = h->d_nn64[d]; t64[d].jw = h->d_jw64[d];
+    t32[d].nn = h->d_nn32[d]; t32[d].jw = h->d_jw32[d];
+  }
+  const void* tx = fp32 ? (const void*)&t32[0] : (const void*)&t64[0];
+  const void* ty = fp32 ? (const void*)&t32[1] : (const void*)&t64[1];
+  const void* tz = fp32 ? (const void*)&t32[2] : (const void*)&t64[2];
+  RUN(h, fp32 ? "assemble_f32" : "assemble_f64", 1, launch_assemble(fp32, a, tx, ty, tz, h->asm_grid, h->stream));
+  FixupArgs f = fixup_args(h, F);
+  RUN(h, "fixup", 1, launch_fixup(f, h->stream));
+  return ADS_OK;
+}
+
+// FP64 Kronecker solve: F (L0) -> out (L0 via the map tm_out)
+int enqueue_solve64(ads_handle* h, const CUtensorMap* tm_in, const CUtensorMap* tm_out, bool trans) {
+  double* const* fac = trans ? h->d_tfac64 : h->d_fac64;
+  SweepArgs ax = sweep_args(h, 0, fac[0]);
+  RUN(h, "sweep_x_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, tm_in, &h->tm_wA_out64, ax, sweep_grid(h, 0), h->stream));
+  SweepArgs ay = sweep_args(h, 1, fac[1]);
+  RUN(h, "sweep_y_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, &h->tm_wA_in64, &h->tm_wB_out64, ay, sweep_grid(h, 1), h->stream));
+  SweepArgs az = sweep_args(h, 2, fac[2]);
+  RUN(h, "sweep_z_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, &h->tm_wB_in64, tm_out, az, sweep_grid(h, 2), h->stream));
+  return ADS_OK;
+}
+
+// FP32 Kronecker solve of a double input (L0) into u: mode 1 (u = s x) or 2 (u += s x)
+int enqueue_solve32(ads_handle* h, const CUtensorMap* tm_in, const double* in_scale, const double* out_scale,
+                    int final_mode, const int* skip, const char* tag) {
+  SweepArgs ax = sweep_args(h, 0, h->d_fac32[0]);
+  ax.in_scale_dev = in_scale;
+  ax.skip_flag = skip;
+  std::string nx = std::string("sweep_x_f32") + tag, ny = std::string("sweep_y_f32") + tag,
+              nz = std::string("sweep_z_f32") + tag;
+  RUN(h, nx.c_str(), 1, launch_sweep(h->P, 0, 1, 0, false, tm_in, &h->tm_wA_out32, ax, sweep_grid(h, 0), h->stream));
+  SweepArgs ay = sweep_args(h, 1, h->d_fac32[1]);
+  ay.skip_flag = skip;
+  RUN(h, ny.c_str(), 1, launch_sweep(h->P, 1, 1, 0, false, &h->tm_wA_in32, &h->tm_wB_out32, ay, sweep_grid(h, 1), h->stream));
+  SweepArgs az = sweep_args(h, 2, h->d_fac32[2]);
+  az.out_scale_dev = out_scale;
+  az.skip_flag = skip;
+  az.out = h->d_u;
+  RUN(h, nz.c_str(), 1, launch_sweep(h->P, 1, 1, final_mode, false, &h->tm_wB_in32, &h->tm_wB_in32, az, sweep_grid(h, 2), h->stream));
+  return ADS_OK;
+}
+
+// Mixed-precision Kronecker solve of d_F into d_u with FP64 iterative refinement.
+int enqueue_solve_mixed(ads_handle* h) {
+  RUN(h, "norm_f", 2, launch_norm_f(h->d_F, h->g, h->d_part, h->norm_parts, h->d_scal, h->stream));
+  int st = enqueue_solve32(h, &h->tm_F_in64, h->d_scal + SC_IN_SCALE, h->d_scal + SC_OUT_SCALE, 1, nullptr, "");
+  if (st) return st;
+  const int* conv = h->d_flags + FL_CONV;
+  for (int k = 0; k < h->opts.max_refine; ++k) {
+    ResidualArgs ra = residual_args(h, h->d_u, h->d_F, h->d_r);
+    ra.skip_flag = conv;
+    RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
+    RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, true, h->d_scal, h->d_flags, h->stream));
+    st = enqueue_solve32(h, &h->tm_r_in64, h->d_scal + SC_C_IN, h->d_scal + SC_C_OUT, 2, conv, "_corr");
+    if (st) return st;
+  }
+  ResidualArgs ra = residual_args(h, h->d_u, h->d_F, h->d_r);
+  ra.skip_flag = conv;
+  RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
+  RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, false, h->d_scal, h->d_flags, h->stream));
+  return ADS_OK;
+}
+
+int enqueue_solve(ads_handle* h) {
+  if (h->opts.precision == ADS_PREC_MIXED) return enqueue_solve_mixed(h);
+  return enqueue_solve64(h, &h->tm_F_in64, &h->tm_u_out64, false);
+}
+
+// one Step (src/ADS.F90:437-461): FormUn+Form3DRHS, three sweeps, R := F
+int enqueue_step(ads_handle* h) {
+  RUN(h, "step_reset", 1, launch_step_reset(h->d_scal, h->d_flags, h->stream));
+  const bool f32 = h->opts.precision == ADS_PREC_MIXED;
+  int st = enqueue_assemble(h, h->d_u, h->d_F, f32, true);
+  if (st) return st;
+  st = enqueue_solve(h);
+  if (st) return st;
+  RUN(h, "record", 1, launch_record(h->d_scal, h->d_flags, h->d_hist, h->hist_cap, h->stream));
+  return ADS_OK;
+}
+
+int check_flags(ads_handle* h) {
+  int fl[FL_COUNT];
+  ADS_CUDA(h, cudaMemcpyAsync(fl, h->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, h->stream));
+  ADS_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (fl[FL_ERR] & ERRF_TMA_TIMEOUT) return fail(h, ADS_ERR_TIMEOUT, "a TMA wait timed out on the device");
+  if (fl[FL_ERR]) return fail(h, ADS_ERR_DEVICE, "a kernel reported error bits " + std::to_string(fl[FL_ERR]));
+  return ADS_OK;
+}
+
+int ensure_hist(ads_handle* h, int cap) {
+  if (cap <= h->hist_cap) return ADS_OK;
+  if (h->d_hist) cudaFree(h->d_hist);
+  h->d_hist = nullptr;
+  ADS_CUDA(h, cudaMalloc(&h->d_hist, sizeof(double) * 4 * (size_t)cap));
+  h->hist_cap = cap;
+  h->graph_valid = false;
+  return ADS_OK;
+}
+
+void invalidate_graph(ads_handle* h) {
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  h->gexec = nullptr;
+  h->graph_valid = false;
+}
+
+int build_graph(ads_handle* h) {
+  invalidate_graph(h);
+  cudaGraph_t graph = nullptr;
+  ADS_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeRelaxed));
+  const long long before = h->launches;
+  int st = enqueue_step(h);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+  if (st) { if (graph) cudaGraphDestroy(graph); return st; }
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+  h->graph_launches = h->launches - before;
+  h->launches = before;
+  e = cudaGraphInstantiate(&h->gexec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+  h->graph_valid = true;
+  return ADS_OK;
+}
+
+int finish_stats(ads_handle* h, int k, double* l2norms) {
+  int st = check_flags(h);
+  if (st) return st;
+  std::vector<double> hist((size_t)4 * k);
+  ADS_CUDA(h, cudaMemcpy(hist.data(), h->d_hist, sizeof(double) * 4 * (size_t)k, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < k; ++i)
+    if (l2norms) l2norms[i] = hist[4 * i];
+  const double* last = &hist[4 * (size_t)(k - 1)];
+  h->last.l2norm = last[0];
+  const bool mixed = h->opts.precision == ADS_PREC_MIXED;
+  h->last.rel_residual = mixed ? last[1] : 0.0;
+  h->last.refinements = mixed ? (int)last[2] : 0;
+  h->last.converged = mixed ? (int)last[3] : 1;
+  for (int i = 0; i < k; ++i)
+    if (!std::isfinite(hist[4 * i])) return fail(h, ADS_ERR_NONFINITE, "non-finite l2norm");
+  if (mixed) {
+    for (int i = 0; i < k; ++i)
+      if (hist[4 * i + 3] == 0.0)
+        return fail(h, ADS_ERR_NOCONV, "iterative refinement did not reach refine_tol (relative residual " +
+                                          std::to_string(hist[4 * i + 1]) + ")");
+  }
+  return ADS_OK;
+}
+
+int pick_zc(int E, int per_xy, int resident) {
+  int zc = E;
+  while (zc > 4 && (long long)per_xy * ((E + zc - 1) / zc) < 4LL * resident) zc = (zc + 1) / 2;
+  return zc;
+}
+
+void free_all(ads_handle* h) {
+  invalidate_graph(h);
+  for (int d = 0; d < 3; ++d) {
+    cudaFree(h->d_nn64[d]); cudaFree(h->d_jw64[d]); cudaFree(h->d_nn32[d]); cudaFree(h->d_jw32[d]);
+    cudaFree(h->d_fac64[d]); cudaFree(h->d_tfac64[d]); cudaFree(h->d_fac32[d]); cudaFree(h->d_band[d]);
+  }
+  cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_wA); cudaFree(h->d_wB);
+  cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_l2part);
+  cudaFree(h->d_part); cudaFree(h->d_scal); cudaFree(h->d_flags); cudaFree(h->d_hist);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  for (cudaEvent_t ev : h->evpool) cudaEventDestroy(ev);
+  h->evpool.clear();
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+}
+
+int create_impl(ads_handle* h) {
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  ADS_CUDA(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  h->own_stream = true;
+  ADS_CUDA(h, cudaEventCreate(&h->ev0));
+  ADS_CUDA(h, cudaEventCreate(&h->ev1));
+  if (!get_encode()) return fail(h, ADS_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+
+  for (int d = 0; d < 3; ++d) {
+    if (axis_setup(h->n[d], h->p[d], h->ax[d])) return fail(h, ADS_ERR_UNSUPPORTED, "axis setup failed");
+    if (h->ax[d].E < 2) return fail(h, ADS_ERR_UNSUPPORTED, "the GPU path needs at least 2 elements per axis");
+  }
+  Geometry& g = h->g;
+  g.P = h->P;
+  g.Q = h->Q;
+  for (int d = 0; d < 3; ++d) { g.E[d] = h->ax[d].E; g.N[d] = h->ax[d].N; }
+  for (int d = 0; d < 3; ++d)
+    if (g.N[d] > 448) return fail(h, ADS_ERR_UNSUPPORTED, "the GPU sweeps support at most 448 DOFs per axis");
+  g.PX = round_up(g.N[0], 8);
+  g.PY = round_up(g.N[1], 8);
+  g.PZ = round_up(g.N[2], 8);
+  h->n0 = (size_t)g.PX * g.N[1] * g.N[2];
+  h->n1 = (size_t)g.PY * g.N[0] * g.N[2];
+  h->n2 = (size_t)g.PZ * g.N[0] * g.N[1];
+  h->nqp = (long long)g.E[0] * g.E[1] * g.E[2] * g.Q * g.Q * g.Q;
+
+  for (int d = 0; d < 3; ++d) {
+    const AxisHost& a = h->ax[d];
+    std::vector<double> fac, tfac;
+    if (band_factor(a, fac, tfac)) return fail(h, ADS_ERR_ZERO_PIVOT, "zero pivot in the 1-D mass matrix");
+    std::vector<float> nn32(a.NN.begin(), a.NN.end()), jw32(a.JW.begin(), a.JW.end()), fac32(fac.begin(), fac.end());
+    int st;
+    if ((st = upload(h, &h->d_nn64[d], a.NN))) return st;
+    if ((st = upload(h, &h->d_jw64[d], a.JW))) return st;
+    if ((st = upload(h, &h->d_nn32[d], nn32))) return st;
+    if ((st = upload(h, &h->d_jw32[d], jw32))) return st;
+    if ((st = upload(h, &h->d_fac64[d], fac))) return st;
+    if ((st = upload(h, &h->d_tfac64[d], tfac))) return st;
+    if ((st = upload(h, &h->d_fac32[d], fac32))) return st;
+    if ((st = upload(h, &h->d_band[d], a.band))) return st;
+  }
+
+  auto zalloc = [&](double** p, size_t n) -> int {
+    ADS_CUDA(h, cudaMalloc((void**)p, sizeof(double) * std::max<size_t>(n, 1)));
+    ADS_CUDA(h, cudaMemset(*p, 0, sizeof(double) * std::max<size_t>(n, 1)));
+    return ADS_OK;
+  };
+  int st;
+  if ((st = zalloc(&h->d_u, h->n0))) return st;
+  if ((st = zalloc(&h->d_F, h->n0))) return st;
+  if ((st = zalloc(&h->d_r, h->n0))) return st;
+  if ((st = zalloc(&h->d_wA, h->n1))) return st;
+  if ((st = zalloc(&h->d_wB, h->n2))) return st;
+  if ((st = zalloc(&h->d_shadow, 7 * h->n0))) return st;
+
+  // assembly launch geometry
+  cudaDeviceProp prop;
+  ADS_CUDA(h, cudaGetDeviceProperties(&prop, h->dev));
+  const int nsm = prop.multiProcessorCount;
+  const size_t smem_max = prop.sharedMemPerMultiprocessor;
+  {
+    const bool f32 = h->opts.precision == ADS_PREC_MIXED;
+    const size_t b = assemble_smem_bytes(h->P, f32) + 1024;
+    int per_sm = (int)std::min<size_t>(smem_max / b, 2048 / AS_THREADS);
+    if (per_sm < 1) per_sm = 1;
+    const int resident = nsm * per_sm;
+    h->asm_nix = (g.E[0] + AS_TX - 1) / AS_TX;
+    h->asm_niy = (g.E[1] + AS_TY - 1) / AS_TY;
+    h->asm_zc = pick_zc(g.E[2], h->asm_nix * h->asm_niy, resident);
+    h->asm_niz = (g.E[2] + h->asm_zc - 1) / h->asm_zc;
+    const int items = h->asm_nix * h->asm_niy * h->asm_niz;
+    h->asm_grid = std::min(items, resident);
+  }
+  {
+    h->res_nix = (g.N[0] + RS_TX - 1) / RS_TX;
+    h->res_niy = (g.N[1] + RS_TY - 1) / RS_TY;
+    h->res_zc = std::min(g.N[2], 32);
+    h->res_niz = (g.N[2] + h->res_zc - 1) / h->res_zc;
+    h->res_grid = h->res_nix * h->res_niy * h->res_niz;
+  }
+  h->norm_parts = 4 * nsm;
+  h->npart = std::max(3 * h->res_grid, 2 * h->norm_parts);
+  if ((st = zalloc(&h->d_l2part, (size_t)h->asm_grid))) return st;
+  if ((st = zalloc(&h->d_part, (size_t)h->npart))) return st;
+  if ((st = zalloc(&h->d_scal, SC_COUNT))) return st;
+  ADS_CUDA(h, cudaMalloc(&h->d_flags, sizeof(int) * FL_COUNT));
+  ADS_CUDA(h, cudaMemset(h->d_flags, 0, sizeof(int) * FL_COUNT));
+  if ((st = ensure_hist(h, 64))) return st;
+
+  bool ok = true;
+  ok &= make_l0_in(h, &h->tm_F_in64, h->d_F, false);
+  ok &= make_l0_in(h, &h->tm_r_in64, h->d_r, false);
+  ok &= make_l0_out(h, &h->tm_u_out64, h->d_u, false);
+  ok &= make_l0_out(h, &h->tm_r_out64, h->d_r, false);
+  ok &= make_l1_out(h, &h->tm_wA_out64, h->d_wA, false);
+  ok &= make_l1_in(h, &h->tm_wA_in64, h->d_wA, false);
+  ok &= make_l2_out(h, &h->tm_wB_out64, h->d_wB, false);
+  ok &= make_l2_in(h, &h->tm_wB_in64, h->d_wB, false);
+  ok &= make_l1_out(h, &h->tm_wA_out32, h->d_wA, true);
+  ok &= make_l1_in(h, &h->tm_wA_in32, h->d_wA, true);
+  ok &= make_l2_out(h, &h->tm_wB_out32, h->d_wB, true);
+  ok &= make_l2_in(h, &h->tm_wB_in32, h->d_wB, true);
+  if (!ok) return fail(h, ADS_ERR_CUDA, "cuTensorMapEncodeTiled rejected a layout");
+  return ADS_OK;
+}
+
+// host <-> device copies between the packed user layouts and the padded ones
+int copy_l0_in(ads_handle* h, double* d, const double* host, cudaMemcpyKind kind) {
+  const Geometry& g = h->g;
+  ADS_CUDA(h, cudaMemcpy2DAsync(d, g.PX * 8, host, (size_t)g.N[0] * 8, (size_t)g.N[0] * 8,
+                                (size_t)g.N[1] * g.N[2], kind, h->stream));
+  return ADS_OK;
+}
+int copy_l0_out(ads_handle* h, double* host, const double* d, cudaMemcpyKind kind) {
+  const Geometry& g = h->g;
+  ADS_CUDA(h, cudaMemcpy2DAsync(host, (size_t)g.N[0] * 8, d, g.PX * 8, (size_t)g.N[0] * 8,
+                                (size_t)g.N[1] * g.N[2], kind, h->stream));
+  return ADS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ads_default_opts(ads_opts* o) {
+  if (!o) return ADS_ERR_ARG;
+  o->precision = ADS_PREC_FP64;
+  o->refine_tol = 1e-10;
+  o->max_refine = 3;
+  o->device = 0;
+  return ADS_OK;
+}
+
+const char* ads_status_string(int s) {
+  switch (s) {
+    case ADS_OK: return "ok";
+    case ADS_ERR_ARG: return "invalid argument";
+    case ADS_ERR_CUDA: return "CUDA error";
+    case ADS_ERR_ZERO_PIVOT: return "zero pivot";
+    case ADS_ERR_NONFINITE: return "non-finite value";
+    case ADS_ERR_NOCONV: return "refinement did not converge";
+    case ADS_ERR_TIMEOUT: return "device wait timed out";
+    case ADS_ERR_UNSUPPORTED: return "unsupported configuration";
+    case ADS_ERR_STATE: return "call out of order";
+    case ADS_ERR_ALLOC: return "allocation failed";
+    case ADS_ERR_DEVICE: return "device error flag";
+  }
+  return "unknown status";
+}
+
+int ads_create(const int n[3], const int p[3], const ads_opts* opts, ads_handle** out) {
+  if (!n || !p || !out) return ADS_ERR_ARG;
+  *out = nullptr;
+  for (int d = 0; d < 3; ++d)
+    if (p[d] < 0 || n[d] < p[d]) return ADS_ERR_ARG;
+  if (p[0] != p[1] || p[1] != p[2] || p[0] < 1 || p[0] > 4) return ADS_ERR_UNSUPPORTED;
+  ads_handle* h = new (std::nothrow) ads_handle();
+  if (!h) return ADS_ERR_ALLOC;
+  for (int d = 0; d < 3; ++d) { h->n[d] = n[d]; h->p[d] = p[d]; }
+  h->P = p[0];
+  h->Q = p[0] + 1;
+  if (opts) h->opts = *opts;
+  else ads_default_opts(&h->opts);
+  if (h->opts.precision != ADS_PREC_FP64 && h->opts.precision != ADS_PREC_MIXED) { delete h; return ADS_ERR_ARG; }
+  if (h->opts.max_refine < 0 || h->opts.max_refine > 16 || !(h->opts.refine_tol >= 0.0)) { delete h; return ADS_ERR_ARG; }
+  h->dev = h->opts.device;
+  int st = create_impl(h);
+  if (st) {
+    free_all(h);
+    delete h;
+    return st;
+  }
+  *out = h;
+  return ADS_OK;
+}
+
+int ads_destroy(ads_handle* h) {
+  if (!h) return ADS_ERR_ARG;
+  cudaSetDevice(h->dev);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  free_all(h);
+  delete h;
+  return ADS_OK;
+}
+
+const char* ads_last_error(const ads_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int ads_dims(const ads_handle* h, int nelem[3], int ndof[3], int nq[3]) {
+  if (!h) return ADS_ERR_ARG;
+  for (int d = 0; d < 3; ++d) {
+    if (nelem) nelem[d] = h->g.E[d];
+    if (ndof) ndof[d] = h->g.N[d];
+    if (nq) nq[d] = h->g.Q;
+  }
+  return ADS_OK;
+}
+
+int ads_qp_points(const ads_handle* h, int axis, double* X) {
+  if (!h || !X || axis < 0 || axis > 2) return ADS_ERR_ARG;
+  std::memcpy(X, h->ax[axis].X.data(), sizeof(double) * h->ax[axis].X.size());
+  return ADS_OK;
+}
+
+int ads_axis_tables(const ads_handle* h, int axis, double* U, int* O, double* J, double* W, double* NN) {
+  if (!h || axis < 0 || axis > 2) return ADS_ERR_ARG;
+  const AxisHost& a = h->ax[axis];
+  if (U) std::memcpy(U, a.U.data(), sizeof(double) * a.U.size());
+  if (O) std::memcpy(O, a.O.data(), sizeof(int) * a.O.size());
+  if (J) std::memcpy(J, a.J.data(), sizeof(double) * a.J.size());
+  if (W) std::memcpy(W, a.W.data(), sizeof(double) * a.W.size());
+  if (NN) std::memcpy(NN, a.NN.data(), sizeof(double) * a.NN.size());
+  return ADS_OK;
+}
+
+int ads_set_form(ads_handle* h, int form, const double* f_qp, const double* kappa_qp, double kappa, double dt) {
+  if (!h) return ADS_ERR_ARG;
+  if (form != ADS_FORM_PROJECT && form != ADS_FORM_HEAT) return fail(h, ADS_ERR_ARG, "unknown form");
+  if (!std::isfinite(kappa) || !std::isfinite(dt)) return fail(h, ADS_ERR_NONFINITE, "non-finite kappa or dt");
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  const size_t bytes = sizeof(double) * (size_t)h->nqp;
+  double* stage = nullptr;
+  auto load = [&](const double* src, double** dst) -> int {
+    if (!*dst) ADS_CUDA(h, cudaMalloc((void**)dst, bytes));
+    if (!stage) ADS_CUDA(h, cudaMalloc((void**)&stage, bytes));
+    ADS_CUDA(h, cudaMemcpyAsync(stage, src, bytes, cudaMemcpyHostToDevice, h->stream));
+    RUN(h, "qp_to_grid", 1, launch_qp_to_grid(stage, *dst, h->g, h->stream));
+    return ADS_OK;
+  };
+  int st = ADS_OK;
+  if (f_qp) st = load(f_qp, &h->d_fqp);
+  if (!st && kappa_qp) st = load(kappa_qp, &h->d_kqp);
+  if (!st) {
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) st = cuda_fail(h, e, "ads_set_form");
+  }
+  if (stage) cudaFree(stage);
+  if (st) return st;
+  h->form = form;
+  h->has_f = f_qp != nullptr;
+  h->has_k = (form == ADS_FORM_HEAT) && kappa_qp != nullptr;
+  h->kappa = kappa;
+  h->dt = dt;
+  h->has_form = true;
+  invalidate_graph(h);
+  return ADS_OK;
+}
+
+int ads_set_coeffs(ads_handle* h, const double* u) {
+  if (!h || !u) return ADS_ERR_ARG;
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  int st = copy_l0_in(h, h->d_u, u, cudaMemcpyHostToDevice);
+  if (st) return st;
+  ADS_CUDA(h, cudaStreamSynchronize(h->stream));
+  return ADS_OK;
+}
+
+int ads_get_coeffs(ads_handle* h, double* u) {
+  if (!h || !u) return ADS_ERR_ARG;
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  int st = copy_l0_out(h, u, h->d_u, cudaMemcpyDeviceToHost);
+  if (st) return st;
+  ADS_CUDA(h, cudaStreamSynchronize(h->stream));
+  return ADS_OK;
+}
+
+int ads_set_coeffs_device(ads_handle* h, const double* d_u) {
+  if (!h || !d_u) return ADS_ERR_ARG;
+  return copy_l0_in(h, h->d_u, d_u, cudaMemcpyDeviceToDevice);
+}
+
+int ads_get_coeffs_device(ads_handle* h, double* d_u) {
+  if (!h || !d_u) return ADS_ERR_ARG;
+  return copy_l0_out(h, d_u, h->d_u, cudaMemcpyDeviceToDevice);
+}
+
+int ads_steps(ads_handle* h, int k, double* l2norms) {
+  if (!h || k < 0) return ADS_ERR_ARG;
+  if (!h->has_form) return fail(h, ADS_ERR_STATE, "ads_set_form must be called before stepping");
+  if (k == 0) return ADS_OK;
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  int st = ensure_hist(h, std::max(k, 64));
+  if (st) return st;
+  ADS_CUDA(h, cudaMemsetAsync(h->d_flags + FL_HIST, 0, sizeof(int), h->stream));
+  if (h->timing) {
+    for (int i = 0; i < k; ++i)
+      if ((st = enqueue_step(h))) return st;
+  } else {
+    if (!h->graph_valid && (st = build_graph(h))) return st;
+    for (int i = 0; i < k; ++i) {
+      ADS_CUDA(h, cudaGraphLaunch(h->gexec, h->stream));
+      h->launches += h->graph_launches;
+    }
+  }
+  return finish_stats(h, k, l2norms);
+}
+
+int ads_step(ads_handle* h, double* l2norm) {
+  double l2 = 0.0;
+  int st = ads_steps(h, 1, &l2);
+  if (l2norm) *l2norm = l2;
+  return st;
+}
+
+int ads_get_stats(const ads_handle* h, ads_stats* s) {
+  if (!h || !s) return ADS_ERR_ARG;
+  *s = h->last;
+  return ADS_OK;
+}
+
+int ads_assemble(ads_handle* h, double* F_out, double* l2norm) {
+  if (!h || !F_out) return ADS_ERR_ARG;
+  if (!h->has_form) return fail(h, ADS_ERR_STATE, "ads_set_form must be called before assembling");
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  int st = enqueue_assemble(h, h->d_u, h->d_F, h->opts.precision == ADS_PREC_MIXED, true);
+  if (st) return st;
+  if ((st = copy_l0_out(h, F_out, h->d_F, cudaMemcpyDeviceToHost))) return st;
+  double l2 = 0.0;
+  ADS_CUDA(h, cudaMemcpyAsync(&l2, h->d_scal + SC_L2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if ((st = check_flags(h))) return st;
+  if (l2norm) *l2norm = l2;
+  return ADS_OK;
+}
+
+int ads_solve(ads_handle* h, const double* F, double* u_out) {
+  if (!h || !F) return ADS_ERR_ARG;
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  int st = copy_l0_in(h, h->d_F, F, cudaMemcpyHostToDevice);
+  if (st) return st;
+  RUN(h, "step_reset", 1, launch_step_reset(h->d_scal, h->d_flags, h->stream));
+  if ((st = enqueue_solve(h))) return st;
+  if (u_out && (st = copy_l0_out(h, u_out, h->d_u, cudaMemcpyDeviceToHost))) return st;
+  if ((st = check_flags(h))) return st;
+  double sc[SC_COUNT];
+  int fl[FL_COUNT];
+  ADS_CUDA(h, cudaMemcpy(sc, h->d_scal, sizeof(sc), cudaMemcpyDeviceToHost));
+  ADS_CUDA(h, cudaMemcpy(fl, h->d_flags, sizeof(fl), cudaMemcpyDeviceToHost));
+  const bool mixed = h->opts.precision == ADS_PREC_MIXED;
+  h->last.rel_residual = mixed ? sc[SC_RELRES] : 0.0;
+  h->last.refinements = mixed ? fl[FL_ITERS] : 0;
+  h->last.converged = mixed ? fl[FL_CONV] : 1;
+  if (mixed && !fl[FL_CONV]) return fail(h, ADS_ERR_NOCONV, "iterative refinement did not reach refine_tol");
+  return ADS_OK;
+}
+
+int ads_apply_mass(ads_handle* h, const double* u, double* out) {
+  if (!h || !u || !out) return ADS_ERR_ARG;
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  int st = copy_l0_in(h, h->d_F, u, cudaMemcpyHostToDevice);
+  if (st) return st;
+  ResidualArgs ra = residual_args(h, h->d_F, nullptr, h->d_r);
+  RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
+  if ((st = copy_l0_out(h, out, h->d_r, cudaMemcpyDeviceToHost))) return st;
+  return check_flags(h);
+}
+
+int ads_reorder(ads_handle* h, int kind, const double* in, double* out) {
+  if (!h || !in || !out) return ADS_ERR_ARG;
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  const Geometry& g = h->g;
+  const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
+  const CUtensorMap *tin, *tout;
+  double* dst;
+  int axis;
+  if (kind == ADS_REORDER_FOR_Y) {  // L0 -> L1
+    ADS_CUDA(h, cudaMemcpy2DAsync(h->d_F, g.PX * 8, in, (size_t)Nx * 8, (size_t)Nx * 8, (size_t)Ny * Nz,
+                                  cudaMemcpyHostToDevice, h->stream));
+    tin = &h->tm_F_in64; tout = &h->tm_wA_out64; dst = h->d_wA; axis = 0;
+  } else if (kind == ADS_REORDER_FOR_Z) {  // L1 -> L2
+    ADS_CUDA(h, cudaMemcpy2DAsync(h->d_wA, g.PY * 8, in, (size_t)Ny * 8, (size_t)Ny * 8, (size_t)Nx * Nz,
+                                  cudaMemcpyHostToDevice, h->stream));
+    tin = &h->tm_wA_in64; tout = &h->tm_wB_out64; dst = h->d_wB; axis = 1;
+  } else if (kind == ADS_REORDER_FOR_X) {  // L2 -> L0
+    ADS_CUDA(h, cudaMemcpy2DAsync(h->d_wB, g.PZ * 8, in, (size_t)Nz * 8, (size_t)Nz * 8, (size_t)Nx * Ny,
+                                  cudaMemcpyHostToDevice, h->stream));
+    tin = &h->tm_wB_in64; tout = &h->tm_r_out64; dst = h->d_r; axis = 2;
+  } else {
+    return fail(h, ADS_ERR_ARG, "unknown reorder kind");
+  }
+  SweepArgs a = sweep_args(h, axis, h->d_fac64[axis]);
+  RUN(h, "transpose_f64", 1, launch_sweep(h->P, 0, 0, 3, false, tin, tout, a, sweep_grid(h, axis), h->stream));
+  if (kind == ADS_REORDER_FOR_Y) {
+    ADS_CUDA(h, cudaMemcpy2DAsync(out, (size_t)Ny * 8, dst, g.PY * 8, (size_t)Ny * 8, (size_t)Nx * Nz,
+                                  cudaMemcpyDeviceToHost, h->stream));
+  } else if (kind == ADS_REORDER_FOR_Z) {
+    ADS_CUDA(h, cudaMemcpy2DAsync(out, (size_t)Nz * 8, dst, g.PZ * 8, (size_t)Nz * 8, (size_t)Nx * Ny,
+                                  cudaMemcpyDeviceToHost, h->stream));
+  } else {
+    ADS_CUDA(h, cudaMemcpy2DAsync(out, (size_t)Nx * 8, dst, g.PX * 8, (size_t)Nx * 8, (size_t)Ny * Nz,
+                                  cudaMemcpyDeviceToHost, h->stream));
+  }
+  return check_flags(h);
+}
+
+int ads_heat_adjoint(ads_handle* h, int K, int ck, const double* u0, const double* ut, double* loss,
+                     double* grad_u0, double* grad_kappa_qp) {
+  if (!h || !u0 || !ut || K < 1 || ck < 1) return ADS_ERR_ARG;
+  if (!h->has_form || h->form != ADS_FORM_HEAT) return fail(h, ADS_ERR_STATE, "the adjoint needs the HEAT form");
+  if (grad_kappa_qp && !h->has_k) return fail(h, ADS_ERR_STATE, "dL/dkappa needs a per-point kappa");
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  const size_t n0 = h->n0;
+  const int ncp = (K + ck - 1) / ck;
+  std::vector<double*> bufs;
+  auto alloc = [&](size_t n) -> double* {
+    double* p = nullptr;
+    if (cudaMalloc(&p, sizeof(double) * std::max<size_t>(n, 1)) != cudaSuccess) return nullptr;
+    cudaMemset(p, 0, sizeof(double) * std::max<size_t>(n, 1));
+    bufs.push_back(p);
+    return p;
+  };
+  auto cleanup = [&]() { for (double* p : bufs) cudaFree(p); };
+  double* cps = alloc(n0 * ncp);
+  double* seg = alloc(n0 * ck);
+  double* lam = alloc(n0);
+  double* mu = alloc(n0);
+  double* e = alloc(n0);
+  double* d_ut = alloc(n0);
+  double* gk = grad_kappa_qp ? alloc((size_t)h->nqp) : nullptr;
+  double* dpart = alloc(1024);
+  if (!cps || !seg || !lam || !mu || !e || !d_ut || !dpart || (grad_kappa_qp && !gk)) {
+    cleanup();
+    return fail(h, ADS_ERR_ALLOC, "adjoint buffers");
+  }
+  CUtensorMap tm_lam_in, tm_mu_out;
+  if (!make_l0_in(h, &tm_lam_in, lam, false) || !make_l0_out(h, &tm_mu_out, mu, false)) {
+    cleanup();
+    return fail(h, ADS_ERR_CUDA, "adjoint tensor maps");
+  }
+  int st = ADS_OK;
+  auto body = [&]() -> int {
+    int s;
+    if ((s = copy_l0_in(h, h->d_u, u0, cudaMemcpyHostToDevice))) return s;
+    if ((s = copy_l0_in(h, d_ut, ut, cudaMemcpyHostToDevice))) return s;
+    if ((s = ensure_hist(h, std::max(64, K + 1)))) return s;
+    ADS_CUDA(h, cudaMemsetAsync(h->d_flags + FL_HIST, 0, sizeof(int), h->stream));
+    // forward with checkpoints
+    for (int n = 0; n < K; ++n) {
+      if (n % ck == 0)
+        ADS_CUDA(h, cudaMemcpyAsync(cps + (size_t)(n / ck) * n0, h->d_u, sizeof(double) * n0,
+                                    cudaMemcpyDeviceToDevice, h->stream));
+      if ((s = enqueue_step(h))) return s;
+    }
+    // loss = 1/2 e^T M e, e = u^K - ut; lambda^K = M e
+    ADS_CUDA(h, cudaMemcpyAsync(e, h->d_u, sizeof(double) * n0, cudaMemcpyDeviceToDevice, h->stream));
+    RUN(h, "axpby", 1, launch_axpby(e, d_ut, -1.0, 1.0, (long long)n0, h->stream));
+    ResidualArgs ra = residual_args(h, e, nullptr, lam);
+    RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
+    RUN(h, "dot", 2, launch_dot(e, lam, (long long)n0, dpart, 512, h->d_scal + SC_DOT, h->stream));
+    double Lval = 0.0;
+    ADS_CUDA(h, cudaMemcpyAsync(&Lval, h->d_scal + SC_DOT, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    ADS_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (loss) *loss = 0.5 * Lval;
+    if (!grad_u0 && !grad_kappa_qp) return ADS_OK;
+    AxisTab<double> t64[3];
+    for (int d = 0; d < 3; ++d) { t64[d].nn = h->d_nn64[d]; t64[d].jw = h->d_jw64[d]; }
+    for (int c = ncp - 1; c >= 0; --c) {
+      const int s0 = c * ck, s1 = std::min(s0 + ck, K);
+      // recompute the segment's states u^{s0} .. u^{s1-1}
+      ADS_CUDA(h, cudaMemcpyAsync(h->d_u, cps + (size_t)c * n0, sizeof(double) * n0, cudaMemcpyDeviceToDevice, h->stream));
+      for (int n = s0; n < s1; ++n) {
+        ADS_CUDA(h, cudaMemcpyAsync(seg + (size_t)(n - s0) * n0, h->d_u, sizeof(double) * n0,
+                                    cudaMemcpyDeviceToDevice, h->stream));
+        if (n + 1 < s1 && (s = enqueue_step(h))) return s;
+      }
+      for (int n = s1 - 1; n >= s0; --n) {
+        // mu = M^{-T} lambda (transposed sweeps, FP64)
+        if ((s = enqueue_solve64(h, &tm_lam_in, &tm_mu_out, true))) return s;
+        if (gk) RUN(h, "kappa_grad", 1, launch_kappa_grad(h->g, seg + (size_t)(n - s0) * n0, mu, h->dt, gk, t64[0], t64[1], t64[2], h->stream));
+        // lambda = A^T mu: the heat operator is symmetric, so the same assembly
+        // kernels apply it (the source term does not depend on u and is left out)
+        if ((s = enqueue_assemble(h, mu, lam, false, false))) return s;
+      }
+    }
+    if (grad_u0 && (s = copy_l0_out(h, grad_u0, lam, cudaMemcpyDeviceToHost))) return s;
+    if (gk) {
+      double* qp = alloc((size_t)h->nqp);
+      if (!qp) return fail(h, ADS_ERR_ALLOC, "adjoint buffers");
+      RUN(h, "grid_to_qp", 1, launch_grid_to_qp(gk, qp, h->g, h->stream));
+      ADS_CUDA(h, cudaMemcpyAsync(grad_kappa_qp, qp, sizeof(double) * (size_t)h->nqp, cudaMemcpyDeviceToHost, h->stream));
+    }
+    return check_flags(h);
+  };
+  st = body();
+  cudaStreamSynchronize(h->stream);
+  cleanup();
+  return st;
+}
+
+int ads_axis_setup(int n, int p, double* U, int* O, double* J, double* W, double* X, double* NN,
+                   double* band, double* fac, double* tfac) {
+  if (p < 1 || p > 4) return ADS_ERR_UNSUPPORTED;
+  if (n < p) return ADS_ERR_ARG;
+  AxisHost a;
+  if (axis_setup(n, p, a)) return ADS_ERR_UNSUPPORTED;
+  if (U) std::memcpy(U, a.U.data(), sizeof(double) * a.U.size());
+  if (O) std::memcpy(O, a.O.data(), sizeof(int) * a.O.size());
+  if (J) std::memcpy(J, a.J.data(), sizeof(double) * a.J.size());
+  if (W) std::memcpy(W, a.W.data(), sizeof(double) * a.W.size());
+  if (X) std::memcpy(X, a.X.data(), sizeof(double) * a.X.size());
+  if (NN) std::memcpy(NN, a.NN.data(), sizeof(double) * a.NN.size());
+  if (band) std::memcpy(band, a.band.data(), sizeof(double) * a.band.size());
+  if (fac || tfac) {
+    std::vector<double> f, t;
+    if (band_factor(a, f, t)) return ADS_ERR_ZERO_PIVOT;
+    if (fac) std::memcpy(fac, f.data(), sizeof(double) * f.size());
+    if (tfac) std::memcpy(tfac, t.data(), sizeof(double) * t.size());
+  }
+  return ADS_OK;
+}
+
+int ads_fma_peak(int device, int fp64, double* tflops) {
+  if (!tflops) return ADS_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return ADS_ERR_CUDA;
+  double t = 0.0;
+  cudaError_t e = measure_fma_peak(fp64 != 0, &t);
+  if (e != cudaSuccess) return ADS_ERR_CUDA;
+  *tflops = t;
+  return ADS_OK;
+}
+
+void* ads_get_stream(const ads_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int ads_set_stream(ads_handle* h, void* stream) {
+  if (!h) return ADS_ERR_ARG;
+  cudaSetDevice(h->dev);
+  cudaStreamSynchronize(h->stream);
+  if (h->own_stream) cudaStreamDestroy(h->stream);
+  h->own_stream = false;
+  h->stream = (cudaStream_t)stream;
+  invalidate_graph(h);
+  return ADS_OK;
+}
+
+int ads_timing_enable(ads_handle* h, int on) {
+  if (!h) return ADS_ERR_ARG;
+  h->timing = on != 0;
+  return ADS_OK;
+}
+
+int ads_timing_reset(ads_handle* h) {
+  if (!h) return ADS_ERR_ARG;
+  resolve_timing(h);
+  h->tnames.clear(); h->tms.clear(); h->tcount.clear();
+  return ADS_OK;
+}
+
+int ads_timing_read(ads_handle* h, char* names, int names_len, double* times_ms, int* launches,
+                    int max_kernels, int* n_kernels) {
+  if (!h) return ADS_ERR_ARG;
+  resolve_timing(h);
+  const int n = (int)std::min<size_t>(h->tnames.size(), (size_t)std::max(max_kernels, 0));
+  std::string all;
+  for (int i = 0; i < n; ++i) {
+    if (i) all += ",";
+    all += h->tnames[i];
+    if (times_ms) times_ms[i] = h->tms[i];
+    if (launches) launches[i] = h->tcount[i];
+  }
+  if (names && names_len > 0) {
+    std::strncpy(names, all.c_str(), (size_t)names_len - 1);
+    names[names_len - 1] = '\0';
+  }
+  if (n_kernels) *n_kernels = n;
+  return ADS_OK;
+}
+
+long long ads_launch_count(const ads_handle* h) { return h ? h->launches : -1; }
+
+int ads_launch_count_reset(ads_handle* h) {
+  if (!h) return ADS_ERR_ARG;
+  h->launches = 0;
+  return ADS_OK;
+}
+
+}  // extern "C"

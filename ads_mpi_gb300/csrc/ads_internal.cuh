@@ -1,0 +1,197 @@
+// ads_internal.cuh — shared declarations of the GB300 ADS library.
+#pragma once
+
+#include <cuda.h>  // CUtensorMap type only; the driver entry point is fetched at run time
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include <vector>
+
+#include "../../include/ads_gpu.h"
+
+namespace ads {
+
+// ---------------------------------------------------------------------------
+// Tiling constants
+// ---------------------------------------------------------------------------
+// Assembly: a CTA owns a brick of AS_TX x AS_TY elements in x/y and streams a
+// chunk of element layers along z.  256 threads = 8 warps; in the x stage a
+// warp handles one row of AS_TX = 32 elements (one element per lane).
+constexpr int AS_TX = 32;
+constexpr int AS_TY = 8;
+constexpr int AS_THREADS = 256;
+
+// Banded sweeps: one warp solves SW_LANES lines; lines are staged through
+// shared memory in chunks of SW_CH positions (TMA boxes).
+constexpr int SW_LANES = 32;
+constexpr int SW_CH = 32;
+
+// Residual (Kronecker mat-vec) tile in x/y, streamed along z.
+constexpr int RS_TX = 32;
+constexpr int RS_TY = 8;
+constexpr int RS_THREADS = 256;
+
+// Upper bound of spin iterations of any device-side wait.
+constexpr long long WAIT_LIMIT = 1ll << 26;
+
+// error-flag bits written by kernels
+constexpr int ERRF_TMA_TIMEOUT = 1;
+constexpr int ERRF_BOUNDS = 2;
+
+// ---------------------------------------------------------------------------
+// Device-side per-axis tables
+// ---------------------------------------------------------------------------
+template <typename T>
+struct AxisTab {
+  const T* nn;   // [E][Q][P+1][2]: value (d=0) and derivative (d=1) of local function a at point k
+  const T* jw;   // [E][Q]: J(e) * W(k)
+};
+
+// Factors of the banded LU of one 1-D matrix, as rows of length N:
+//   row 0        : fs[i]     forward scale
+//   rows 1..P    : f[m][i]   forward coefficients (y_i -= f[m][i] * y_{i-m})
+//   row P+1      : bs[i]     backward scale
+//   rows P+2..2P+1: g[m][i]  backward coefficients (x_i -= g[m][i] * x_{i+m})
+// Normal solve (M = L U, no pivoting): fs = 1, f = L, bs = 1/U_ii, g = U_{i,i+m}/U_ii.
+// Transposed solve (M^T = U^T L^T):     fs = 1/U_ii, f = U_{i-m,i}/U_ii, bs = 1, g = L_{i+m,i}.
+
+// ---------------------------------------------------------------------------
+// Launch descriptors
+// ---------------------------------------------------------------------------
+struct Geometry {
+  int E[3];      // elements per axis
+  int N[3];      // DOFs per axis (E + P)
+  int P, Q;
+  long long PX, PY, PZ;  // padded pitches of the three layouts (elements)
+  // L0 index: x + PX*(y + Ny*z); L1 index: y + PY*(x + Nx*z); L2 index: z + PZ*(x + Nx*y)
+};
+
+struct AssembleArgs {
+  Geometry g;
+  int form;            // ADS_FORM_*
+  int zc;              // element layers per z-chunk
+  int nix, niy, niz;   // items per axis
+  double dt, kappa;
+  const double* u;     // L0 coefficients (FP64)
+  double* F;           // L0 output (owned DOFs)
+  double* shadow;      // 7 spill classes, each an L0-sized array
+  long long shadow_stride;
+  const double* fqp;   // qp-grid layout (qx + QX*(qy + QY*qz)), may be null
+  const double* kqp;   // same layout, may be null
+  double* l2part;      // one partial per CTA
+  int* err;
+};
+
+struct FixupArgs {
+  Geometry g;
+  int zc, nix, niy, niz;
+  double* F;
+  const double* shadow;
+  long long shadow_stride;
+  const double* l2part;
+  int nl2;
+  double* l2out;
+};
+
+struct SweepArgs {
+  int L;            // line length
+  int nchunk;       // ceil(L / SW_CH)
+  int lanes_total;  // extent of the lane dimension
+  int tiles_lane;   // ceil(lanes_total / SW_LANES)
+  int lane_dim;     // 1 or 2: which input tensor dimension carries the lanes
+  const void* fac;  // factor rows (TC), (2P+2) x L
+  double in_scale;  // multiply the input by this before the solve
+  const double* in_scale_dev;   // if set, in_scale = *in_scale_dev (refinement)
+  double out_scale;
+  const double* out_scale_dev;  // if set, out_scale = *out_scale_dev
+  const int* skip_flag;         // if set and *skip_flag != 0, the kernel returns at once
+  double* out;      // FINAL modes: L0 base
+  long long out_pitch;   // PX
+  long long out_slice;   // PX * Ny
+  int out_line_dim;      // TMA store: 1 -> coords (lanes, line, third); 2 -> (lanes, third, line)
+  int* err;
+};
+
+struct ResidualArgs {
+  Geometry g;
+  int zc, nix, niy, niz;
+  const double* u;    // L0
+  const double* F;    // L0 (may be null: plain mat-vec)
+  double* r;          // L0 output: F - M u (or M u)
+  const double* band[3];  // per axis, (2P+1) x N: band[(m+P)*N + i] = M_{i,i+m}
+  double* part;       // per CTA: [rr, ff, rmax]
+  const int* skip_flag;
+  int* err;
+};
+
+// ---------------------------------------------------------------------------
+// Kernel launchers (defined in the .cu files)
+// ---------------------------------------------------------------------------
+cudaError_t launch_assemble(bool fp32, const AssembleArgs& a, const void* tabs_x,
+                            const void* tabs_y, const void* tabs_z, int grid, cudaStream_t s);
+cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s);
+
+// kind: 0 = x sweep (L0 -> L1), 1 = y sweep (L1 -> L2), 2 = z sweep (L2 -> L0)
+// mode: 0 = TMA store to the next layout, 1 = final store to L0 (u = s*x),
+//       2 = final accumulate into L0 (u += s*x), 3 = identity transpose (no solve)
+// tin: 0 = double input, 1 = float input; tc: 0 = double compute, 1 = float compute
+cudaError_t launch_sweep(int P, int tin, int tc, int mode, bool trans, const CUtensorMap* tmin,
+                         const CUtensorMap* tmout, const SweepArgs& a, int grid, cudaStream_t s);
+
+// device scalar slots (double) and flag slots (int) of a handle
+enum ScalarSlot {
+  SC_L2 = 0,        // l2norm of the last assembly
+  SC_FF,            // ||F||_2^2
+  SC_FMAX,          // max |F|
+  SC_RR,            // ||r||_2^2 of the last residual
+  SC_RELRES,        // ||r|| / ||F|| of the last residual
+  SC_IN_SCALE,      // first solve: input scale 2^-e (max|F| ~ 2^e)
+  SC_OUT_SCALE,     // first solve: output scale 2^e
+  SC_C_IN,          // correction: input scale
+  SC_C_OUT,         // correction: output scale
+  SC_DOT,           // result of launch_dot
+  SC_COUNT = 16
+};
+enum FlagSlot {
+  FL_ERR = 0,       // error bits (ERRF_*)
+  FL_CONV,          // refinement converged
+  FL_ITERS,         // corrections applied in the current solve
+  FL_HIST,          // number of recorded steps
+  FL_COUNT = 8
+};
+
+cudaError_t launch_residual(int P, const ResidualArgs& a, int grid, cudaStream_t s);
+// reduce residual partials; sets SC_RR, SC_RELRES, FL_CONV, correction scales and
+// (if count_iter and not converged) FL_ITERS += 1.  Skipped when FL_CONV is set.
+cudaError_t launch_decide(const double* part, int n, double tol, bool count_iter, double* scal,
+                          int* flags, cudaStream_t s);
+// ||F||^2, max|F| and the first-solve scales
+cudaError_t launch_norm_f(const double* F, const Geometry& g, double* part, int nparts, double* scal,
+                          cudaStream_t s);
+cudaError_t launch_step_reset(double* scal, int* flags, cudaStream_t s);
+cudaError_t launch_record(const double* scal, int* flags, double* hist, int cap, cudaStream_t s);
+
+// layout conversions between the per-point (kx,ky,kz,ex,ey,ez) layout and the
+// quadrature grid layout qx + QX*(qy + QY*qz)
+cudaError_t launch_qp_to_grid(const double* src, double* dst, const Geometry& g, cudaStream_t s);
+cudaError_t launch_grid_to_qp(const double* src, double* dst, const Geometry& g, cudaStream_t s);
+// y = alpha*x + beta*y over n entries
+cudaError_t launch_axpby(double* y, const double* x, double alpha, double beta, long long n,
+                         cudaStream_t s);
+// out = sum x*y over n entries (deterministic two-stage)
+cudaError_t launch_dot(const double* x, const double* y, long long n, double* part, int nparts,
+                       double* out, cudaStream_t s);
+
+// adjoint: gk[q] += -dt * J W grad u(q) . grad mu(q) on the quadrature grid layout
+cudaError_t launch_kappa_grad(const Geometry& g, const double* u, const double* mu, double dt,
+                              double* gk, const AxisTab<double>& tx, const AxisTab<double>& ty,
+                              const AxisTab<double>& tz, cudaStream_t s);
+
+// FMA throughput of the FP32 or FP64 pipe (TFLOP/s, an FMA counted as 2 flops)
+cudaError_t measure_fma_peak(bool fp64, double* tflops);
+
+size_t assemble_smem_bytes(int P, bool fp32);
+size_t sweep_smem_bytes(int tin, int tc, int nchunk);
+
+}  // namespace ads

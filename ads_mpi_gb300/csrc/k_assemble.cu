@@ -1,0 +1,538 @@
+// k_assemble.cu — Gauss-quadrature right-hand-side assembly (K1).
+//
+// Replaces FormUn (src/projection_engine.F90:306-441) followed by Form3DRHS
+// (src/projection_engine.F90:154-284) with the integrands of
+// problems/heat/RHS_eq.F90:69-86 and problems/L2Projection/RHS_eq.F90:66-70.
+//
+// The reference evaluates u and grad u at every quadrature point with
+// (p+1)^3 basis products per point, stores them in Un/dUn, and then calls the
+// integrand once per (point, test function).  Here the same sums are
+// sum-factorised one direction at a time and fused into one kernel; nothing is
+// materialised per quadrature point:
+//
+//   interpolation   C[bz,by,bx] --z--> ZA,ZB --y--> Y0,Y1,Y2 --x--> u, du/dx, du/dy, du/dz
+//   integrand       g0 = JW (u + dt f),  g{1,2,3} = -dt kappa JW du/d{x,y,z}     (heat)
+//                   g0 = JW f                                                   (projection)
+//   test functions  g --x--> H0,H1,H2 --y--> I0,I1 --z--> F (accumulated in FP64)
+//
+// Work decomposition: a CTA owns a brick of AS_TX x AS_TY elements in x/y and
+// a chunk of element layers in z, which it streams layer by layer with a ring
+// of p+2 coefficient planes (prefetched with cp.async) and a ring of p+1 FP64
+// accumulator planes.  A DOF plane is complete once the layer with the same
+// index is done and is then written out.  DOFs of the brick's footprint that
+// belong to the next brick in x, y or z ("spill" DOFs, p wide) go to one of
+// seven shadow arrays instead; k_fixup adds them in a fixed order, so the
+// result is deterministic and no atomics are used.
+//
+// The integrand's l2norm (J W u^2 for heat, J W f^2 for projection; the
+// reference sums J W v u^2 over the test functions v, which is the same by the
+// partition of unity) is reduced per CTA and finished by k_fixup.
+#include "ads_internal.cuh"
+
+namespace ads {
+
+template <typename T>
+struct Tabs3 {
+  AxisTab<T> x, y, z;
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <int P, typename T>
+struct AsmLayout {
+  static constexpr int Q = P + 1;
+  static constexpr int TX = AS_TX, TY = AS_TY;
+  static constexpr int CX = TX + P, CY = TY + P;
+  static constexpr int NCOL = CX * CY;
+  static constexpr int CXP = 2 * ((CX + 1) / 2);  // even row pitch of the coefficient planes
+  static constexpr int NCOLP = CXP * CY;
+  static constexpr int QY = TY * Q;
+  static constexpr int RC = P + 2;  // coefficient ring
+  static constexpr int RF = P + 1;  // accumulator ring
+  static constexpr int NT = Q * (P + 1) * 2;  // table entries per element
+  // offsets in bytes
+  static constexpr size_t o_cring = 0;
+  static constexpr size_t o_fring = o_cring + sizeof(double) * RC * NCOLP;
+  static constexpr size_t o_za = o_fring + sizeof(double) * RF * NCOL;
+  static constexpr size_t o_zb = o_za + sizeof(T) * Q * NCOL;
+  static constexpr size_t o_y = o_zb + sizeof(T) * Q * NCOL;
+  static constexpr size_t o_h = o_y + sizeof(T) * 3 * QY * CX;
+  static constexpr size_t o_ny = o_h + sizeof(T) * 3 * QY * CX;
+  static constexpr size_t o_jwy = o_ny + sizeof(T) * TY * NT;
+  static constexpr size_t o_nz = o_jwy + sizeof(T) * TY * Q;
+  static constexpr size_t o_jwz = o_nz + sizeof(T) * NT;
+  static constexpr size_t o_red = (o_jwz + sizeof(T) * Q + 15) / 16 * 16;
+  static constexpr size_t bytes = o_red + sizeof(double) * (AS_THREADS / 32);
+};
+
+template <int P>
+__device__ __forceinline__ void issue_plane(double* ring_plane, const double* __restrict__ u,
+                                            const Geometry& g, int x0, int y0, int z) {
+  using L = AsmLayout<P, double>;
+  constexpr int PAIRS = L::CXP / 2;
+  const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
+  for (int it = threadIdx.x; it < PAIRS * L::CY; it += AS_THREADS) {
+    const int cy = it / PAIRS, pr = it % PAIRS;
+    const int cx = 2 * pr;
+    const int x = x0 + cx, y = y0 + cy;
+    int bytes = 0;
+    const double* src = u;
+    if (z < Nz && y < Ny && x < Nx) {
+      bytes = (x + 1 < Nx) ? 16 : 8;
+      src = u + (size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * z);
+    }
+    // rows have an even pitch CXP, so a pair never crosses into the next row
+    cp_async16(ring_plane + cy * L::CXP + cx, src, bytes);
+  }
+}
+
+template <int P, typename T, int FORM, bool HAS_F, bool HAS_K>
+__global__ void __launch_bounds__(AS_THREADS)
+    k_assemble(const AssembleArgs a, const Tabs3<T> tb) {
+  using L = AsmLayout<P, T>;
+  constexpr int Q = L::Q, TX = L::TX, TY = L::TY, CX = L::CX, CY = L::CY;
+  constexpr int CXP = L::CXP, NCOLP = L::NCOLP;
+  constexpr int NCOL = L::NCOL, QY = L::QY, RC = L::RC, RF = L::RF;
+  constexpr bool HEAT = (FORM == ADS_FORM_HEAT);
+
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* cring = reinterpret_cast<double*>(smem + L::o_cring);
+  double* fring = reinterpret_cast<double*>(smem + L::o_fring);
+  T* ZA = reinterpret_cast<T*>(smem + L::o_za);
+  T* ZB = reinterpret_cast<T*>(smem + L::o_zb);
+  T* Y0 = reinterpret_cast<T*>(smem + L::o_y);
+  T* Y1 = Y0 + QY * CX;
+  T* Y2 = Y1 + QY * CX;
+  T* H0 = reinterpret_cast<T*>(smem + L::o_h);
+  T* H1 = H0 + QY * CX;
+  T* H2 = H1 + QY * CX;
+  T* NYs = reinterpret_cast<T*>(smem + L::o_ny);
+  T* JWYs = reinterpret_cast<T*>(smem + L::o_jwy);
+  T* NZs = reinterpret_cast<T*>(smem + L::o_nz);
+  T* JWZs = reinterpret_cast<T*>(smem + L::o_jwz);
+  double* red = reinterpret_cast<double*>(smem + L::o_red);
+
+  const Geometry& g = a.g;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int Ex = g.E[0], Ey = g.E[1], Ez = g.E[2];
+  const int Nx = g.N[0], Ny = g.N[1];
+  const long long QXt = (long long)Ex * Q, QYt = (long long)Ey * Q;
+  const T dt = (T)a.dt;
+  const T kappa = (T)a.kappa;
+  const int nitems = a.nix * a.niy * a.niz;
+
+  double l2_thread = 0.0;
+
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const int ix = item % a.nix;
+    const int iy = (item / a.nix) % a.niy;
+    const int iz = item / (a.nix * a.niy);
+    const int x0 = ix * TX, y0 = iy * TY;
+    const int ez0 = iz * a.zc;
+    const int ez1 = min(ez0 + a.zc, Ez);
+    const bool lastx = (ix == a.nix - 1), lasty = (iy == a.niy - 1), lastz = (iz == a.niz - 1);
+
+    __syncthreads();  // previous item fully done with shared memory
+
+    // per-lane x tables (element x0 + lane)
+    T nx[Q][P + 1][2];
+    T jwx[Q];
+    {
+      const int ex = x0 + lane;
+      const bool ok = ex < Ex;
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        jwx[k] = ok ? tb.x.jw[(size_t)ex * Q + k] : T(0);
+#pragma unroll
+        for (int b = 0; b <= P; ++b) {
+          nx[k][b][0] = ok ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 0] : T(0);
+          nx[k][b][1] = ok ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 1] : T(0);
+        }
+      }
+    }
+    for (int i = tid; i < TY * L::NT; i += AS_THREADS) {
+      const int ey = y0 + i / L::NT;
+      NYs[i] = (ey < Ey) ? tb.y.nn[(size_t)ey * L::NT + (i % L::NT)] : T(0);
+    }
+    for (int i = tid; i < TY * Q; i += AS_THREADS) {
+      const int ey = y0 + i / Q;
+      JWYs[i] = (ey < Ey) ? tb.y.jw[(size_t)ey * Q + (i % Q)] : T(0);
+    }
+    for (int i = tid; i < RF * NCOL; i += AS_THREADS) fring[i] = 0.0;
+
+    // initial coefficient planes ez0 .. ez0+P
+    if (HEAT) {
+#pragma unroll
+      for (int b = 0; b <= P; ++b)
+        issue_plane<P>(cring + ((ez0 + b) % RC) * NCOLP, a.u, g, x0, y0, ez0 + b);
+    }
+    cp_async_commit();
+
+    T acc[2][P + 1];
+#pragma unroll
+    for (int s = 0; s < 2; ++s)
+#pragma unroll
+      for (int b = 0; b <= P; ++b) acc[s][b] = T(0);
+
+    for (int ez = ez0; ez < ez1; ++ez) {
+      // prefetch the plane the next layer adds
+      if (HEAT && ez + 1 < ez1) issue_plane<P>(cring + ((ez + P + 1) % RC) * NCOLP, a.u, g, x0, y0, ez + P + 1);
+      cp_async_commit();
+      // z tables of this layer
+      for (int i = tid; i < L::NT; i += AS_THREADS) NZs[i] = tb.z.nn[(size_t)ez * L::NT + i];
+      for (int i = tid; i < Q; i += AS_THREADS) JWZs[i] = tb.z.jw[(size_t)ez * Q + i];
+      cp_async_wait<1>();
+      __syncthreads();
+
+      T l2_layer = T(0);
+
+      // ---- z interpolation: ZA = sum_b Nz C, ZB = sum_b dNz C, per column ----
+      if (HEAT) {
+        for (int col = tid; col < NCOL; col += AS_THREADS) {
+          const int cy = col / CX, cx = col % CX;
+          T c[P + 1];
+#pragma unroll
+          for (int b = 0; b <= P; ++b) c[b] = (T)cring[((ez + b) % RC) * NCOLP + cy * CXP + cx];
+#pragma unroll
+          for (int kz = 0; kz < Q; ++kz) {
+            T za = T(0), zb = T(0);
+#pragma unroll
+            for (int b = 0; b <= P; ++b) {
+              za += NZs[(kz * (P + 1) + b) * 2 + 0] * c[b];
+              zb += NZs[(kz * (P + 1) + b) * 2 + 1] * c[b];
+            }
+            ZA[kz * NCOL + col] = za;
+            ZB[kz * NCOL + col] = zb;
+          }
+        }
+        __syncthreads();
+      }
+
+#pragma unroll 1
+      for (int kz = 0; kz < Q; ++kz) {
+        // ---- y interpolation ----
+        if (HEAT) {
+          for (int it = tid; it < TY * CX; it += AS_THREADS) {
+            const int ey = it / CX, cx = it % CX;
+            T za[P + 1], zb[P + 1];
+#pragma unroll
+            for (int b = 0; b <= P; ++b) {
+              za[b] = ZA[kz * NCOL + (ey + b) * CX + cx];
+              zb[b] = ZB[kz * NCOL + (ey + b) * CX + cx];
+            }
+#pragma unroll
+            for (int ky = 0; ky < Q; ++ky) {
+              T y0v = T(0), y1v = T(0), y2v = T(0);
+#pragma unroll
+              for (int b = 0; b <= P; ++b) {
+                const T nyv = NYs[ey * L::NT + (ky * (P + 1) + b) * 2 + 0];
+                const T dny = NYs[ey * L::NT + (ky * (P + 1) + b) * 2 + 1];
+                y0v += nyv * za[b];
+                y1v += dny * za[b];
+                y2v += nyv * zb[b];
+              }
+              const int qy = ey * Q + ky;
+              Y0[qy * CX + cx] = y0v;
+              Y1[qy * CX + cx] = y1v;
+              Y2[qy * CX + cx] = y2v;
+            }
+          }
+          __syncthreads();
+        }
+
+        // ---- x interpolation + integrand + x test contraction (warp per row) ----
+        for (int qy = warp; qy < QY; qy += AS_THREADS / 32) {
+          const int ey_l = qy / Q;
+          const bool elem_ok = (x0 + lane < Ex) && (y0 + ey_l < Ey);
+          const T jwyz = JWYs[qy] * JWZs[kz];
+          T h0[P + 1], h1[P + 1], h2[P + 1];
+#pragma unroll
+          for (int b = 0; b <= P; ++b) { h0[b] = T(0); h1[b] = T(0); h2[b] = T(0); }
+          T yv0[P + 1], yv1[P + 1], yv2[P + 1];
+          if (HEAT) {
+#pragma unroll
+            for (int b = 0; b <= P; ++b) {
+              yv0[b] = Y0[qy * CX + lane + b];
+              yv1[b] = Y1[qy * CX + lane + b];
+              yv2[b] = Y2[qy * CX + lane + b];
+            }
+          }
+          const long long qyg = (long long)y0 * Q + qy;
+          const long long qzg = (long long)ez * Q + kz;
+#pragma unroll
+          for (int kx = 0; kx < Q; ++kx) {
+            const T s = jwx[kx] * jwyz;
+            const long long qidx = ((long long)(x0 + lane) * Q + kx) + QXt * (qyg + QYt * qzg);
+            if (HEAT) {
+              T uu = T(0), dux = T(0), duy = T(0), duz = T(0);
+#pragma unroll
+              for (int b = 0; b <= P; ++b) {
+                uu += nx[kx][b][0] * yv0[b];
+                dux += nx[kx][b][1] * yv0[b];
+                duy += nx[kx][b][0] * yv1[b];
+                duz += nx[kx][b][0] * yv2[b];
+              }
+              T fv = T(0), kv = kappa;
+              if (HAS_F) fv = elem_ok ? (T)a.fqp[qidx] : T(0);
+              if (HAS_K) kv = elem_ok ? (T)a.kqp[qidx] : T(0);
+              const T g0 = HAS_F ? s * (uu + dt * fv) : s * uu;
+              const T c = -dt * kv * s;
+              const T g1 = c * dux, g2 = c * duy, g3 = c * duz;
+              l2_layer += s * uu * uu;
+#pragma unroll
+              for (int b = 0; b <= P; ++b) {
+                h0[b] += nx[kx][b][0] * g0 + nx[kx][b][1] * g1;
+                h1[b] += nx[kx][b][0] * g2;
+                h2[b] += nx[kx][b][0] * g3;
+              }
+            } else {
+              const T fv = (HAS_F && elem_ok) ? (T)a.fqp[qidx] : (HAS_F ? T(0) : T(1));
+              const T g0 = s * fv;
+              l2_layer += s * fv * fv;
+#pragma unroll
+              for (int b = 0; b <= P; ++b) h0[b] += nx[kx][b][0] * g0;
+            }
+          }
+          // combine the p+1 local contributions of neighbouring elements (lanes)
+          {
+            T v0 = h0[0], v1 = h1[0], v2 = h2[0];
+#pragma unroll
+            for (int b = 1; b <= P; ++b) {
+              const T s0 = __shfl_up_sync(0xffffffffu, h0[b], b);
+              const T s1 = HEAT ? __shfl_up_sync(0xffffffffu, h1[b], b) : T(0);
+              const T s2 = HEAT ? __shfl_up_sync(0xffffffffu, h2[b], b) : T(0);
+              if (lane >= b) { v0 += s0; v1 += s1; v2 += s2; }
+            }
+            H0[qy * CX + lane] = v0;
+            if (HEAT) { H1[qy * CX + lane] = v1; H2[qy * CX + lane] = v2; }
+#pragma unroll
+            for (int j = 0; j < P; ++j) {
+              T e0 = T(0), e1 = T(0), e2 = T(0);
+#pragma unroll
+              for (int b = j + 1; b <= P; ++b) {
+                e0 += __shfl_sync(0xffffffffu, h0[b], TX + j - b);
+                if (HEAT) {
+                  e1 += __shfl_sync(0xffffffffu, h1[b], TX + j - b);
+                  e2 += __shfl_sync(0xffffffffu, h2[b], TX + j - b);
+                }
+              }
+              if (lane == 0) {
+                H0[qy * CX + TX + j] = e0;
+                if (HEAT) { H1[qy * CX + TX + j] = e1; H2[qy * CX + TX + j] = e2; }
+              }
+            }
+          }
+        }
+        __syncthreads();
+
+        // ---- y test contraction + z test contraction into per-thread sums ----
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+          const int it = tid + s * AS_THREADS;
+          if (it < NCOL) {
+            const int cy = it / CX, cx = it % CX;
+            T i0 = T(0), i1 = T(0);
+            const int eylo = max(0, cy - P), eyhi = min(TY - 1, cy);
+            for (int ey = eylo; ey <= eyhi; ++ey) {
+              const int b = cy - ey;
+#pragma unroll
+              for (int ky = 0; ky < Q; ++ky) {
+                const int qy = ey * Q + ky;
+                const T nyv = NYs[ey * L::NT + (ky * (P + 1) + b) * 2 + 0];
+                if (HEAT) {
+                  const T dny = NYs[ey * L::NT + (ky * (P + 1) + b) * 2 + 1];
+                  i0 += nyv * H0[qy * CX + cx] + dny * H1[qy * CX + cx];
+                  i1 += nyv * H2[qy * CX + cx];
+                } else {
+                  i0 += nyv * H0[qy * CX + cx];
+                }
+              }
+            }
+#pragma unroll
+            for (int b = 0; b <= P; ++b) {
+              if (HEAT)
+                acc[s][b] += NZs[(kz * (P + 1) + b) * 2 + 0] * i0 + NZs[(kz * (P + 1) + b) * 2 + 1] * i1;
+              else
+                acc[s][b] += NZs[(kz * (P + 1) + b) * 2 + 0] * i0;
+            }
+          }
+        }
+        __syncthreads();
+      }  // kz
+
+      l2_thread += (double)l2_layer;
+
+      // FP64 accumulation of this layer's per-element sums into DOF planes ez..ez+P
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        const int it = tid + s * AS_THREADS;
+        if (it < NCOL) {
+#pragma unroll
+          for (int b = 0; b <= P; ++b) {
+            fring[((ez + b) % RF) * NCOL + it] += (double)acc[s][b];
+            acc[s][b] = T(0);
+          }
+        }
+      }
+      __syncthreads();
+
+      // DOF plane ez is complete: write it out and clear its ring slot
+      {
+        const int cz = ez;
+        const bool ownz = (cz < ez1) || lastz;
+        double* plane = fring + (cz % RF) * NCOL;
+        for (int it = tid; it < NCOL; it += AS_THREADS) {
+          const int cy = it / CX, cx = it % CX;
+          const int x = x0 + cx, y = y0 + cy;
+          if (x < Nx && y < Ny) {
+            const bool ownx = (cx < TX) || lastx, owny = (cy < TY) || lasty;
+            const int cls = (ownx ? 0 : 1) | (owny ? 0 : 2) | (ownz ? 0 : 4);
+            double* dst = (cls == 0) ? a.F : a.shadow + (size_t)(cls - 1) * a.shadow_stride;
+            dst[(size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * cz)] = plane[it];
+          }
+          plane[it] = 0.0;
+        }
+      }
+      __syncthreads();
+    }  // ez
+
+    // remaining planes ez1 .. ez1+P-1
+    for (int cz = ez1; cz < ez1 + P; ++cz) {
+      const bool ownz = lastz;
+      const double* plane = fring + (cz % RF) * NCOL;
+      for (int it = tid; it < NCOL; it += AS_THREADS) {
+        const int cy = it / CX, cx = it % CX;
+        const int x = x0 + cx, y = y0 + cy;
+        if (x < Nx && y < Ny && cz < g.N[2]) {
+          const bool ownx = (cx < TX) || lastx, owny = (cy < TY) || lasty;
+          const int cls = (ownx ? 0 : 1) | (owny ? 0 : 2) | (ownz ? 0 : 4);
+          double* dst = (cls == 0) ? a.F : a.shadow + (size_t)(cls - 1) * a.shadow_stride;
+          dst[(size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * cz)] = plane[it];
+        }
+      }
+    }
+    cp_async_wait<0>();
+  }  // item
+
+  // deterministic block reduction of the l2 partial
+  double v = l2_thread;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (tid == 0) {
+    double t = 0.0;
+    for (int w = 0; w < AS_THREADS / 32; ++w) t += red[w];
+    a.l2part[blockIdx.x] = t;
+  }
+}
+
+// F += shadow contributions, in class order; block 0 also finishes the l2norm.
+__global__ void k_fixup(const FixupArgs a) {
+  const Geometry& g = a.g;
+  const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
+  const long long total = (long long)Nx * Ny * Nz;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < a.nl2; ++i) t += a.l2part[i];
+    *a.l2out = t;
+  }
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(idx % Nx);
+    const int y = (int)((idx / Nx) % Ny);
+    const int z = (int)(idx / ((long long)Nx * Ny));
+    const bool zx = (x >= AS_TX) && (x % AS_TX < g.P) && (x / AS_TX <= a.nix - 1);
+    const bool zy = (y >= AS_TY) && (y % AS_TY < g.P) && (y / AS_TY <= a.niy - 1);
+    const bool zz = (z >= a.zc) && (z % a.zc < g.P) && (z / a.zc <= a.niz - 1);
+    if (!(zx || zy || zz)) continue;
+    const int zone = (zx ? 1 : 0) | (zy ? 2 : 0) | (zz ? 4 : 0);
+    const size_t o = (size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * z);
+    double v = a.F[o];
+    for (int cls = 1; cls < 8; ++cls)
+      if ((cls & zone) == cls) v += a.shadow[(size_t)(cls - 1) * a.shadow_stride + o];
+    a.F[o] = v;
+  }
+}
+
+template <int P, typename T, int FORM, bool HF, bool HK>
+static cudaError_t launch_one(const AssembleArgs& a, const void* tx, const void* ty, const void* tz,
+                              int grid, cudaStream_t s) {
+  using L = AsmLayout<P, T>;
+  Tabs3<T> tb;
+  tb.x = *static_cast<const AxisTab<T>*>(tx);
+  tb.y = *static_cast<const AxisTab<T>*>(ty);
+  tb.z = *static_cast<const AxisTab<T>*>(tz);
+  auto kern = k_assemble<P, T, FORM, HF, HK>;
+  const size_t bytes = L::bytes;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, AS_THREADS, bytes, s>>>(a, tb);
+  return cudaGetLastError();
+}
+
+template <int P, typename T>
+static cudaError_t dispatch_form(const AssembleArgs& a, const void* tx, const void* ty,
+                                 const void* tz, int grid, cudaStream_t s) {
+  const bool hf = a.fqp != nullptr, hk = a.kqp != nullptr;
+  if (a.form == ADS_FORM_PROJECT) {
+    return hf ? launch_one<P, T, ADS_FORM_PROJECT, true, false>(a, tx, ty, tz, grid, s)
+              : launch_one<P, T, ADS_FORM_PROJECT, false, false>(a, tx, ty, tz, grid, s);
+  }
+  if (hf && hk) return launch_one<P, T, ADS_FORM_HEAT, true, true>(a, tx, ty, tz, grid, s);
+  if (hf) return launch_one<P, T, ADS_FORM_HEAT, true, false>(a, tx, ty, tz, grid, s);
+  if (hk) return launch_one<P, T, ADS_FORM_HEAT, false, true>(a, tx, ty, tz, grid, s);
+  return launch_one<P, T, ADS_FORM_HEAT, false, false>(a, tx, ty, tz, grid, s);
+}
+
+template <typename T>
+static cudaError_t dispatch_p(const AssembleArgs& a, const void* tx, const void* ty, const void* tz,
+                              int grid, cudaStream_t s) {
+  switch (a.g.P) {
+    case 1: return dispatch_form<1, T>(a, tx, ty, tz, grid, s);
+    case 2: return dispatch_form<2, T>(a, tx, ty, tz, grid, s);
+    case 3: return dispatch_form<3, T>(a, tx, ty, tz, grid, s);
+    case 4: return dispatch_form<4, T>(a, tx, ty, tz, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_assemble(bool fp32, const AssembleArgs& a, const void* tx, const void* ty,
+                            const void* tz, int grid, cudaStream_t s) {
+  return fp32 ? dispatch_p<float>(a, tx, ty, tz, grid, s) : dispatch_p<double>(a, tx, ty, tz, grid, s);
+}
+
+size_t assemble_smem_bytes(int P, bool fp32) {
+  switch (P) {
+    case 1: return fp32 ? AsmLayout<1, float>::bytes : AsmLayout<1, double>::bytes;
+    case 2: return fp32 ? AsmLayout<2, float>::bytes : AsmLayout<2, double>::bytes;
+    case 3: return fp32 ? AsmLayout<3, float>::bytes : AsmLayout<3, double>::bytes;
+    case 4: return fp32 ? AsmLayout<4, float>::bytes : AsmLayout<4, double>::bytes;
+  }
+  return 0;
+}
+
+cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s) {
+  const long long total = (long long)a.g.N[0] * a.g.N[1] * a.g.N[2];
+  long long blocks = (total + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  k_fixup<<<(int)blocks, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace ads

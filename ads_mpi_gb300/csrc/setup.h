@@ -1,0 +1,25 @@
+// setup.h — host-side setup tables (knots, Gauss rule, basis tables, mass band, LU factors).
+#pragma once
+#include <vector>
+
+namespace ads {
+
+struct AxisHost {
+  int n = 0, p = 0, q = 0, E = 0, N = 0;
+  std::vector<double> U;    // n+p+2 knots
+  std::vector<int> O;       // first DOF of each element
+  std::vector<double> J;    // element Jacobians
+  std::vector<double> W;    // Gauss weights
+  std::vector<double> X;    // [E][q] Gauss points
+  std::vector<double> JW;   // [E][q] J(e) W(k)
+  std::vector<double> NN;   // [E][q][p+1][2]
+  std::vector<double> band; // [(m+p)*N + i] = M[i][i+m]
+};
+
+void open_knot(int n, int p, std::vector<double>& U);
+int gauss_legendre(int q, double* x, double* w);
+int axis_setup(int n, int p, AxisHost& a);
+// LU factors (see ads_internal.cuh) of the mass band; returns 1 on a zero pivot
+int band_factor(const AxisHost& a, std::vector<double>& fac, std::vector<double>& tfac);
+
+}  // namespace ads

@@ -1,0 +1,110 @@
+"""Seeded synthetic inputs of the benchmark configurations.
+
+No dataset is involved: every field is generated on the host in FP64 from a
+numpy ``default_rng(seed)`` and evaluated at the quadrature points, so the CPU
+oracle and the GPU path see bit-identical inputs.  Arrays use the per-point
+layout of the C-ABI, (kx,ky,kz,ex,ey,ez) column-major = numpy C-order shape
+(Ez, Ey, Ex, q, q, q).
+"""
+import numpy as np
+
+
+def projection_target(x, y, z, seed=0):
+    """L2-projection target: sin(2 pi x) sin(2 pi y) sin(2 pi z) plus
+    0.1 * sum_{k=1..8} a_k exp(-|x - c_k|^2 / 0.01), a_k ~ U(-1,1), c_k ~ U[0,1]^3."""
+    rng = np.random.default_rng(seed)
+    a = rng.uniform(-1.0, 1.0, 8)
+    c = rng.uniform(0.0, 1.0, (8, 3))
+    f = np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y) * np.sin(2 * np.pi * z)
+    for k in range(8):
+        r2 = (x - c[k, 0]) ** 2 + (y - c[k, 1]) ** 2 + (z - c[k, 2]) ** 2
+        f = f + 0.1 * a[k] * np.exp(-r2 / 0.01)
+    return np.ascontiguousarray(f, dtype=np.float64)
+
+
+def gaussian_bumps(x, y, z, seed=0, n=16, width=0.05):
+    """Heat initial state: sum of n Gaussian bumps A_i exp(-|x - c_i|^2 / (2 width^2)),
+    A_i ~ U(0,1), c_i ~ U[0.2,0.8]^3 (width is the standard deviation)."""
+    rng = np.random.default_rng(seed)
+    A = rng.uniform(0.0, 1.0, n)
+    c = rng.uniform(0.2, 0.8, (n, 3))
+    f = np.zeros(np.broadcast(x, y, z).shape)
+    for i in range(n):
+        r2 = (x - c[i, 0]) ** 2 + (y - c[i, 1]) ** 2 + (z - c[i, 2]) ** 2
+        f = f + A[i] * np.exp(-r2 / (2.0 * width * width))
+    return np.ascontiguousarray(f, dtype=np.float64)
+
+
+def gaussian_random_field(x, y, z, seed=0, sigma=0.5, corr=0.1, grid=64):
+    """Stationary Gaussian random field with squared-exponential covariance
+    sigma^2 exp(-|r|^2 / (2 corr^2)) on the periodic unit cube: white noise is
+    filtered in Fourier space on a uniform `grid`^3 mesh, normalised to variance
+    sigma^2, and evaluated at (x, y, z) by trilinear interpolation."""
+    rng = np.random.default_rng(seed)
+    noise = rng.standard_normal((grid, grid, grid))
+    k = np.fft.fftfreq(grid, d=1.0 / grid) * 2 * np.pi
+    kx, ky, kz = np.meshgrid(k, k, k, indexing="ij")
+    # square root of the spectral density of the squared-exponential kernel
+    amp = np.exp(-0.25 * corr * corr * (kx * kx + ky * ky + kz * kz))
+    g = np.real(np.fft.ifftn(np.fft.fftn(noise) * amp))
+    g = g - g.mean()
+    g = g * (sigma / g.std())
+    # trilinear interpolation on the periodic grid (cell-vertex at i/grid)
+    X = np.asarray(x) * grid
+    Y = np.asarray(y) * grid
+    Z = np.asarray(z) * grid
+    shape = np.broadcast(X, Y, Z).shape
+    X, Y, Z = (np.broadcast_to(v, shape) for v in (X, Y, Z))
+    i0 = np.floor(X).astype(np.int64)
+    j0 = np.floor(Y).astype(np.int64)
+    k0 = np.floor(Z).astype(np.int64)
+    fx, fy, fz = X - i0, Y - j0, Z - k0
+    out = np.zeros(shape)
+    for di in (0, 1):
+        wx = fx if di else 1.0 - fx
+        ii = (i0 + di) % grid
+        for dj in (0, 1):
+            wy = fy if dj else 1.0 - fy
+            jj = (j0 + dj) % grid
+            for dk in (0, 1):
+                wz = fz if dk else 1.0 - fz
+                kk = (k0 + dk) % grid
+                out += wx * wy * wz * g[ii, jj, kk]
+    return np.ascontiguousarray(out, dtype=np.float64)
+
+
+def gaussian_bumps_separable(Xx, Xy, Xz, seed=0, n=16, width=0.05, device=None):
+    """gaussian_bumps on the tensor grid of quadrature points, using that each
+    bump factors per axis: exp(-|x-c|^2/(2w^2)) = gx(x) gy(y) gz(z).  Xx, Xy, Xz
+    are the per-axis point tables (E, q); the result has the per-point layout
+    shape (Ez, Ey, Ex, q, q, q).  Uses torch on `device` when given (fast at
+    256^3), numpy otherwise; the bump parameters are drawn exactly as in
+    gaussian_bumps."""
+    rng = np.random.default_rng(seed)
+    A = rng.uniform(0.0, 1.0, n)
+    c = rng.uniform(0.2, 0.8, (n, 3))
+    s2 = 2.0 * width * width
+    if device is not None:
+        import torch
+        tx = torch.as_tensor(Xx, dtype=torch.float64, device=device)
+        ty = torch.as_tensor(Xy, dtype=torch.float64, device=device)
+        tz = torch.as_tensor(Xz, dtype=torch.float64, device=device)
+        Ez, q = tz.shape
+        Ey, Ex = ty.shape[0], tx.shape[0]
+        out = torch.zeros((Ez, Ey, Ex, q, q, q), dtype=torch.float64, device=device)
+        for i in range(n):
+            gx = torch.exp(-(tx - float(c[i, 0])) ** 2 / s2)
+            gy = torch.exp(-(ty - float(c[i, 1])) ** 2 / s2)
+            gz = torch.exp(-(tz - float(c[i, 2])) ** 2 / s2) * float(A[i])
+            yz = gz[:, None, :, None] * gy[None, :, None, :]           # (Ez, Ey, qz, qy)
+            out += yz[:, :, None, :, :, None] * gx[None, None, :, None, None, :]
+        return out.cpu().numpy()
+    Ez, q = Xz.shape
+    out = np.zeros((Xz.shape[0], Xy.shape[0], Xx.shape[0], q, q, q))
+    for i in range(n):
+        gx = np.exp(-(Xx - c[i, 0]) ** 2 / s2)
+        gy = np.exp(-(Xy - c[i, 1]) ** 2 / s2)
+        gz = np.exp(-(Xz - c[i, 2]) ** 2 / s2) * A[i]
+        yz = gz[:, None, :, None] * gy[None, :, None, :]
+        out += yz[:, :, None, :, :, None] * gx[None, None, :, None, None, :]
+    return out

@@ -1,0 +1,430 @@
+#!/usr/bin/env python3
+"""Benchmark of the explicit ADS heat step on GB300.
+
+Metric (the benchmark spec): DOF-updates/s per ADS step at 256^3 elements, p = 2,
+FP64 vs FP32 + FP64 refinement (each Kronecker solve refined to <= 1e-10
+relative residual).  Workload: heat equation, kappa = 1, dt = 1e-5, initial
+state = L2 projection of 16 seeded Gaussian bumps (synthetic, seed 0).
+
+`value` is the mixed-precision step with its state resident in HBM, timed with
+CUDA events over exactly --steps steps (graph-launched); the FP64 drop-in step
+is timed the same way and reported under "fp64".  `e2e` times the same steps
+through the C-ABI with host buffers: every step copies the coefficients in
+from pinned host memory, steps, and copies the solution back.  A separate pass
+with per-kernel CUDA events gives the roofline of the dominant kernel.
+
+--impl reference times the oracle (a C++ restatement of the reference's
+Fortran FP64 path; the Fortran itself cannot be built here) on the host cores.
+
+Multi-GPU: the step does not shard here (one GPU per ADS instance), so N > 1
+runs N independent replicas, one per rank; value = all ranks' DOF-updates
+divided by the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DOF-updates/s per ADS step, 256³ p=2: FP64 vs FP32+refine at ≤1e-10 rel err"
+UNIT = "DOF-updates/s"
+HBM_FALLBACK_GBS = 6800.0
+
+# DRAM traffic per launch of the dominant kernels from ncu captures
+# (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (kernel, workload);
+# the captures and the commands are summarised in profiles/.
+NCU_TRAFFIC = {}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--elements", type=int, default=256)
+    ap.add_argument("--degree", type=int, default=2)
+    ap.add_argument("--dt", type=float, default=1e-5)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-slab", type=int, default=32,
+                    help="reference arm: z elements of the 256x256xS sample per step")
+    return ap.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, v, device):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        try:
+            with open(path) as f:
+                return json.load(f), "measured"
+        except Exception:
+            pass
+    return None, "fallback"
+
+
+def hbm_peak():
+    peaks, src = load_peaks()
+    if peaks:
+        for k in ("hbm_gbs", "hbm_GBs", "hbm_gb_s"):
+            if k in peaks:
+                v = peaks[k]
+                if isinstance(v, dict):
+                    v = v.get("burst", v.get("value"))
+                return float(v), "of measured"
+    return HBM_FALLBACK_GBS, "of fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "50",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self, t0=None, t1=None):
+        rows = []
+        for t, line in self.lines:
+            if t0 is not None and (t < t0 or t > t1):
+                continue
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            rows.append(parts)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def algorithmic_assembly_flops(P, nelem):
+    """Flops of the sum-factorised heat assembly per launch: per element
+    interpolation (2q + 3q^2 + 4q^3)(p+1) FMA, test contraction the same,
+    and 9 flops per quadrature point for the integrand."""
+    q = P + 1
+    fma = 2 * (2 * q + 3 * q * q + 4 * q ** 3) * (P + 1)
+    return (2 * fma + 9 * q ** 3) * nelem
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    import numpy as np
+    from ads_mpi_gb300 import inputs
+    O.build()
+    E, p = args.elements, args.degree
+    S = max(2, min(args.ref_slab, E))
+    n = (E + p - 1, E + p - 1, S + p - 1)
+    o = O.Oracle(n, (p, p, p))
+    X = o.axis_tables(0)["X"]
+    Z = o.axis_tables(2)["X"]
+    u0 = inputs.gaussian_bumps_separable(X, X, Z, seed=args.seed)
+    o.step(O.FORM_PROJECT, fqp=u0)
+    for _ in range(args.warmup):
+        o.step(O.FORM_HEAT, kappa=1.0, dt=args.dt)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step(O.FORM_HEAT, kappa=1.0, dt=args.dt)
+    dt_s = time.perf_counter() - t0
+    value = o.N * args.steps / dt_s
+    cores = O.num_threads()
+    sample = (f"oracle (C++ restatement of the reference FP64 path, 1 rank, OpenMP {cores} threads) on a "
+              f"{E}x{E}x{S}-element slab of the {E}^3 p={p} heat step per step")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dt_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": f"heat {E}^3 elements p={p} dt={args.dt} kappa=1 (sample {E}x{E}x{S})",
+                   "elements": [E, E, S], "degree": p, "dofs_per_step": o.N},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def time_device_steps(torch, g, K):
+    ext = torch.cuda.ExternalStream(g.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(ext)
+    g.steps(K)
+    e1.record(ext)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def time_e2e(torch, g, K, host_in, host_out):
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        g.set_coeffs(host_in)
+        g.step()
+        g.coeffs_into(host_out)
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0
+
+
+def kernel_profile(g, K):
+    g.timing(True)
+    g.timing_reset()
+    g.steps(K)
+    t = g.timing_read()
+    g.timing(False)
+    return t
+
+
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+    import ads_mpi_gb300 as A
+    from ads_mpi_gb300 import inputs
+
+    A.load()
+    dev = local
+    torch.cuda.set_device(dev)
+    E, p = args.elements, args.degree
+    n = (E + p - 1,) * 3
+    K, W = args.steps, args.warmup
+
+    # initial state: FP64 projection of the seeded bumps
+    g64 = A.ADS(n, (p, p, p), precision=A.PREC_FP64, device=dev)
+    X = [g64.qp_points(a) for a in range(3)]
+    f = inputs.gaussian_bumps_separable(X[0], X[1], X[2], seed=args.seed, device=f"cuda:{dev}")
+    g64.set_form(A.FORM_PROJECT, f_qp=f)
+    del f
+    g64.step()
+    u0 = g64.coeffs()
+    N = g64.N
+    g64.set_form(A.FORM_HEAT, kappa=1.0, dt=args.dt)
+
+    gmx = A.ADS(n, (p, p, p), precision=A.PREC_MIXED, refine_tol=1e-10, max_refine=3, device=dev)
+    gmx.set_form(A.FORM_HEAT, kappa=1.0, dt=args.dt)
+
+    clocks = ClockSampler(dev)
+    clocks.start()
+    res = {}
+    for name, g in (("mixed", gmx), ("fp64", g64)):
+        g.set_coeffs(u0)
+        g.steps(W)
+        barrier(world)
+        g.launch_count_reset()
+        t0 = time.perf_counter()
+        secs = time_device_steps(torch, g, K)
+        t1 = time.perf_counter()
+        launches = g.launch_count()
+        st = g.stats()
+        secs = max_over_ranks(world, secs, f"cuda:{dev}")
+        res[name] = dict(secs=secs, launches=launches, stats=st, window=(t0, t1))
+    clocks.stop()
+
+    # error of the mixed step against the FP64 step, one step from the same state
+    g64.set_coeffs(u0)
+    gmx.set_coeffs(u0)
+    g64.step()
+    gmx.step()
+    a64 = g64.coeffs()
+    amx = gmx.coeffs()
+    err1 = float(np.linalg.norm(amx - a64) / np.linalg.norm(a64))
+    mixed_stats = gmx.stats()
+
+    # end to end through the C-ABI with pinned host buffers
+    host_in = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    host_out = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    host_in[:] = u0
+    e2e = {}
+    for name, g in (("mixed", gmx), ("fp64", g64)):
+        time_e2e(torch, g, min(W, 2), host_in, host_out)
+        barrier(world)
+        secs = time_e2e(torch, g, K, host_in, host_out)
+        secs = max_over_ranks(world, secs, f"cuda:{dev}")
+        e2e[name] = world * N * K / secs
+
+    # per-kernel CUDA events (a separate pass over the same steps)
+    prof = {}
+    for name, g in (("mixed", gmx), ("fp64", g64)):
+        g.set_coeffs(u0)
+        prof[name] = kernel_profile(g, K)
+
+    if rank != 0:
+        return
+
+    nelem = E ** 3
+    fp32_peak = A.fma_peak(False, dev)
+    fp64_peak = A.fma_peak(True, dev)
+    hbm, hbm_src = hbm_peak()
+
+    def roofline_for(pr, kname, steps):
+        tot, cnt = pr[kname]
+        avg = tot / max(cnt, 1) * 1e-3
+        if kname.startswith("assemble"):
+            flops = algorithmic_assembly_flops(p, nelem)
+            achieved = flops / avg / 1e12
+            peak = fp32_peak if kname.endswith("f32") else fp64_peak
+            return {"kernel": kname, "bound": "fp32" if kname.endswith("f32") else "fp64",
+                    "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                    "peak_source": "measured FMA-pipe throughput on this GPU (ads_fma_peak), live",
+                    "traffic": NCU_TRAFFIC.get((kname, f"heat{E}p{p}")),
+                    "algorithmic_flops_per_launch": flops, "avg_launch_ms": avg * 1e3}
+        s_in, s_out = 8, 8
+        if "f32" in kname:
+            s_in = 8 if kname.startswith("sweep_x") else 4
+            s_out = 8 if kname.startswith("sweep_z") else 4
+            if kname.startswith("sweep_z") and kname.endswith("_corr"):
+                s_out = 16
+        bytes_ = N * (s_in + s_out)
+        achieved = bytes_ / avg / 1e9
+        return {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_source": hbm_src, "traffic": NCU_TRAFFIC.get((kname, f"heat{E}p{p}")),
+                "algorithmic_bytes_per_launch": bytes_, "avg_launch_ms": avg * 1e3}
+
+    pm = prof["mixed"]
+    dominant = max(pm, key=lambda k: pm[k][0])
+    roof = roofline_for(pm, dominant, K)
+    sweeps = {k: roofline_for(pm, k, K) for k in pm if k.startswith("sweep") and pm[k][1] > 0}
+    p64 = prof["fp64"]
+    dom64 = max(p64, key=lambda k: p64[k][0])
+    roof64 = roofline_for(p64, dom64, K)
+
+    # CPU baseline: one oracle step at the full size on all host cores
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        o = O.Oracle(n, (p, p, p))
+        o.set_coeffs(u0)
+        t0 = time.perf_counter()
+        o.step(O.FORM_HEAT, kappa=1.0, dt=args.dt)
+        dt_s = time.perf_counter() - t0
+        cores = O.num_threads()
+        cpu = {"value": o.N / dt_s, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"one {E}^3 p={p} heat step of the oracle (C++ restatement of the reference FP64 path), "
+                         f"1 rank, OpenMP {cores} threads, {dt_s:.1f} s"}
+        o.close()
+
+    secs = res["mixed"]["secs"]
+    ck = clocks.summary(*res["mixed"]["window"]) or clocks.summary()
+    line = {
+        "metric": METRIC,
+        "value": world * N * K / secs,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": 1e3 * secs / K,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64-refine",
+        "data": "synthetic",
+        "config": {"workload": f"heat {E}^3 elements p={p} dt={args.dt} kappa=1, mixed precision "
+                               f"(FP32 assembly and sweeps, FP64 residual refinement to 1e-10)",
+                   "elements": E, "degree": p, "dofs": N, "parallelism": f"replicas{world}",
+                   "l2_flush": "inputs larger than L2 (FP64 state 137 MB; step working set > 500 MB)",
+                   "initial_state": "L2 projection of 16 seeded Gaussian bumps, seed 0"},
+        "fp64": {"value": world * N * K / res["fp64"]["secs"], "unit": UNIT,
+                 "ms_per_step": 1e3 * res["fp64"]["secs"] / K, "e2e": e2e["fp64"], "roofline": roof64,
+                 "gpu_launches": res["fp64"]["launches"]},
+        "mixed_over_fp64": res["fp64"]["secs"] / secs,
+        "mixed_rel_err_vs_fp64_one_step": err1,
+        "mixed_refinement": {"rel_residual": mixed_stats["rel_residual"], "corrections": mixed_stats["refinements"],
+                             "converged": mixed_stats["converged"], "tol": 1e-10},
+        "e2e": {"value": e2e["mixed"], "unit": UNIT, "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N + 8},
+        "roofline": roof,
+        "roofline_sweeps": sweeps,
+        "kernel_ms_per_step": {k: v[0] / K for k, v in sorted(pm.items(), key=lambda kv: -kv[1][0])},
+        "gpu_launches": res["mixed"]["launches"],
+        "cpu_baseline": cpu,
+        "clocks": ck,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

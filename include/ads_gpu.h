@@ -1,0 +1,184 @@
+/*
+ * ads_gpu.h — C-ABI of the GB300 implementation of the IGA-ADS explicit time
+ * step (macwozni/ADS_MPI).  Plain C types only; every entry point returns an
+ * int status (ADS_OK == 0) and never exits the process.
+ *
+ * Reference interface that each entry point replaces (paths are relative to the
+ * reference project):
+ *   ads_create          initialize(n, p, ads, ads_data, mierr)     src/ADS.F90:11-107
+ *   ads_destroy         Cleanup(ads, ads_data, mierr)               src/ADS.F90:802-863
+ *   ads_set_form        the RHS_fun procedure argument of Step      src/Interfaces.F90:52-81
+ *                       (integrands problems/heat/RHS_eq.F90:69-86,
+ *                        problems/L2Projection/RHS_eq.F90:66-70)
+ *   ads_step            Step(iter, RHS_fun, ads, ads_data, l2norm, mierr)  src/ADS.F90:437-461
+ *   ads_steps           the time loop of problems/heat/main.F90:49-60 (Step + MPI_Reduce)
+ *   ads_get_coeffs      ads_data%F after Step / R(:,2,2,2)          src/ADS.F90:777-779
+ *   ads_set_coeffs      R(:,2,2,2) before FormUn                    src/projection_engine.F90:412
+ *   ads_qp_points       ads%Xx/Xy/Xz (BasisData X output)           src/basis.F90:74-112
+ *   ads_axis_tables     ads%Ox,Jx,Wx,NNx (BasisData outputs)        src/basis.F90:74-112
+ *   ads_assemble        FormUn + Form3DRHS                          src/projection_engine.F90:154-441
+ *   ads_solve           the Kronecker solve of Sub_Step             src/ADS.F90:518-779
+ *   ads_reorder         ReorderRHSForY / ForZ / ForX                src/reorderRHS.F90:7-93
+ *   ads_apply_mass      (Mx (x) My (x) Mz) u with MKBBT's mass band  src/projection_engine.F90:63-132
+ *   ads_heat_adjoint    new: hand-written adjoint of the explicit heat step
+ *
+ * Layouts.  Coefficient vectors are x-fastest, u[x + Nx*(y + Ny*z)], which is
+ * the Fortran F(x, y+z*Ny) and R(:,2,2,2) of the reference.  Quadrature-point
+ * arrays use the (kx,ky,kz,ex,ey,ez) column-major layout of the reference's
+ * per-point caches (problems/oil/RHS_eq.F90:78): index
+ * kx + q*(ky + q*(kz + q*(ex + Ex*(ey + Ey*ez)))).
+ *
+ * Index convention (src/knot_vector.F90): n is the number of basis functions
+ * minus one per axis; an axis has n-p+1 elements and n+1 DOFs.
+ *
+ * Threading: a handle is used by one host thread at a time.  All device work
+ * of a handle runs on one CUDA stream (ads_get_stream / ads_set_stream); calls
+ * that return host data synchronise that stream.
+ */
+#ifndef ADS_GPU_H
+#define ADS_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* status codes */
+#define ADS_OK 0
+#define ADS_ERR_ARG 1          /* invalid argument (sizes, degree, null pointer) */
+#define ADS_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define ADS_ERR_ZERO_PIVOT 3   /* zero pivot in the banded LU factorisation */
+#define ADS_ERR_NONFINITE 4    /* non-finite value in an input or result */
+#define ADS_ERR_NOCONV 5       /* iterative refinement did not reach the tolerance */
+#define ADS_ERR_TIMEOUT 6      /* a bounded device-side wait gave up */
+#define ADS_ERR_UNSUPPORTED 7  /* valid but not supported by the GPU path (e.g. p > 4) */
+#define ADS_ERR_STATE 8        /* call out of order (no form set, ...) */
+#define ADS_ERR_ALLOC 9        /* device or host allocation failed */
+#define ADS_ERR_DEVICE 10      /* a kernel reported an error flag */
+
+/* precision of the time step */
+#define ADS_PREC_FP64 0   /* FP64 assembly and FP64 banded sweeps (the drop-in) */
+#define ADS_PREC_MIXED 1  /* FP32 assembly/sweeps, FP64 residual + refinement */
+
+/* integrand forms (replace the RHS_fun callback) */
+#define ADS_FORM_PROJECT 0  /* J W v f: L2Projection, heat at t = 0 */
+#define ADS_FORM_HEAT 1     /* J W (v u + dt (-kappa grad u . grad v + v f)): heat at t > 0 */
+
+/* 3-D permutations of ReorderRHSFor{Y,Z,X} */
+#define ADS_REORDER_FOR_Y 0 /* F(x, y+z*Ny) -> F2(y, x+z*Nx) */
+#define ADS_REORDER_FOR_Z 1 /* F2(y, x+z*Nx) -> F3(z, x+y*Nx) */
+#define ADS_REORDER_FOR_X 2 /* F3(z, x+y*Nx) -> F(x, y+z*Ny) */
+
+typedef struct ads_opts {
+  int precision;      /* ADS_PREC_FP64 or ADS_PREC_MIXED */
+  double refine_tol;  /* mixed: stop when ||F - M u||_2 <= refine_tol * ||F||_2 */
+  int max_refine;     /* mixed: maximum refinement corrections per solve */
+  int device;         /* CUDA device ordinal */
+} ads_opts;
+
+typedef struct ads_handle ads_handle;
+
+/* per-step statistics of the last ads_step / ads_steps call */
+typedef struct ads_stats {
+  double l2norm;        /* the step's l2norm (problems/heat/main.F90:53) */
+  double rel_residual;  /* final ||F - M u|| / ||F|| (mixed), 0 for FP64 */
+  int refinements;      /* corrections applied in the last solve (mixed) */
+  int converged;        /* 1 if the refinement reached refine_tol (mixed), 1 for FP64 */
+} ads_stats;
+
+int ads_default_opts(ads_opts* opts);
+
+/* initialize: n[3] = functions minus one per axis, p[3] = degrees.
+ * The GPU kernels need p[0] == p[1] == p[2] in {1,2,3,4} and >= 2 elements
+ * per axis; anything else returns ADS_ERR_UNSUPPORTED. */
+int ads_create(const int n[3], const int p[3], const ads_opts* opts, ads_handle** out);
+int ads_destroy(ads_handle* h);
+const char* ads_last_error(const ads_handle* h);
+const char* ads_status_string(int status);
+
+int ads_dims(const ads_handle* h, int nelem[3], int ndof[3], int nq[3]);
+/* X[k + q*e] for axis 0/1/2 (Gauss points of element e, BasisData's X) */
+int ads_qp_points(const ads_handle* h, int axis, double* X);
+/* knots U[n+p+2], O[E], J[E], W[q], NN[((e*q + k)*(p+1) + a)*2 + d] */
+int ads_axis_tables(const ads_handle* h, int axis, double* U, int* O, double* J, double* W,
+                    double* NN);
+
+/* Select the integrand.  f_qp: projection target (PROJECT) or source term
+ * (HEAT, may be NULL = 0).  kappa_qp: per-point conductivity (HEAT, may be
+ * NULL, then kappa is used).  Arrays are copied; the caller keeps ownership. */
+int ads_set_form(ads_handle* h, int form, const double* f_qp, const double* kappa_qp,
+                 double kappa, double dt);
+
+/* Coefficient state (host buffers, x-fastest). */
+int ads_set_coeffs(ads_handle* h, const double* u);
+int ads_get_coeffs(ads_handle* h, double* u);
+
+/* One Step: assemble with the current form from the current coefficients,
+ * Kronecker solve, store the solution as the new coefficients.  l2norm may be
+ * NULL. */
+int ads_step(ads_handle* h, double* l2norm);
+/* k Steps; l2norms (k entries) may be NULL.  Runs without host round trips. */
+int ads_steps(ads_handle* h, int k, double* l2norms);
+int ads_get_stats(const ads_handle* h, ads_stats* st);
+
+/* Parts of the step, host buffers in and out. */
+int ads_assemble(ads_handle* h, double* F_out, double* l2norm);  /* from current coeffs */
+int ads_solve(ads_handle* h, const double* F, double* u_out);    /* (Mx(x)My(x)Mz) u = F */
+int ads_apply_mass(ads_handle* h, const double* u, double* out); /* (Mx(x)My(x)Mz) u     */
+int ads_reorder(ads_handle* h, int kind, const double* in, double* out);
+
+/* Device-resident variants: pointers are device addresses of x-fastest
+ * double arrays of ndof entries (ads_set/get with copies on the handle's
+ * stream, no host synchronisation). */
+int ads_set_coeffs_device(ads_handle* h, const double* d_u);
+int ads_get_coeffs_device(ads_handle* h, double* d_u);
+
+/* Adjoint of K explicit heat steps from u0 with the current HEAT form:
+ * loss = 1/2 (u^K - u_target)^T (Mx(x)My(x)Mz) (u^K - u_target).
+ * grad_u0 (ndof) and grad_kappa_qp (quadrature-point layout; only with a
+ * per-point kappa) may be NULL.  States are checkpointed every
+ * checkpoint_every steps and recomputed segment by segment.  The forward
+ * uses the handle's precision; the backward runs in FP64. */
+int ads_heat_adjoint(ads_handle* h, int K, int checkpoint_every, const double* u0,
+                     const double* u_target, double* loss, double* grad_u0,
+                     double* grad_kappa_qp);
+
+/* Host-only setup helpers (no GPU needed): the tables ads_create builds for
+ * one axis.  U[n+p+2], O[E], J[E], W[p+1], X[E*(p+1)], NN[E*(p+1)*(p+1)*2],
+ * band[(2p+1)*(n+1)] with band[(m+p)*(n+1) + i] = M[i][i+m] (MKBBT mass
+ * matrix, src/projection_engine.F90:63-132), fac/tfac[(2p+2)*(n+1)] the LU
+ * factor rows of the normal and transposed banded solves.  Any output may be
+ * NULL.  Returns ADS_ERR_UNSUPPORTED for p outside 1..4. */
+int ads_axis_setup(int n, int p, double* U, int* O, double* J, double* W, double* X, double* NN,
+                   double* band, double* fac, double* tfac);
+
+/* Diagnostic with no counterpart in the reference: measured FMA throughput of
+ * the FP32 (fp64 = 0) or FP64 (fp64 = 1) pipe of a device, in TFLOP/s
+ * (an FMA counts as two flops).  Used as the roofline denominator of the
+ * SIMT-bound assembly kernel. */
+int ads_fma_peak(int device, int fp64, double* tflops);
+
+/* Stream interop and per-kernel timing (CUDA events on the handle's stream). */
+void* ads_get_stream(const ads_handle* h);
+int ads_set_stream(ads_handle* h, void* stream);
+int ads_timing_enable(ads_handle* h, int on);
+/* names: comma-separated kernel names; times_ms/launches: per kernel totals */
+int ads_timing_read(ads_handle* h, char* names, int names_len, double* times_ms, int* launches,
+                    int max_kernels, int* n_kernels);
+int ads_timing_reset(ads_handle* h);
+/* number of this library's kernel launches since the last reset */
+long long ads_launch_count(const ads_handle* h);
+int ads_launch_count_reset(ads_handle* h);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ADS_GPU_H */

@@ -1,0 +1,302 @@
+"""GPU parity: the CUDA path, called through the C-ABI, against the CPU oracle on
+the same seeded inputs.  FP64 results must agree to 1e-12 relative L2 (the
+bar of the FP64 drop-in); the mixed-precision path must reach its refinement
+tolerance (1e-10 relative residual) and its error against the FP64 oracle is
+checked against a stated bound."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+
+
+def make(ads_mod, E, p, prec=0, **kw):
+    if isinstance(E, int):
+        E = (E, E, E)
+    n = tuple(e + p - 1 for e in E)
+    return ads_mod.ADS(n, (p, p, p), precision=prec, **kw), n
+
+
+def oracle_for(oracle_mod, n, p):
+    return oracle_mod.Oracle(n, (p, p, p))
+
+
+# --------------------------------------------------------------------------
+# assembly (K1)
+# --------------------------------------------------------------------------
+@pytest.mark.parametrize("E,p", [((6, 5, 4), 1), ((9, 10, 7), 2), ((40, 19, 11), 2), ((35, 12, 9), 3),
+                                 ((8, 9, 6), 4), ((64, 20, 70), 2)])
+def test_heat_assembly_matches_oracle(ads_mod, oracle_mod, E, p):
+    g, n = make(ads_mod, E, p)
+    o = oracle_for(oracle_mod, n, p)
+    rng = np.random.default_rng(sum(E) + p)
+    u = rng.standard_normal(g.N)
+    g.set_coeffs(u)
+    o.set_coeffs(u)
+    g.set_form(ads_mod.FORM_HEAT, kappa=0.7, dt=1e-3)
+    F, l2 = g.assemble()
+    Fo, l2o = o.assemble(oracle_mod.FORM_HEAT, kappa=0.7, dt=1e-3)
+    assert rel_l2(F, Fo) < FP64_TOL
+    assert abs(l2 - l2o) < FP64_TOL * abs(l2o)
+
+
+@pytest.mark.parametrize("E,p", [((10, 9, 12), 2), ((33, 9, 17), 3)])
+def test_variable_kappa_and_source_assembly(ads_mod, oracle_mod, E, p):
+    g, n = make(ads_mod, E, p)
+    o = oracle_for(oracle_mod, n, p)
+    rng = np.random.default_rng(7)
+    u = rng.standard_normal(g.N)
+    kq = np.exp(0.5 * rng.standard_normal(g.nqp))
+    f = rng.standard_normal(g.nqp)
+    g.set_coeffs(u)
+    o.set_coeffs(u)
+    g.set_form(ads_mod.FORM_HEAT, f_qp=f, kappa_qp=kq, dt=2e-3)
+    F, l2 = g.assemble()
+    Fo, l2o = o.assemble(oracle_mod.FORM_HEAT, fqp=f, kappa_qp=kq, dt=2e-3)
+    assert rel_l2(F, Fo) < FP64_TOL
+    assert abs(l2 - l2o) < FP64_TOL * abs(l2o)
+
+
+@pytest.mark.parametrize("E,p", [((7, 6, 5), 2), ((34, 9, 10), 3)])
+def test_projection_assembly_matches_oracle(ads_mod, oracle_mod, E, p):
+    g, n = make(ads_mod, E, p)
+    o = oracle_for(oracle_mod, n, p)
+    f = np.random.default_rng(9).standard_normal(g.nqp)
+    g.set_form(ads_mod.FORM_PROJECT, f_qp=f)
+    F, l2 = g.assemble()
+    Fo, l2o = o.assemble(oracle_mod.FORM_PROJECT, fqp=f)
+    assert rel_l2(F, Fo) < FP64_TOL
+    assert abs(l2 - l2o) < FP64_TOL * abs(l2o)
+
+
+def test_fp32_assembly_error_bound(ads_mod, oracle_mod):
+    g, n = make(ads_mod, (20, 18, 16), 2, prec=1)
+    o = oracle_for(oracle_mod, n, 2)
+    u = np.random.default_rng(11).standard_normal(g.N)
+    g.set_coeffs(u)
+    o.set_coeffs(u)
+    g.set_form(ads_mod.FORM_HEAT, kappa=1.0, dt=1e-4)
+    F, _ = g.assemble()
+    Fo, _ = o.assemble(oracle_mod.FORM_HEAT, kappa=1.0, dt=1e-4)
+    assert rel_l2(F, Fo) < 1e-5
+
+
+# --------------------------------------------------------------------------
+# solve (K3 + K4) and the stand-alone pieces
+# --------------------------------------------------------------------------
+@pytest.mark.parametrize("E,p", [((6, 7, 8), 1), ((30, 33, 40), 2), ((17, 64, 9), 3), ((12, 11, 10), 4)])
+def test_fp64_solve_matches_oracle(ads_mod, oracle_mod, E, p):
+    g, n = make(ads_mod, E, p)
+    o = oracle_for(oracle_mod, n, p)
+    F = np.random.default_rng(13).standard_normal(g.N)
+    u = g.solve(F)
+    uo = o.solve(F)
+    assert rel_l2(u, uo) < FP64_TOL
+
+
+@pytest.mark.parametrize("E,p", [((30, 33, 40), 2), ((17, 24, 9), 3)])
+def test_mixed_solve_refines_to_tolerance(ads_mod, oracle_mod, E, p):
+    g, n = make(ads_mod, E, p, prec=1)
+    o = oracle_for(oracle_mod, n, p)
+    F = np.random.default_rng(17).standard_normal(g.N)
+    u = g.solve(F)
+    st = g.stats()
+    assert st["converged"] and st["rel_residual"] <= 1e-10
+    assert rel_l2(u, o.solve(F)) < 1e-9
+
+
+@pytest.mark.parametrize("s", [(5, 4, 3), (34, 33, 40), (70, 9, 33)])
+def test_reorders_match_reference_permutations(ads_mod, oracle_mod, s):
+    E = tuple(v - 1 for v in s)
+    g, n = make(ads_mod, E, 2)
+    F = np.random.default_rng(19).standard_normal(g.N)
+    for kind, name in ((ads_mod.REORDER_FOR_Y, "y"), (ads_mod.REORDER_FOR_Z, "z"), (ads_mod.REORDER_FOR_X, "x")):
+        out = g.reorder(kind, F)
+        assert np.array_equal(out, oracle_mod.reorder(name, g.ndof, F))
+        F = out
+
+
+def test_apply_mass_matches_oracle(ads_mod, oracle_mod):
+    g, n = make(ads_mod, (33, 10, 40), 2)
+    o = oracle_for(oracle_mod, n, 2)
+    u = np.random.default_rng(23).standard_normal(g.N)
+    assert rel_l2(g.apply_mass(u), o.apply_mass(u)) < 1e-14
+
+
+# --------------------------------------------------------------------------
+# full steps
+# --------------------------------------------------------------------------
+# the mixed path assembles in FP32, so its coefficients carry ~1e-7 relative
+# error; it is held to its refinement tolerance and to this stated bound
+MIXED_KAT_TOL = 2e-6
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_l2_projection_known_answer(ads_mod, prec):
+    """problems/L2Projection/main.F90:62,72-78 at its 32^3, p=2 size."""
+    g, _ = make(ads_mod, 32, 2, prec=prec)
+    g.set_form(ads_mod.FORM_PROJECT)
+    l2 = g.step()
+    tol = 1e-10 if prec == 0 else MIXED_KAT_TOL
+    assert abs(l2 - 1.0) < tol
+    assert np.abs(g.coeffs() - 1.0).max() < tol
+    if prec == 1:
+        assert g.stats()["rel_residual"] <= 1e-10
+
+
+def test_projection_config_matches_oracle(ads_mod, oracle_mod):
+    """The L2-projection configuration: E = 32, p = 2, seeded target."""
+    from ads_mpi_gb300 import inputs
+    g, n = make(ads_mod, 32, 2)
+    o = oracle_for(oracle_mod, n, 2)
+    f = inputs.projection_target(*g.qp_coords(), seed=0)
+    g.set_form(ads_mod.FORM_PROJECT, f_qp=f)
+    l2 = g.step()
+    l2o = o.step(oracle_mod.FORM_PROJECT, fqp=f)
+    assert rel_l2(g.coeffs(), o.coeffs()) < FP64_TOL
+    assert abs(l2 - l2o) < FP64_TOL * abs(l2o)
+
+
+def test_reference_heat_problem_trajectory(ads_mod, oracle_mod):
+    """problems/heat: projection of 2*bump3d(0.05,0.4,x) at t=0, then explicit
+    steps with kappa = 1, f = 0 (stable at E = 16, dt = 1e-5)."""
+    g, n = make(ads_mod, 16, 2)
+    o = oracle_for(oracle_mod, n, 2)
+    f0 = o.heat_initial_qp()
+    g.set_form(ads_mod.FORM_PROJECT, f_qp=f0)
+    l2g = [g.step()]
+    l2o = [o.step(oracle_mod.FORM_PROJECT, heat_initial=True)]
+    g.set_form(ads_mod.FORM_HEAT, kappa=1.0, dt=1e-5)
+    l2g += list(g.steps(20))
+    for _ in range(20):
+        l2o.append(o.step(oracle_mod.FORM_HEAT, kappa=1.0, dt=1e-5))
+    assert rel_l2(g.coeffs(), o.coeffs()) < FP64_TOL
+    assert np.abs(np.array(l2g) - np.array(l2o)).max() < FP64_TOL * max(l2o)
+
+
+@pytest.mark.parametrize("E,p,dt,K", [(24, 2, 1e-5, 10), (20, 3, 5e-6, 8), ((40, 12, 18), 2, 1e-5, 6)])
+def test_heat_steps_match_oracle(ads_mod, oracle_mod, E, p, dt, K):
+    from ads_mpi_gb300 import inputs
+    g, n = make(ads_mod, E, p)
+    o = oracle_for(oracle_mod, n, p)
+    u0 = inputs.gaussian_bumps(*g.qp_coords(), seed=1)
+    g.set_form(ads_mod.FORM_PROJECT, f_qp=u0)
+    g.step()
+    o.step(oracle_mod.FORM_PROJECT, fqp=u0)
+    g.set_form(ads_mod.FORM_HEAT, kappa=1.0, dt=dt)
+    l2g = g.steps(K)
+    l2o = [o.step(oracle_mod.FORM_HEAT, kappa=1.0, dt=dt) for _ in range(K)]
+    assert rel_l2(g.coeffs(), o.coeffs()) < FP64_TOL
+    assert np.abs(l2g - np.array(l2o)).max() < FP64_TOL * max(l2o)
+
+
+def test_heat_config_size_first_steps(ads_mod, oracle_mod):
+    """The 128^3, p=2, dt=1e-5 heat configuration: projection plus two steps
+    against the oracle (the explicit scheme is unstable at this dt, which
+    amplifies rounding differences by ~10x per step, so only the first steps
+    are compared at 1e-12)."""
+    from ads_mpi_gb300 import inputs
+    g, n = make(ads_mod, 128, 2)
+    o = oracle_for(oracle_mod, n, 2)
+    u0 = inputs.gaussian_bumps(*g.qp_coords(), seed=0)
+    g.set_form(ads_mod.FORM_PROJECT, f_qp=u0)
+    g.step()
+    o.step(oracle_mod.FORM_PROJECT, fqp=u0)
+    assert rel_l2(g.coeffs(), o.coeffs()) < FP64_TOL
+    g.set_form(ads_mod.FORM_HEAT, kappa=1.0, dt=1e-5)
+    for _ in range(2):
+        g.step()
+        o.step(oracle_mod.FORM_HEAT, kappa=1.0, dt=1e-5)
+    assert rel_l2(g.coeffs(), o.coeffs()) < FP64_TOL
+
+
+def test_mixed_heat_steps_error_bound(ads_mod, oracle_mod):
+    from ads_mpi_gb300 import inputs
+    gm, n = make(ads_mod, 24, 2, prec=1)
+    o = oracle_for(oracle_mod, n, 2)
+    u0 = inputs.gaussian_bumps(*gm.qp_coords(), seed=2)
+    gm.set_form(ads_mod.FORM_PROJECT, f_qp=u0)
+    gm.step()
+    o.step(oracle_mod.FORM_PROJECT, fqp=u0)
+    gm.set_form(ads_mod.FORM_HEAT, kappa=1.0, dt=1e-5)
+    for _ in range(5):
+        gm.step()
+        o.step(oracle_mod.FORM_HEAT, kappa=1.0, dt=1e-5)
+        st = gm.stats()
+        assert st["converged"] and st["rel_residual"] <= 1e-10
+    assert rel_l2(gm.coeffs(), o.coeffs()) < 1e-6
+
+
+def test_steps_are_deterministic(ads_mod):
+    from ads_mpi_gb300 import inputs
+    outs = []
+    for _ in range(2):
+        g, _ = make(ads_mod, (40, 20, 30), 2)
+        g.set_form(ads_mod.FORM_PROJECT, f_qp=inputs.gaussian_bumps(*g.qp_coords(), seed=3))
+        g.step()
+        g.set_form(ads_mod.FORM_HEAT, kappa=1.0, dt=1e-5)
+        g.steps(3)
+        outs.append(g.coeffs())
+        g.cleanup()
+    assert np.array_equal(outs[0], outs[1])
+
+
+# --------------------------------------------------------------------------
+# properties at the full 256^3 size (too large for the oracle)
+# --------------------------------------------------------------------------
+@pytest.mark.parametrize("prec", [0, 1])
+def test_full_size_projection_of_one(ads_mod, prec):
+    g, _ = make(ads_mod, 256, 2, prec=prec)
+    g.set_form(ads_mod.FORM_PROJECT)
+    l2 = g.step()
+    tol = 1e-10 if prec == 0 else MIXED_KAT_TOL
+    assert abs(l2 - 1.0) < tol
+    assert np.abs(g.coeffs() - 1.0).max() < tol
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_full_size_constant_state_is_steady(ads_mod, prec):
+    """grad u = 0 for u == c, so one explicit heat step returns u == c."""
+    g, _ = make(ads_mod, 256, 2, prec=prec)
+    g.set_coeffs(np.full(g.N, 2.5))
+    g.set_form(ads_mod.FORM_HEAT, kappa=1.0, dt=1e-5)
+    g.step()
+    tol = 1e-12 if prec == 0 else 2.5 * MIXED_KAT_TOL
+    assert np.abs(g.coeffs() - 2.5).max() < tol
+    if prec == 1:
+        assert g.stats()["rel_residual"] <= 1e-10
+
+
+def test_full_size_step_is_linear(ads_mod):
+    rng = np.random.default_rng(29)
+    g, _ = make(ads_mod, 256, 2)
+    g.set_form(ads_mod.FORM_HEAT, kappa=1.0, dt=1e-7)
+    a = rng.standard_normal(g.N)
+    b = rng.standard_normal(g.N)
+    res = []
+    for u in (a, b, 2.0 * a - 3.0 * b):
+        g.set_coeffs(u)
+        g.step()
+        res.append(g.coeffs())
+    assert rel_l2(res[2], 2.0 * res[0] - 3.0 * res[1]) < 1e-12
+
+
+# --------------------------------------------------------------------------
+# errors
+# --------------------------------------------------------------------------
+def test_errors_are_status_codes(ads_mod):
+    with pytest.raises(ads_mod.ADSError) as e:
+        ads_mod.ADS((10, 10, 10), (5, 5, 5))
+    assert e.value.status == 7
+    with pytest.raises(ads_mod.ADSError) as e:
+        ads_mod.ADS((10, 10, 10), (2, 3, 2))
+    assert e.value.status == 7
+    g, _ = make(ads_mod, 6, 2)
+    with pytest.raises(ads_mod.ADSError) as e:
+        g.step()
+    assert e.value.status == 8
+    with pytest.raises(ValueError):
+        g.set_coeffs(np.zeros(3))
