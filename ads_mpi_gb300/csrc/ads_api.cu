@@ -75,6 +75,7 @@ struct ads_handle {
   double* d_u = nullptr;
   double* d_F = nullptr;
   double* d_r = nullptr;
+  double* d_delta = nullptr;  // mixed: increment of the heat step
   double* d_wA = nullptr;  // L1 (double-sized; float view uses the same memory)
   double* d_wB = nullptr;  // L2
   double* d_shadow = nullptr;
@@ -308,7 +309,7 @@ ResidualArgs residual_args(const ads_handle* h, const double* u, const double* F
 }
 
 // assembly (+ fixup) of F from coefficients u with the handle's form
-int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool with_f) {
+int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool incr, bool with_f) {
   AssembleArgs a = assemble_args(h, u, F, with_f);
   AxisTab<double> t64[3];
   AxisTab<float> t32[3];
@@ -319,7 +320,7 @@ int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool 
   const void* tx = fp32 ? (const void*)&t32[0] : (const void*)&t64[0];
   const void* ty = fp32 ? (const void*)&t32[1] : (const void*)&t64[1];
   const void* tz = fp32 ? (const void*)&t32[2] : (const void*)&t64[2];
-  RUN(h, fp32 ? "assemble_f32" : "assemble_f64", 1, launch_assemble(fp32, a, tx, ty, tz, h->asm_grid, h->stream));
+  RUN(h, fp32 ? "assemble_f32" : "assemble_f64", 1, launch_assemble(fp32, incr, a, tx, ty, tz, h->asm_grid, h->stream));
   FixupArgs f = fixup_args(h, F);
   RUN(h, "fixup", 1, launch_fixup(f, h->stream));
   return ADS_OK;
@@ -337,9 +338,9 @@ int enqueue_solve64(ads_handle* h, const CUtensorMap* tm_in, const CUtensorMap* 
   return ADS_OK;
 }
 
-// FP32 Kronecker solve of a double input (L0) into u: mode 1 (u = s x) or 2 (u += s x)
+// FP32 Kronecker solve of a double input (L0) into out: mode 1 (out = s x) or 2 (out += s x)
 int enqueue_solve32(ads_handle* h, const CUtensorMap* tm_in, const double* in_scale, const double* out_scale,
-                    int final_mode, const int* skip, const char* tag) {
+                    int final_mode, const int* skip, const char* tag, double* out) {
   SweepArgs ax = sweep_args(h, 0, h->d_fac32[0]);
   ax.in_scale_dev = in_scale;
   ax.skip_flag = skip;
@@ -352,26 +353,28 @@ int enqueue_solve32(ads_handle* h, const CUtensorMap* tm_in, const double* in_sc
   SweepArgs az = sweep_args(h, 2, h->d_fac32[2]);
   az.out_scale_dev = out_scale;
   az.skip_flag = skip;
-  az.out = h->d_u;
+  az.out = out;
   RUN(h, nz.c_str(), 1, launch_sweep(h->P, 1, 1, final_mode, false, &h->tm_wB_in32, &h->tm_wB_in32, az, sweep_grid(h, 2), h->stream));
   return ADS_OK;
 }
 
-// Mixed-precision Kronecker solve of d_F into d_u with FP64 iterative refinement.
-int enqueue_solve_mixed(ads_handle* h) {
+// Mixed-precision Kronecker solve of d_F into x with FP64 iterative refinement:
+// x = M^{-1} F by FP32 sweeps, then up to max_refine corrections from the FP64
+// residual F - M x, stopping once ||F - M x|| <= refine_tol ||F||.
+int enqueue_solve_mixed(ads_handle* h, double* x) {
   RUN(h, "norm_f", 2, launch_norm_f(h->d_F, h->g, h->d_part, h->norm_parts, h->d_scal, h->stream));
-  int st = enqueue_solve32(h, &h->tm_F_in64, h->d_scal + SC_IN_SCALE, h->d_scal + SC_OUT_SCALE, 1, nullptr, "");
+  int st = enqueue_solve32(h, &h->tm_F_in64, h->d_scal + SC_IN_SCALE, h->d_scal + SC_OUT_SCALE, 1, nullptr, "", x);
   if (st) return st;
   const int* conv = h->d_flags + FL_CONV;
   for (int k = 0; k < h->opts.max_refine; ++k) {
-    ResidualArgs ra = residual_args(h, h->d_u, h->d_F, h->d_r);
+    ResidualArgs ra = residual_args(h, x, h->d_F, h->d_r);
     ra.skip_flag = conv;
     RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
     RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, true, h->d_scal, h->d_flags, h->stream));
-    st = enqueue_solve32(h, &h->tm_r_in64, h->d_scal + SC_C_IN, h->d_scal + SC_C_OUT, 2, conv, "_corr");
+    st = enqueue_solve32(h, &h->tm_r_in64, h->d_scal + SC_C_IN, h->d_scal + SC_C_OUT, 2, conv, "_corr", x);
     if (st) return st;
   }
-  ResidualArgs ra = residual_args(h, h->d_u, h->d_F, h->d_r);
+  ResidualArgs ra = residual_args(h, x, h->d_F, h->d_r);
   ra.skip_flag = conv;
   RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
   RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, false, h->d_scal, h->d_flags, h->stream));
@@ -379,18 +382,31 @@ int enqueue_solve_mixed(ads_handle* h) {
 }
 
 int enqueue_solve(ads_handle* h) {
-  if (h->opts.precision == ADS_PREC_MIXED) return enqueue_solve_mixed(h);
+  if (h->opts.precision == ADS_PREC_MIXED) return enqueue_solve_mixed(h, h->d_u);
   return enqueue_solve64(h, &h->tm_F_in64, &h->tm_u_out64, false);
 }
 
-// one Step (src/ADS.F90:437-461): FormUn+Form3DRHS, three sweeps, R := F
+// one Step (src/ADS.F90:437-461): FormUn+Form3DRHS, three sweeps, R := F.
+// FP64: assemble F, solve M u = F.
+// Mixed, heat form (increment form): with exact Gauss quadrature the mass part
+// of F is M u^n, so G = F - M u^n is assembled in FP32 from the remaining
+// terms, M delta = G is solved with FP64 refinement, and u^{n+1} = u^n + delta
+// in FP64; the FP32 rounding then scales with |delta|, not |u|.
+// Mixed, projection form (the t = 0 step): F in FP64, refined solve into u.
 int enqueue_step(ads_handle* h) {
   RUN(h, "step_reset", 1, launch_step_reset(h->d_scal, h->d_flags, h->stream));
-  const bool f32 = h->opts.precision == ADS_PREC_MIXED;
-  int st = enqueue_assemble(h, h->d_u, h->d_F, f32, true);
-  if (st) return st;
-  st = enqueue_solve(h);
-  if (st) return st;
+  int st;
+  if (h->opts.precision == ADS_PREC_MIXED && h->form == ADS_FORM_HEAT) {
+    if ((st = enqueue_assemble(h, h->d_u, h->d_F, true, true, true))) return st;
+    if ((st = enqueue_solve_mixed(h, h->d_delta))) return st;
+    RUN(h, "update", 1, launch_axpby(h->d_u, h->d_delta, 1.0, 1.0, (long long)h->n0, h->stream));
+  } else if (h->opts.precision == ADS_PREC_MIXED) {
+    if ((st = enqueue_assemble(h, h->d_u, h->d_F, false, false, true))) return st;
+    if ((st = enqueue_solve_mixed(h, h->d_u))) return st;
+  } else {
+    if ((st = enqueue_assemble(h, h->d_u, h->d_F, false, false, true))) return st;
+    if ((st = enqueue_solve64(h, &h->tm_F_in64, &h->tm_u_out64, false))) return st;
+  }
   RUN(h, "record", 1, launch_record(h->d_scal, h->d_flags, h->d_hist, h->hist_cap, h->stream));
   return ADS_OK;
 }
@@ -462,9 +478,17 @@ int finish_stats(ads_handle* h, int k, double* l2norms) {
   return ADS_OK;
 }
 
-int pick_zc(int E, int per_xy, int resident) {
+// element layers per z-chunk of the assembly: halve until there are enough
+// work items, but never below p (the z spill of a chunk, p DOF planes, must
+// lie inside the next chunk) nor below 4
+int pick_zc(int E, int per_xy, int resident, int zmin) {
   int zc = E;
-  while (zc > 4 && (long long)per_xy * ((E + zc - 1) / zc) < 4LL * resident) zc = (zc + 1) / 2;
+  while (true) {
+    const int next = (zc + 1) / 2;
+    if (next < zmin || next >= zc) break;
+    if ((long long)per_xy * ((E + zc - 1) / zc) >= 4LL * resident) break;
+    zc = next;
+  }
   return zc;
 }
 
@@ -474,7 +498,7 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_nn64[d]); cudaFree(h->d_jw64[d]); cudaFree(h->d_nn32[d]); cudaFree(h->d_jw32[d]);
     cudaFree(h->d_fac64[d]); cudaFree(h->d_tfac64[d]); cudaFree(h->d_fac32[d]); cudaFree(h->d_band[d]);
   }
-  cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_wA); cudaFree(h->d_wB);
+  cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_wA); cudaFree(h->d_wB);
   cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_l2part);
   cudaFree(h->d_part); cudaFree(h->d_scal); cudaFree(h->d_flags); cudaFree(h->d_hist);
   if (h->ev0) cudaEventDestroy(h->ev0);
@@ -535,6 +559,7 @@ int create_impl(ads_handle* h) {
   if ((st = zalloc(&h->d_u, h->n0))) return st;
   if ((st = zalloc(&h->d_F, h->n0))) return st;
   if ((st = zalloc(&h->d_r, h->n0))) return st;
+  if (h->opts.precision == ADS_PREC_MIXED && (st = zalloc(&h->d_delta, h->n0))) return st;
   if ((st = zalloc(&h->d_wA, h->n1))) return st;
   if ((st = zalloc(&h->d_wB, h->n2))) return st;
   if ((st = zalloc(&h->d_shadow, 7 * h->n0))) return st;
@@ -552,7 +577,7 @@ int create_impl(ads_handle* h) {
     const int resident = nsm * per_sm;
     h->asm_nix = (g.E[0] + AS_TX - 1) / AS_TX;
     h->asm_niy = (g.E[1] + AS_TY - 1) / AS_TY;
-    h->asm_zc = pick_zc(g.E[2], h->asm_nix * h->asm_niy, resident);
+    h->asm_zc = pick_zc(g.E[2], h->asm_nix * h->asm_niy, resident, std::max(h->P, 4));
     h->asm_niz = (g.E[2] + h->asm_zc - 1) / h->asm_zc;
     const int items = h->asm_nix * h->asm_niy * h->asm_niz;
     h->asm_grid = std::min(items, resident);
@@ -797,7 +822,7 @@ int ads_assemble(ads_handle* h, double* F_out, double* l2norm) {
   if (!h || !F_out) return ADS_ERR_ARG;
   if (!h->has_form) return fail(h, ADS_ERR_STATE, "ads_set_form must be called before assembling");
   ADS_CUDA(h, cudaSetDevice(h->dev));
-  int st = enqueue_assemble(h, h->d_u, h->d_F, h->opts.precision == ADS_PREC_MIXED, true);
+  int st = enqueue_assemble(h, h->d_u, h->d_F, h->opts.precision == ADS_PREC_MIXED, false, true);
   if (st) return st;
   if ((st = copy_l0_out(h, F_out, h->d_F, cudaMemcpyDeviceToHost))) return st;
   double l2 = 0.0;
@@ -953,7 +978,7 @@ int ads_heat_adjoint(ads_handle* h, int K, int ck, const double* u0, const doubl
         if (gk) RUN(h, "kappa_grad", 1, launch_kappa_grad(h->g, seg + (size_t)(n - s0) * n0, mu, h->dt, gk, t64[0], t64[1], t64[2], h->stream));
         // lambda = A^T mu: the heat operator is symmetric, so the same assembly
         // kernels apply it (the source term does not depend on u and is left out)
-        if ((s = enqueue_assemble(h, mu, lam, false, false))) return s;
+        if ((s = enqueue_assemble(h, mu, lam, false, false, false))) return s;
       }
     }
     if (grad_u0 && (s = copy_l0_out(h, grad_u0, lam, cudaMemcpyDeviceToHost))) return s;

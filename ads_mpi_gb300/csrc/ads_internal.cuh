@@ -128,7 +128,9 @@ struct ResidualArgs {
 // ---------------------------------------------------------------------------
 // Kernel launchers (defined in the .cu files)
 // ---------------------------------------------------------------------------
-cudaError_t launch_assemble(bool fp32, const AssembleArgs& a, const void* tabs_x,
+// incr (FP32 heat form only): leave out the mass term J W v u, i.e. assemble
+// G = F - M u instead of F
+cudaError_t launch_assemble(bool fp32, bool incr, const AssembleArgs& a, const void* tabs_x,
                             const void* tabs_y, const void* tabs_z, int grid, cudaStream_t s);
 cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s);
 

@@ -99,7 +99,7 @@ __device__ __forceinline__ void issue_plane(double* ring_plane, const double* __
   }
 }
 
-template <int P, typename T, int FORM, bool HAS_F, bool HAS_K>
+template <int P, typename T, int FORM, bool HAS_F, bool HAS_K, bool INCR>
 __global__ void __launch_bounds__(AS_THREADS)
     k_assemble(const AssembleArgs a, const Tabs3<T> tb) {
   using L = AsmLayout<P, T>;
@@ -288,7 +288,9 @@ __global__ void __launch_bounds__(AS_THREADS)
               T fv = T(0), kv = kappa;
               if (HAS_F) fv = elem_ok ? (T)a.fqp[qidx] : T(0);
               if (HAS_K) kv = elem_ok ? (T)a.kqp[qidx] : T(0);
-              const T g0 = HAS_F ? s * (uu + dt * fv) : s * uu;
+              // INCR: increment form, the mass term J W v u is left out (its
+              // exact-quadrature value M u is added back analytically)
+              const T g0 = INCR ? (HAS_F ? s * dt * fv : T(0)) : (HAS_F ? s * (uu + dt * fv) : s * uu);
               const T c = -dt * kv * s;
               const T g1 = c * dux, g2 = c * duy, g3 = c * duz;
               l2_layer += s * uu * uu;
@@ -469,7 +471,7 @@ __global__ void k_fixup(const FixupArgs a) {
   }
 }
 
-template <int P, typename T, int FORM, bool HF, bool HK>
+template <int P, typename T, int FORM, bool HF, bool HK, bool INCR>
 static cudaError_t launch_one(const AssembleArgs& a, const void* tx, const void* ty, const void* tz,
                               int grid, cudaStream_t s) {
   using L = AsmLayout<P, T>;
@@ -477,7 +479,7 @@ static cudaError_t launch_one(const AssembleArgs& a, const void* tx, const void*
   tb.x = *static_cast<const AxisTab<T>*>(tx);
   tb.y = *static_cast<const AxisTab<T>*>(ty);
   tb.z = *static_cast<const AxisTab<T>*>(tz);
-  auto kern = k_assemble<P, T, FORM, HF, HK>;
+  auto kern = k_assemble<P, T, FORM, HF, HK, INCR>;
   const size_t bytes = L::bytes;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e != cudaSuccess) return e;
@@ -485,35 +487,41 @@ static cudaError_t launch_one(const AssembleArgs& a, const void* tx, const void*
   return cudaGetLastError();
 }
 
-template <int P, typename T>
-static cudaError_t dispatch_form(const AssembleArgs& a, const void* tx, const void* ty,
-                                 const void* tz, int grid, cudaStream_t s) {
+template <int P, typename T, bool INCR>
+static cudaError_t dispatch_heat(const AssembleArgs& a, const void* tx, const void* ty, const void* tz,
+                                 int grid, cudaStream_t s) {
   const bool hf = a.fqp != nullptr, hk = a.kqp != nullptr;
-  if (a.form == ADS_FORM_PROJECT) {
-    return hf ? launch_one<P, T, ADS_FORM_PROJECT, true, false>(a, tx, ty, tz, grid, s)
-              : launch_one<P, T, ADS_FORM_PROJECT, false, false>(a, tx, ty, tz, grid, s);
-  }
-  if (hf && hk) return launch_one<P, T, ADS_FORM_HEAT, true, true>(a, tx, ty, tz, grid, s);
-  if (hf) return launch_one<P, T, ADS_FORM_HEAT, true, false>(a, tx, ty, tz, grid, s);
-  if (hk) return launch_one<P, T, ADS_FORM_HEAT, false, true>(a, tx, ty, tz, grid, s);
-  return launch_one<P, T, ADS_FORM_HEAT, false, false>(a, tx, ty, tz, grid, s);
+  if (hf && hk) return launch_one<P, T, ADS_FORM_HEAT, true, true, INCR>(a, tx, ty, tz, grid, s);
+  if (hf) return launch_one<P, T, ADS_FORM_HEAT, true, false, INCR>(a, tx, ty, tz, grid, s);
+  if (hk) return launch_one<P, T, ADS_FORM_HEAT, false, true, INCR>(a, tx, ty, tz, grid, s);
+  return launch_one<P, T, ADS_FORM_HEAT, false, false, INCR>(a, tx, ty, tz, grid, s);
 }
 
-template <typename T>
-static cudaError_t dispatch_p(const AssembleArgs& a, const void* tx, const void* ty, const void* tz,
-                              int grid, cudaStream_t s) {
+template <int P>
+static cudaError_t dispatch_form(bool fp32, bool incr, const AssembleArgs& a, const void* tx,
+                                 const void* ty, const void* tz, int grid, cudaStream_t s) {
+  const bool hf = a.fqp != nullptr;
+  if (a.form == ADS_FORM_PROJECT) {
+    if (fp32)
+      return hf ? launch_one<P, float, ADS_FORM_PROJECT, true, false, false>(a, tx, ty, tz, grid, s)
+                : launch_one<P, float, ADS_FORM_PROJECT, false, false, false>(a, tx, ty, tz, grid, s);
+    return hf ? launch_one<P, double, ADS_FORM_PROJECT, true, false, false>(a, tx, ty, tz, grid, s)
+              : launch_one<P, double, ADS_FORM_PROJECT, false, false, false>(a, tx, ty, tz, grid, s);
+  }
+  if (fp32) return incr ? dispatch_heat<P, float, true>(a, tx, ty, tz, grid, s)
+                        : dispatch_heat<P, float, false>(a, tx, ty, tz, grid, s);
+  return dispatch_heat<P, double, false>(a, tx, ty, tz, grid, s);
+}
+
+cudaError_t launch_assemble(bool fp32, bool incr, const AssembleArgs& a, const void* tx, const void* ty,
+                            const void* tz, int grid, cudaStream_t s) {
   switch (a.g.P) {
-    case 1: return dispatch_form<1, T>(a, tx, ty, tz, grid, s);
-    case 2: return dispatch_form<2, T>(a, tx, ty, tz, grid, s);
-    case 3: return dispatch_form<3, T>(a, tx, ty, tz, grid, s);
-    case 4: return dispatch_form<4, T>(a, tx, ty, tz, grid, s);
+    case 1: return dispatch_form<1>(fp32, incr, a, tx, ty, tz, grid, s);
+    case 2: return dispatch_form<2>(fp32, incr, a, tx, ty, tz, grid, s);
+    case 3: return dispatch_form<3>(fp32, incr, a, tx, ty, tz, grid, s);
+    case 4: return dispatch_form<4>(fp32, incr, a, tx, ty, tz, grid, s);
     default: return cudaErrorInvalidValue;
   }
-}
-
-cudaError_t launch_assemble(bool fp32, const AssembleArgs& a, const void* tx, const void* ty,
-                            const void* tz, int grid, cudaStream_t s) {
-  return fp32 ? dispatch_p<float>(a, tx, ty, tz, grid, s) : dispatch_p<double>(a, tx, ty, tz, grid, s);
 }
 
 size_t assemble_smem_bytes(int P, bool fp32) {

@@ -1,0 +1,145 @@
+!------------------------------------------------------------------------------
+! ads_gpu — ISO_C_BINDING interface of the GB300 ADS library (include/ads_gpu.h)
+! and drop-in style wrappers with the reference ADSS module's names.
+!
+! The reference drives the time step with
+!   call Initialize(n, p, ads, ads_data, mierr)            (src/ADS.F90:11)
+!   call Step(iter, ComputePointForRHS, ads, ads_data, l2norm, mierr)   (:437)
+!   call Cleanup(ads, ads_data, mierr)                      (:802)
+! Here the two derived types are replaced by an opaque handle, and the
+! per-point callback by an integrand form plus arrays sampled at the
+! quadrature points (GpuQpPoints gives their coordinates), because a GPU
+! kernel cannot call a Fortran procedure.  Layouts match the reference:
+! coefficients F(x, y+z*Ny) (x fastest), per-point arrays (kx,ky,kz,ex,ey,ez).
+!------------------------------------------------------------------------------
+module ads_gpu
+   use iso_c_binding
+   implicit none
+
+   integer(c_int), parameter :: ADS_OK = 0
+   integer(c_int), parameter :: ADS_PREC_FP64 = 0, ADS_PREC_MIXED = 1
+   integer(c_int), parameter :: ADS_FORM_PROJECT = 0, ADS_FORM_HEAT = 1
+
+   type, bind(c) :: ads_opts
+      integer(c_int) :: precision
+      real(c_double) :: refine_tol
+      integer(c_int) :: max_refine
+      integer(c_int) :: device
+   end type ads_opts
+
+   type :: ads_gpu_handle
+      type(c_ptr) :: h = c_null_ptr
+      integer(c_int) :: nelem(3), ndof(3), nq(3)
+   end type ads_gpu_handle
+
+   interface
+      integer(c_int) function ads_default_opts(opts) bind(c, name="ads_default_opts")
+         import :: c_int, ads_opts
+         type(ads_opts), intent(out) :: opts
+      end function
+      integer(c_int) function ads_create(n, p, opts, h) bind(c, name="ads_create")
+         import :: c_int, c_ptr, ads_opts
+         integer(c_int), intent(in) :: n(3), p(3)
+         type(ads_opts), intent(in) :: opts
+         type(c_ptr), intent(out) :: h
+      end function
+      integer(c_int) function ads_destroy(h) bind(c, name="ads_destroy")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: h
+      end function
+      integer(c_int) function ads_dims(h, nelem, ndof, nq) bind(c, name="ads_dims")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: h
+         integer(c_int), intent(out) :: nelem(3), ndof(3), nq(3)
+      end function
+      integer(c_int) function ads_qp_points(h, axis, x) bind(c, name="ads_qp_points")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         integer(c_int), value :: axis
+         real(c_double), intent(out) :: x(*)
+      end function
+      integer(c_int) function ads_set_form(h, form, f_qp, kappa_qp, kappa, dt) bind(c, name="ads_set_form")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         integer(c_int), value :: form
+         type(c_ptr), value :: f_qp, kappa_qp
+         real(c_double), value :: kappa, dt
+      end function
+      integer(c_int) function ads_set_coeffs(h, u) bind(c, name="ads_set_coeffs")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         real(c_double), intent(in) :: u(*)
+      end function
+      integer(c_int) function ads_get_coeffs(h, u) bind(c, name="ads_get_coeffs")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         real(c_double), intent(out) :: u(*)
+      end function
+      integer(c_int) function ads_step(h, l2norm) bind(c, name="ads_step")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         real(c_double), intent(out) :: l2norm
+      end function
+   end interface
+
+contains
+
+   ! Initialize (src/ADS.F90:11): n = functions minus one, p = degrees per axis.
+   subroutine GpuInitialize(n, p, precision, g, mierr)
+      integer(kind=4), intent(in) :: n(3), p(3)
+      integer(c_int), intent(in) :: precision
+      type(ads_gpu_handle), intent(out) :: g
+      integer(kind=4), intent(out) :: mierr
+      type(ads_opts) :: o
+      mierr = ads_default_opts(o)
+      o % precision = precision
+      mierr = ads_create(int(n, c_int), int(p, c_int), o, g % h)
+      if (mierr /= ADS_OK) return
+      mierr = ads_dims(g % h, g % nelem, g % ndof, g % nq)
+   end subroutine GpuInitialize
+
+   ! Gauss points of one axis, X(q, nelem) as the reference's ads % Xx.
+   subroutine GpuQpPoints(g, axis, X, mierr)
+      type(ads_gpu_handle), intent(in) :: g
+      integer(kind=4), intent(in) :: axis
+      real(c_double), intent(out) :: X(:,:)
+      integer(kind=4), intent(out) :: mierr
+      mierr = ads_qp_points(g % h, int(axis - 1, c_int), X)
+   end subroutine GpuQpPoints
+
+   ! Select the integrand; fqp/kqp are per-point arrays (kx,ky,kz,ex,ey,ez).
+   subroutine GpuSetForm(g, form, fqp, kqp, kappa, dt, mierr)
+      type(ads_gpu_handle), intent(in) :: g
+      integer(c_int), intent(in) :: form
+      real(c_double), intent(in), target, optional :: fqp(:), kqp(:)
+      real(c_double), intent(in) :: kappa, dt
+      integer(kind=4), intent(out) :: mierr
+      type(c_ptr) :: pf, pk
+      pf = c_null_ptr
+      pk = c_null_ptr
+      if (present(fqp)) pf = c_loc(fqp)
+      if (present(kqp)) pk = c_loc(kqp)
+      mierr = ads_set_form(g % h, form, pf, pk, kappa, dt)
+   end subroutine GpuSetForm
+
+   ! Step (src/ADS.F90:437); F receives the solution (ads_data % F after Step).
+   subroutine GpuStep(iter, g, F, l2norm, mierr)
+      integer(kind=4), intent(in) :: iter
+      type(ads_gpu_handle), intent(in) :: g
+      real(c_double), intent(out) :: F(:)
+      real(c_double), intent(out) :: l2norm
+      integer(kind=4), intent(out) :: mierr
+      mierr = ads_step(g % h, l2norm)
+      if (mierr /= ADS_OK) return
+      mierr = ads_get_coeffs(g % h, F)
+   end subroutine GpuStep
+
+   ! Cleanup (src/ADS.F90:802).
+   subroutine GpuCleanup(g, mierr)
+      type(ads_gpu_handle), intent(inout) :: g
+      integer(kind=4), intent(out) :: mierr
+      mierr = ads_destroy(g % h)
+      g % h = c_null_ptr
+   end subroutine GpuCleanup
+
+end module ads_gpu

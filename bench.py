@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-slab", type=int, default=32,
                     help="reference arm: z elements of the 256x256xS sample per step")
+    ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
+                    help="profiling case: set up one precision and run warmup + steps only (for ncu)")
     return ap.parse_args()
 
 
@@ -247,6 +249,27 @@ def kernel_profile(g, K):
     return t
 
 
+def run_only(args, local):
+    """Minimal case for ncu: one handle of the chosen precision, the seeded
+    initial state, --warmup + --steps eager steps, nothing else."""
+    import ads_mpi_gb300 as A
+    from ads_mpi_gb300 import inputs
+    E, p = args.elements, args.degree
+    n = (E + p - 1,) * 3
+    prec = A.PREC_MIXED if args.only == "mixed" else A.PREC_FP64
+    g = A.ADS(n, (p, p, p), precision=prec, device=local)
+    X = [g.qp_points(a) for a in range(3)]
+    f = inputs.gaussian_bumps_separable(X[0], X[1], X[2], seed=args.seed)
+    g.set_form(A.FORM_PROJECT, f_qp=f)
+    del f
+    g.step()
+    g.set_form(A.FORM_HEAT, kappa=1.0, dt=args.dt)
+    g.timing(True)  # eager launches, one kernel at a time
+    g.steps(args.warmup + args.steps)
+    t = g.timing_read()
+    print(json.dumps({"only": args.only, "elements": E, "degree": p, "kernels_ms": t}), flush=True)
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -418,6 +441,8 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.only:
+        run_only(args, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

@@ -129,9 +129,11 @@ def test_apply_mass_matches_oracle(ads_mod, oracle_mod):
 # --------------------------------------------------------------------------
 # full steps
 # --------------------------------------------------------------------------
-# the mixed path assembles in FP32, so its coefficients carry ~1e-7 relative
-# error; it is held to its refinement tolerance and to this stated bound
-MIXED_KAT_TOL = 2e-6
+# The mixed path refines each Kronecker solve to a relative residual of 1e-10;
+# with cond(Mx (x) My (x) Mz) ~ 1.2e3 at p = 2 that bounds the coefficient error
+# by ~1e-7 (the projection step is assembled in FP64, the heat steps in FP32 in
+# increment form, whose rounding scales with the increment).
+MIXED_KAT_TOL = 1e-7
 
 
 @pytest.mark.parametrize("prec", [0, 1])
@@ -227,7 +229,7 @@ def test_mixed_heat_steps_error_bound(ads_mod, oracle_mod):
         o.step(oracle_mod.FORM_HEAT, kappa=1.0, dt=1e-5)
         st = gm.stats()
         assert st["converged"] and st["rel_residual"] <= 1e-10
-    assert rel_l2(gm.coeffs(), o.coeffs()) < 1e-6
+    assert rel_l2(gm.coeffs(), o.coeffs()) < 1e-7
 
 
 def test_steps_are_deterministic(ads_mod):
@@ -264,7 +266,7 @@ def test_full_size_constant_state_is_steady(ads_mod, prec):
     g.set_coeffs(np.full(g.N, 2.5))
     g.set_form(ads_mod.FORM_HEAT, kappa=1.0, dt=1e-5)
     g.step()
-    tol = 1e-12 if prec == 0 else 2.5 * MIXED_KAT_TOL
+    tol = 1e-12 if prec == 0 else 1e-8
     assert np.abs(g.coeffs() - 2.5).max() < tol
     if prec == 1:
         assert g.stats()["rel_residual"] <= 1e-10
