@@ -243,9 +243,10 @@ SweepArgs sweep_args(const ads_handle* h, int axis, const void* fac) {
   const int* N = h->g.N;
   a.L = N[axis];
   a.nchunk = (a.L + SW_CH - 1) / SW_CH;
-  if (axis == 0) { a.lanes_total = N[1]; a.lane_dim = 1; a.out_line_dim = 1; }
-  if (axis == 1) { a.lanes_total = N[2]; a.lane_dim = 2; a.out_line_dim = 2; }
-  if (axis == 2) { a.lanes_total = N[0]; a.lane_dim = 1; a.out_line_dim = 2; }
+  if (axis == 0) { a.lanes_total = N[1]; a.lane_dim = 1; a.out_line_dim = 1; a.third_extent = N[2]; }
+  if (axis == 1) { a.lanes_total = N[2]; a.lane_dim = 2; a.out_line_dim = 2; a.third_extent = N[0]; }
+  if (axis == 2) { a.lanes_total = N[0]; a.lane_dim = 1; a.out_line_dim = 2; a.third_extent = N[1]; }
+  a.out_third_extent = a.third_extent;
   a.tiles_lane = (a.lanes_total + SW_LANES - 1) / SW_LANES;
   a.fac = fac;
   a.in_scale = 1.0;
@@ -292,7 +293,7 @@ FixupArgs fixup_args(const ads_handle* h, double* F) {
   f.shadow_stride = (long long)h->n0;
   f.l2part = h->d_l2part;
   f.nl2 = h->asm_grid;
-  f.l2out = h->d_scal + SC_L2;
+  f.scal = h->d_scal;
   return f;
 }
 
@@ -361,8 +362,9 @@ int enqueue_solve32(ads_handle* h, const CUtensorMap* tm_in, const double* in_sc
 // Mixed-precision Kronecker solve of d_F into x with FP64 iterative refinement:
 // x = M^{-1} F by FP32 sweeps, then up to max_refine corrections from the FP64
 // residual F - M x, stopping once ||F - M x|| <= refine_tol ||F||.
-int enqueue_solve_mixed(ads_handle* h, double* x) {
-  RUN(h, "norm_f", 2, launch_norm_f(h->d_F, h->g, h->d_part, h->norm_parts, h->d_scal, h->stream));
+int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready) {
+  // the first solve's scale comes from the assembly (fixup) or, for a caller's F, from a norm pass
+  if (!scales_ready) RUN(h, "norm_f", 2, launch_norm_f(h->d_F, h->g, h->d_part, h->norm_parts, h->d_scal, h->stream));
   int st = enqueue_solve32(h, &h->tm_F_in64, h->d_scal + SC_IN_SCALE, h->d_scal + SC_OUT_SCALE, 1, nullptr, "", x);
   if (st) return st;
   const int* conv = h->d_flags + FL_CONV;
@@ -382,7 +384,7 @@ int enqueue_solve_mixed(ads_handle* h, double* x) {
 }
 
 int enqueue_solve(ads_handle* h) {
-  if (h->opts.precision == ADS_PREC_MIXED) return enqueue_solve_mixed(h, h->d_u);
+  if (h->opts.precision == ADS_PREC_MIXED) return enqueue_solve_mixed(h, h->d_u, false);
   return enqueue_solve64(h, &h->tm_F_in64, &h->tm_u_out64, false);
 }
 
@@ -398,11 +400,11 @@ int enqueue_step(ads_handle* h) {
   int st;
   if (h->opts.precision == ADS_PREC_MIXED && h->form == ADS_FORM_HEAT) {
     if ((st = enqueue_assemble(h, h->d_u, h->d_F, true, true, true))) return st;
-    if ((st = enqueue_solve_mixed(h, h->d_delta))) return st;
+    if ((st = enqueue_solve_mixed(h, h->d_delta, true))) return st;
     RUN(h, "update", 1, launch_axpby(h->d_u, h->d_delta, 1.0, 1.0, (long long)h->n0, h->stream));
   } else if (h->opts.precision == ADS_PREC_MIXED) {
     if ((st = enqueue_assemble(h, h->d_u, h->d_F, false, false, true))) return st;
-    if ((st = enqueue_solve_mixed(h, h->d_u))) return st;
+    if ((st = enqueue_solve_mixed(h, h->d_u, true))) return st;
   } else {
     if ((st = enqueue_assemble(h, h->d_u, h->d_F, false, false, true))) return st;
     if ((st = enqueue_solve64(h, &h->tm_F_in64, &h->tm_u_out64, false))) return st;
@@ -591,7 +593,7 @@ int create_impl(ads_handle* h) {
   }
   h->norm_parts = 4 * nsm;
   h->npart = std::max(3 * h->res_grid, 2 * h->norm_parts);
-  if ((st = zalloc(&h->d_l2part, (size_t)h->asm_grid))) return st;
+  if ((st = zalloc(&h->d_l2part, 2 * (size_t)h->asm_grid))) return st;
   if ((st = zalloc(&h->d_part, (size_t)h->npart))) return st;
   if ((st = zalloc(&h->d_scal, SC_COUNT))) return st;
   ADS_CUDA(h, cudaMalloc(&h->d_flags, sizeof(int) * FL_COUNT));

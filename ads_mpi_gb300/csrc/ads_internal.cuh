@@ -79,7 +79,7 @@ struct AssembleArgs {
   long long shadow_stride;
   const double* fqp;   // qp-grid layout (qx + QX*(qy + QY*qz)), may be null
   const double* kqp;   // same layout, may be null
-  double* l2part;      // one partial per CTA
+  double* l2part;      // per CTA: l2 partial at [cta], max |written value| at [grid + cta]
   int* err;
 };
 
@@ -89,9 +89,9 @@ struct FixupArgs {
   double* F;
   const double* shadow;
   long long shadow_stride;
-  const double* l2part;
+  const double* l2part;  // [nl2] l2 partials, then [nl2] max |value| partials
   int nl2;
-  double* l2out;
+  double* scal;          // device scalars (SC_*)
 };
 
 struct SweepArgs {
@@ -110,6 +110,8 @@ struct SweepArgs {
   long long out_pitch;   // PX
   long long out_slice;   // PX * Ny
   int out_line_dim;      // TMA store: 1 -> coords (lanes, line, third); 2 -> (lanes, third, line)
+  int third_extent;      // extent of the tile's fixed (third) dimension
+  int out_third_extent;  // same, for the final modes (y extent of L0)
   int* err;
 };
 
@@ -194,6 +196,6 @@ cudaError_t launch_kappa_grad(const Geometry& g, const double* u, const double* 
 cudaError_t measure_fma_peak(bool fp64, double* tflops);
 
 size_t assemble_smem_bytes(int P, bool fp32);
-size_t sweep_smem_bytes(int tin, int tc, int nchunk);
+size_t sweep_smem_bytes(int tin, int tc, int P, int L, int nchunk);
 
 }  // namespace ads

@@ -75,7 +75,7 @@ struct AsmLayout {
   static constexpr size_t o_nz = o_jwy + sizeof(T) * TY * Q;
   static constexpr size_t o_jwz = o_nz + sizeof(T) * NT;
   static constexpr size_t o_red = (o_jwz + sizeof(T) * Q + 15) / 16 * 16;
-  static constexpr size_t bytes = o_red + sizeof(double) * (AS_THREADS / 32);
+  static constexpr size_t bytes = o_red + 2 * sizeof(double) * (AS_THREADS / 32);
 };
 
 template <int P>
@@ -135,6 +135,9 @@ __global__ void __launch_bounds__(AS_THREADS)
   const int nitems = a.nix * a.niy * a.niz;
 
   double l2_thread = 0.0;
+  // max |value| written by this thread, as the bit pattern of a non-negative
+  // double (integer order = numeric order); feeds the FP32 solve's scale
+  unsigned long long amax_bits = 0ull;
 
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
     const int ix = item % a.nix;
@@ -403,7 +406,10 @@ __global__ void __launch_bounds__(AS_THREADS)
             const bool ownx = (cx < TX) || lastx, owny = (cy < TY) || lasty;
             const int cls = (ownx ? 0 : 1) | (owny ? 0 : 2) | (ownz ? 0 : 4);
             double* dst = (cls == 0) ? a.F : a.shadow + (size_t)(cls - 1) * a.shadow_stride;
-            dst[(size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * cz)] = plane[it];
+            const double v = plane[it];
+            dst[(size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * cz)] = v;
+            const unsigned long long vb = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+            amax_bits = vb > amax_bits ? vb : amax_bits;
           }
           plane[it] = 0.0;
         }
@@ -422,52 +428,101 @@ __global__ void __launch_bounds__(AS_THREADS)
           const bool ownx = (cx < TX) || lastx, owny = (cy < TY) || lasty;
           const int cls = (ownx ? 0 : 1) | (owny ? 0 : 2) | (ownz ? 0 : 4);
           double* dst = (cls == 0) ? a.F : a.shadow + (size_t)(cls - 1) * a.shadow_stride;
-          dst[(size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * cz)] = plane[it];
+          const double v = plane[it];
+          dst[(size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * cz)] = v;
+          const unsigned long long vb = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+          amax_bits = vb > amax_bits ? vb : amax_bits;
         }
       }
     }
     cp_async_wait<0>();
   }  // item
 
-  // deterministic block reduction of the l2 partial
+  // deterministic block reduction of the l2 partial and of max |value|
   double v = l2_thread;
+  unsigned long long mb = amax_bits;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  for (int o = 16; o > 0; o >>= 1) {
+    v += __shfl_down_sync(0xffffffffu, v, o);
+    const unsigned long long ob = __shfl_down_sync(0xffffffffu, mb, o);
+    mb = ob > mb ? ob : mb;
+  }
   __syncthreads();
-  if (lane == 0) red[warp] = v;
+  unsigned long long* redm = reinterpret_cast<unsigned long long*>(red + AS_THREADS / 32);
+  if (lane == 0) { red[warp] = v; redm[warp] = mb; }
   __syncthreads();
   if (tid == 0) {
     double t = 0.0;
-    for (int w = 0; w < AS_THREADS / 32; ++w) t += red[w];
+    unsigned long long m = 0ull;
+    for (int w = 0; w < AS_THREADS / 32; ++w) {
+      t += red[w];
+      m = redm[w] > m ? redm[w] : m;
+    }
     a.l2part[blockIdx.x] = t;
+    a.l2part[gridDim.x + blockIdx.x] = __longlong_as_double((long long)m);
   }
 }
 
-// F += shadow contributions, in class order; block 0 also finishes the l2norm.
+// F += shadow contributions, in class order.  One warp per (y, z) row: the
+// whole row when y or z lies in a spill slab, else only the x slabs.  Block 0
+// also finishes the l2norm and the power-of-two scale of the FP32 solve
+// (from the largest value the assembly wrote, which is within a factor 8 of
+// max |F|: a DOF sums at most 8 written parts).
+__device__ __forceinline__ bool in_slab(int v, int tile, int P, int nitems) {
+  return v >= tile && (v % tile) < P && (v / tile) <= nitems - 1;
+}
+
 __global__ void k_fixup(const FixupArgs a) {
   const Geometry& g = a.g;
   const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
-  const long long total = (long long)Nx * Ny * Nz;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  const int P = g.P;
+  const int lane = threadIdx.x & 31;
+  if (blockIdx.x == 0 && threadIdx.x < 32) {
     double t = 0.0;
-    for (int i = 0; i < a.nl2; ++i) t += a.l2part[i];
-    *a.l2out = t;
+    unsigned long long m = 0ull;
+    for (int i = lane; i < a.nl2; i += 32) {
+      t += a.l2part[i];
+      const unsigned long long b = (unsigned long long)__double_as_longlong(a.l2part[a.nl2 + i]);
+      m = b > m ? b : m;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      t += __shfl_down_sync(0xffffffffu, t, o);
+      const unsigned long long ob = __shfl_down_sync(0xffffffffu, m, o);
+      m = ob > m ? ob : m;
+    }
+    if (lane == 0) {
+      a.scal[SC_L2] = t;
+      const double fm = __longlong_as_double((long long)m);
+      a.scal[SC_FMAX] = fm;
+      int e = 0;
+      if (fm > 0.0 && fm <= 1.7976931348623157e308) (void)frexp(fm, &e);
+      a.scal[SC_OUT_SCALE] = ldexp(1.0, e);
+      a.scal[SC_IN_SCALE] = ldexp(1.0, -e);
+    }
   }
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(idx % Nx);
-    const int y = (int)((idx / Nx) % Ny);
-    const int z = (int)(idx / ((long long)Nx * Ny));
-    const bool zx = (x >= AS_TX) && (x % AS_TX < g.P) && (x / AS_TX <= a.nix - 1);
-    const bool zy = (y >= AS_TY) && (y % AS_TY < g.P) && (y / AS_TY <= a.niy - 1);
-    const bool zz = (z >= a.zc) && (z % a.zc < g.P) && (z / a.zc <= a.niz - 1);
-    if (!(zx || zy || zz)) continue;
-    const int zone = (zx ? 1 : 0) | (zy ? 2 : 0) | (zz ? 4 : 0);
-    const size_t o = (size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * z);
-    double v = a.F[o];
-    for (int cls = 1; cls < 8; ++cls)
-      if ((cls & zone) == cls) v += a.shadow[(size_t)(cls - 1) * a.shadow_stride + o];
-    a.F[o] = v;
+  const long long rows = (long long)Ny * Nz;
+  const int wpb = blockDim.x / 32;
+  const int nxz = a.nix - 1;  // x slabs start at x = k*AS_TX, k = 1..nix-1
+  for (long long row = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); row < rows;
+       row += (long long)gridDim.x * wpb) {
+    const int y = (int)(row % Ny), z = (int)(row / Ny);
+    const bool zy = in_slab(y, AS_TY, P, a.niy);
+    const bool zz = in_slab(z, a.zc, P, a.niz);
+    const size_t rb = (size_t)g.PX * ((size_t)y + (size_t)Ny * z);
+    const int count = (zy || zz) ? Nx : nxz * P;
+    for (int t = lane; t < count; t += 32) {
+      const int x = (zy || zz) ? t : (t / P + 1) * AS_TX + (t % P);
+      if (x >= Nx) continue;
+      const bool zx = in_slab(x, AS_TX, P, a.nix);
+      const int zone = (zx ? 1 : 0) | (zy ? 2 : 0) | (zz ? 4 : 0);
+      if (zone == 0) continue;
+      const size_t o = rb + (size_t)x;
+      double v = a.F[o];
+      for (int cls = 1; cls < 8; ++cls)
+        if ((cls & zone) == cls) v += a.shadow[(size_t)(cls - 1) * a.shadow_stride + o];
+      a.F[o] = v;
+    }
   }
 }
 
@@ -535,9 +590,9 @@ size_t assemble_smem_bytes(int P, bool fp32) {
 }
 
 cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s) {
-  const long long total = (long long)a.g.N[0] * a.g.N[1] * a.g.N[2];
-  long long blocks = (total + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  const long long rows = (long long)a.g.N[1] * a.g.N[2];
+  long long blocks = (rows + 7) / 8;
+  if (blocks > 152 * 8) blocks = 152 * 8;
   if (blocks < 1) blocks = 1;
   k_fixup<<<(int)blocks, 256, 0, s>>>(a);
   return cudaGetLastError();

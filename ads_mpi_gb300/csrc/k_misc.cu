@@ -203,9 +203,16 @@ __global__ void k_norm_partial(const double* F, long long n, double* part) {
 }
 
 __global__ void k_norm_final(const double* part, int n, double* scal) {
-  if (threadIdx.x != 0) return;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x >= 32) return;
   double ff = 0.0, fm = 0.0;
-  for (int i = 0; i < n; ++i) { ff += part[2 * i]; fm = fmax(fm, part[2 * i + 1]); }
+  for (int i = lane; i < n; i += 32) { ff += part[2 * i]; fm = fmax(fm, part[2 * i + 1]); }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ff += __shfl_down_sync(0xffffffffu, ff, o);
+    fm = fmax(fm, __shfl_down_sync(0xffffffffu, fm, o));
+  }
+  if (lane != 0) return;
   scal[SC_FF] = ff;
   scal[SC_FMAX] = fm;
   int e;
@@ -318,10 +325,13 @@ __global__ void k_dot_partial(const double* x, const double* y, long long n, dou
   if (threadIdx.x == 0) part[blockIdx.x] = s0[0];
 }
 __global__ void k_sum_final(const double* part, int n, double* out) {
-  if (threadIdx.x != 0) return;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x >= 32) return;
   double t = 0.0;
-  for (int i = 0; i < n; ++i) t += part[i];
-  *out = t;
+  for (int i = lane; i < n; i += 32) t += part[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  if (lane == 0) *out = t;
 }
 cudaError_t launch_dot(const double* x, const double* y, long long n, double* part, int nparts,
                        double* out, cudaStream_t s) {
