@@ -321,8 +321,11 @@ int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool 
   const void* tx = fp32 ? (const void*)&t32[0] : (const void*)&t64[0];
   const void* ty = fp32 ? (const void*)&t32[1] : (const void*)&t64[1];
   const void* tz = fp32 ? (const void*)&t32[2] : (const void*)&t64[2];
-  RUN(h, fp32 ? "assemble_f32" : "assemble_f64", 1, launch_assemble(fp32, incr, a, tx, ty, tz, h->asm_grid, h->stream));
+  int used = h->asm_grid;
+  RUN(h, fp32 ? "assemble_f32" : "assemble_f64", 1,
+      launch_assemble(fp32, incr, a, tx, ty, tz, h->asm_grid, &used, h->stream));
   FixupArgs f = fixup_args(h, F);
+  f.nl2 = used;
   RUN(h, "fixup", 1, launch_fixup(f, h->stream));
   return ADS_OK;
 }
@@ -572,17 +575,17 @@ int create_impl(ads_handle* h) {
   const int nsm = prop.multiProcessorCount;
   const size_t smem_max = prop.sharedMemPerMultiprocessor;
   {
+    // expected residency: 3 CTAs/SM for FP32 at p <= 2, else 2 (registers)
     const bool f32 = h->opts.precision == ADS_PREC_MIXED;
     const size_t b = assemble_smem_bytes(h->P, f32) + 1024;
-    int per_sm = (int)std::min<size_t>(smem_max / b, 2048 / AS_THREADS);
+    int per_sm = (int)std::min<size_t>(smem_max / b, (f32 && h->P <= 2) ? 3 : 2);
     if (per_sm < 1) per_sm = 1;
     const int resident = nsm * per_sm;
-    h->asm_nix = (g.E[0] + AS_TX - 1) / AS_TX;
+    h->asm_nix = (g.E[0] + as_tx(h->P) - 1) / as_tx(h->P);
     h->asm_niy = (g.E[1] + AS_TY - 1) / AS_TY;
     h->asm_zc = pick_zc(g.E[2], h->asm_nix * h->asm_niy, resident, std::max(h->P, 4));
     h->asm_niz = (g.E[2] + h->asm_zc - 1) / h->asm_zc;
-    const int items = h->asm_nix * h->asm_niy * h->asm_niz;
-    h->asm_grid = std::min(items, resident);
+    h->asm_grid = nsm * 8;  // bound of persistent CTAs; the launch uses the real residency
   }
   {
     h->res_nix = (g.N[0] + RS_TX - 1) / RS_TX;

@@ -15,12 +15,13 @@ namespace ads {
 // ---------------------------------------------------------------------------
 // Tiling constants
 // ---------------------------------------------------------------------------
-// Assembly: a CTA owns a brick of AS_TX x AS_TY elements in x/y and streams a
-// chunk of element layers along z.  256 threads = 8 warps; in the x stage a
-// warp handles one row of AS_TX = 32 elements (one element per lane).
-constexpr int AS_TX = 32;
+// Assembly: a CTA owns a brick of as_tx(p) x AS_TY elements in x/y and streams
+// a chunk of element layers along z.  as_tx(p) = 32 - p makes the brick's DOF
+// footprint in x exactly 32 wide (one warp); 256 threads = 8 warps = one
+// thread per (element row, footprint column) in the y/z stages.
 constexpr int AS_TY = 8;
 constexpr int AS_THREADS = 256;
+__host__ __device__ constexpr int as_tx(int p) { return 32 - p; }
 
 // Banded sweeps: one warp solves SW_LANES lines; lines are staged through
 // shared memory in chunks of SW_CH positions (TMA boxes).
@@ -132,8 +133,10 @@ struct ResidualArgs {
 // ---------------------------------------------------------------------------
 // incr (FP32 heat form only): leave out the mass term J W v u, i.e. assemble
 // G = F - M u instead of F
+// grid: upper bound of persistent CTAs (size of the partial arrays); the grid
+// actually launched (resident CTAs, at most the work items) is returned
 cudaError_t launch_assemble(bool fp32, bool incr, const AssembleArgs& a, const void* tabs_x,
-                            const void* tabs_y, const void* tabs_z, int grid, cudaStream_t s);
+                            const void* tabs_y, const void* tabs_z, int grid, int* used_grid, cudaStream_t s);
 cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s);
 
 // kind: 0 = x sweep (L0 -> L1), 1 = y sweep (L1 -> L2), 2 = z sweep (L2 -> L0)

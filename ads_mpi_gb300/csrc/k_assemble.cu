@@ -15,7 +15,7 @@
 //                   g0 = JW f                                                   (projection)
 //   test functions  g --x--> H0,H1,H2 --y--> I0,I1 --z--> F (accumulated in FP64)
 //
-// Work decomposition: a CTA owns a brick of AS_TX x AS_TY elements in x/y and
+// Work decomposition: a CTA owns a brick of (32-p) x AS_TY elements in x/y and
 // a chunk of element layers in z, which it streams layer by layer with a ring
 // of p+2 coefficient planes (prefetched with cp.async) and a ring of p+1 FP64
 // accumulator planes.  A DOF plane is complete once the layer with the same
@@ -29,6 +29,8 @@
 // partition of unity) is reduced per CTA and finished by k_fixup.
 #include "ads_internal.cuh"
 
+#include <algorithm>
+
 namespace ads {
 
 template <typename T>
@@ -40,8 +42,8 @@ __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return static_cast<unsigned>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ void cp_async16(void* dst, const void* src, int src_bytes) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_u32(dst)), "l"(src),
+__device__ __forceinline__ void cp_async8(void* dst, const void* src, int src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(smem_u32(dst)), "l"(src),
                "r"(src_bytes)
                : "memory");
 }
@@ -54,22 +56,25 @@ __device__ __forceinline__ void cp_async_wait() {
 template <int P, typename T>
 struct AsmLayout {
   static constexpr int Q = P + 1;
-  static constexpr int TX = AS_TX, TY = AS_TY;
-  static constexpr int CX = TX + P, CY = TY + P;
+  static constexpr int TX = as_tx(P), TY = AS_TY;
+  static constexpr int CX = TX + P;  // == 32: the x footprint is one warp wide
+  static constexpr int CY = TY + P;
   static constexpr int NCOL = CX * CY;
-  static constexpr int CXP = 2 * ((CX + 1) / 2);  // even row pitch of the coefficient planes
-  static constexpr int NCOLP = CXP * CY;
   static constexpr int QY = TY * Q;
-  static constexpr int RC = P + 2;  // coefficient ring
+  static constexpr int RC = P + 2;  // coefficient ring (P+1 planes in use + 1 in flight)
   static constexpr int RF = P + 1;  // accumulator ring
   static constexpr int NT = Q * (P + 1) * 2;  // table entries per element
+  static constexpr bool F32 = sizeof(T) == 4;
+  static_assert(CX == 32, "footprint must be one warp wide");
   // offsets in bytes
-  static constexpr size_t o_cring = 0;
-  static constexpr size_t o_fring = o_cring + sizeof(double) * RC * NCOLP;
-  static constexpr size_t o_za = o_fring + sizeof(double) * RF * NCOL;
+  static constexpr size_t o_cring = 0;                                          // double [RC][NCOL]
+  static constexpr size_t o_tring = o_cring + sizeof(double) * RC * NCOL;       // T [RC][NCOL] (FP32 only)
+  static constexpr size_t o_fring = o_tring + (F32 ? sizeof(float) * RC * NCOL : 0);
+  static constexpr size_t fring_bytes = F32 ? 2 * sizeof(float) * RF * NCOL : sizeof(double) * RF * NCOL;
+  static constexpr size_t o_za = o_fring + fring_bytes;                         // T [Q][NCOL]
   static constexpr size_t o_zb = o_za + sizeof(T) * Q * NCOL;
-  static constexpr size_t o_y = o_zb + sizeof(T) * Q * NCOL;
-  static constexpr size_t o_h = o_y + sizeof(T) * 3 * QY * CX;
+  static constexpr size_t o_y = o_zb + sizeof(T) * Q * NCOL;                    // T [3][QY][CX]
+  static constexpr size_t o_h = o_y + sizeof(T) * 3 * QY * CX;                  // T [3][QY][CX]
   static constexpr size_t o_ny = o_h + sizeof(T) * 3 * QY * CX;
   static constexpr size_t o_jwy = o_ny + sizeof(T) * TY * NT;
   static constexpr size_t o_nz = o_jwy + sizeof(T) * TY * Q;
@@ -78,39 +83,61 @@ struct AsmLayout {
   static constexpr size_t bytes = o_red + 2 * sizeof(double) * (AS_THREADS / 32);
 };
 
+// One coefficient plane z of the brick's footprint (CY rows of 32 DOFs along
+// x, coalesced) into shared memory with 8-byte cp.async copies; entries
+// outside the mesh are zero-filled.  (The brick's x origin is a multiple of
+// 32 - p, odd for odd p, so 16-byte copies would not stay aligned.)
 template <int P>
 __device__ __forceinline__ void issue_plane(double* ring_plane, const double* __restrict__ u,
                                             const Geometry& g, int x0, int y0, int z) {
-  using L = AsmLayout<P, double>;
-  constexpr int PAIRS = L::CXP / 2;
+  constexpr int CX = 32, CY = AS_TY + P;
   const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
-  for (int it = threadIdx.x; it < PAIRS * L::CY; it += AS_THREADS) {
-    const int cy = it / PAIRS, pr = it % PAIRS;
-    const int cx = 2 * pr;
+  for (int it = threadIdx.x; it < CX * CY; it += AS_THREADS) {
+    const int cy = it / CX, cx = it % CX;
     const int x = x0 + cx, y = y0 + cy;
-    int bytes = 0;
-    const double* src = u;
-    if (z < Nz && y < Ny && x < Nx) {
-      bytes = (x + 1 < Nx) ? 16 : 8;
-      src = u + (size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * z);
-    }
-    // rows have an even pitch CXP, so a pair never crosses into the next row
-    cp_async16(ring_plane + cy * L::CXP + cx, src, bytes);
+    const bool ok = (z < Nz) && (y < Ny) && (x < Nx);
+    const double* src = ok ? u + (size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * z) : u;
+    cp_async8(ring_plane + it, src, ok ? 8 : 0);
   }
 }
 
+// exact float -> double with integer operations (normal numbers; the rest
+// takes the conversion instruction)
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) |
+                                  ((unsigned long long)(e + 896u) << 52) |
+                                  ((unsigned long long)(b & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+// (hi, lo) += v without rounding loss (two-sum)
+__device__ __forceinline__ void two_sum_add(float& hi, float& lo, float v) {
+  const float s = hi + v;
+  const float bp = s - hi;
+  const float err = (hi - (s - bp)) + (v - bp);
+  hi = s;
+  lo += err;
+}
+
 template <int P, typename T, int FORM, bool HAS_F, bool HAS_K, bool INCR>
-__global__ void __launch_bounds__(AS_THREADS)
+__global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (P <= 2 || sizeof(T) == 4 ? 2 : 1))
     k_assemble(const AssembleArgs a, const Tabs3<T> tb) {
   using L = AsmLayout<P, T>;
   constexpr int Q = L::Q, TX = L::TX, TY = L::TY, CX = L::CX, CY = L::CY;
-  constexpr int CXP = L::CXP, NCOLP = L::NCOLP;
   constexpr int NCOL = L::NCOL, QY = L::QY, RC = L::RC, RF = L::RF;
   constexpr bool HEAT = (FORM == ADS_FORM_HEAT);
+  constexpr bool F32 = L::F32;
+  constexpr bool G0_ZERO = HEAT && INCR && !HAS_F;  // increment form without source: no v-term
 
   extern __shared__ __align__(16) unsigned char smem[];
   double* cring = reinterpret_cast<double*>(smem + L::o_cring);
-  double* fring = reinterpret_cast<double*>(smem + L::o_fring);
+  float* tring = reinterpret_cast<float*>(smem + L::o_tring);
+  double* fr64 = reinterpret_cast<double*>(smem + L::o_fring);
+  float* frhi = reinterpret_cast<float*>(smem + L::o_fring);
+  float* frlo = frhi + RF * NCOL;
   T* ZA = reinterpret_cast<T*>(smem + L::o_za);
   T* ZB = reinterpret_cast<T*>(smem + L::o_zb);
   T* Y0 = reinterpret_cast<T*>(smem + L::o_y);
@@ -132,7 +159,10 @@ __global__ void __launch_bounds__(AS_THREADS)
   const long long QXt = (long long)Ex * Q, QYt = (long long)Ey * Q;
   const T dt = (T)a.dt;
   const T kappa = (T)a.kappa;
+  const T ndtk = -(T)a.dt * (T)a.kappa;
   const int nitems = a.nix * a.niy * a.niz;
+  // this thread's (element row, footprint column) for the y/z stages
+  const int my_ey = tid / CX, my_cx = tid % CX;
 
   double l2_thread = 0.0;
   // max |value| written by this thread, as the bit pattern of a non-negative
@@ -150,19 +180,19 @@ __global__ void __launch_bounds__(AS_THREADS)
 
     __syncthreads();  // previous item fully done with shared memory
 
-    // per-lane x tables (element x0 + lane)
+    // per-lane x tables (element x0 + lane; lanes >= TX have no element)
     T nx[Q][P + 1][2];
     T jwx[Q];
+    const bool lane_elem = (lane < TX) && (x0 + lane < Ex);
     {
       const int ex = x0 + lane;
-      const bool ok = ex < Ex;
 #pragma unroll
       for (int k = 0; k < Q; ++k) {
-        jwx[k] = ok ? tb.x.jw[(size_t)ex * Q + k] : T(0);
+        jwx[k] = lane_elem ? tb.x.jw[(size_t)ex * Q + k] : T(0);
 #pragma unroll
         for (int b = 0; b <= P; ++b) {
-          nx[k][b][0] = ok ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 0] : T(0);
-          nx[k][b][1] = ok ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 1] : T(0);
+          nx[k][b][0] = lane_elem ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 0] : T(0);
+          nx[k][b][1] = lane_elem ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 1] : T(0);
         }
       }
     }
@@ -174,41 +204,50 @@ __global__ void __launch_bounds__(AS_THREADS)
       const int ey = y0 + i / Q;
       JWYs[i] = (ey < Ey) ? tb.y.jw[(size_t)ey * Q + (i % Q)] : T(0);
     }
-    for (int i = tid; i < RF * NCOL; i += AS_THREADS) fring[i] = 0.0;
+    if (F32) {
+      for (int i = tid; i < 2 * RF * NCOL; i += AS_THREADS) frhi[i] = 0.f;
+    } else {
+      for (int i = tid; i < RF * NCOL; i += AS_THREADS) fr64[i] = 0.0;
+    }
 
     // initial coefficient planes ez0 .. ez0+P
     if (HEAT) {
 #pragma unroll
-      for (int b = 0; b <= P; ++b)
-        issue_plane<P>(cring + ((ez0 + b) % RC) * NCOLP, a.u, g, x0, y0, ez0 + b);
+      for (int b = 0; b <= P; ++b) issue_plane<P>(cring + ((ez0 + b) % RC) * NCOL, a.u, g, x0, y0, ez0 + b);
     }
     cp_async_commit();
 
-    T acc[2][P + 1];
-#pragma unroll
-    for (int s = 0; s < 2; ++s)
-#pragma unroll
-      for (int b = 0; b <= P; ++b) acc[s][b] = T(0);
+    T l2_item = T(0);
 
     for (int ez = ez0; ez < ez1; ++ez) {
       // prefetch the plane the next layer adds
-      if (HEAT && ez + 1 < ez1) issue_plane<P>(cring + ((ez + P + 1) % RC) * NCOLP, a.u, g, x0, y0, ez + P + 1);
+      if (HEAT && ez + 1 < ez1) issue_plane<P>(cring + ((ez + P + 1) % RC) * NCOL, a.u, g, x0, y0, ez + P + 1);
       cp_async_commit();
-      // z tables of this layer
       for (int i = tid; i < L::NT; i += AS_THREADS) NZs[i] = tb.z.nn[(size_t)ez * L::NT + i];
       for (int i = tid; i < Q; i += AS_THREADS) JWZs[i] = tb.z.jw[(size_t)ez * Q + i];
       cp_async_wait<1>();
       __syncthreads();
 
-      T l2_layer = T(0);
+      // FP32: convert each coefficient plane once, when it arrives
+      if (HEAT && F32) {
+        const int zlo = (ez == ez0) ? ez : ez + P;
+        for (int z = zlo; z <= ez + P; ++z) {
+          const double* src = cring + (z % RC) * NCOL;
+          float* dst = tring + (z % RC) * NCOL;
+          for (int i = tid; i < NCOL; i += AS_THREADS) dst[i] = (float)src[i];
+        }
+        __syncthreads();
+      }
 
       // ---- z interpolation: ZA = sum_b Nz C, ZB = sum_b dNz C, per column ----
       if (HEAT) {
         for (int col = tid; col < NCOL; col += AS_THREADS) {
-          const int cy = col / CX, cx = col % CX;
           T c[P + 1];
 #pragma unroll
-          for (int b = 0; b <= P; ++b) c[b] = (T)cring[((ez + b) % RC) * NCOLP + cy * CXP + cx];
+          for (int b = 0; b <= P; ++b) {
+            if (F32) c[b] = (T)tring[((ez + b) % RC) * NCOL + col];
+            else c[b] = (T)cring[((ez + b) % RC) * NCOL + col];
+          }
 #pragma unroll
           for (int kz = 0; kz < Q; ++kz) {
             T za = T(0), zb = T(0);
@@ -224,34 +263,38 @@ __global__ void __launch_bounds__(AS_THREADS)
         __syncthreads();
       }
 
+      // per-thread partial sums of this layer for DOF rows my_ey+by, planes ez+bz
+      T acc[P + 1][P + 1];
+#pragma unroll
+      for (int by = 0; by <= P; ++by)
+#pragma unroll
+        for (int bz = 0; bz <= P; ++bz) acc[by][bz] = T(0);
+
 #pragma unroll 1
       for (int kz = 0; kz < Q; ++kz) {
-        // ---- y interpolation ----
+        // ---- y interpolation, one (element row, column) per thread ----
         if (HEAT) {
-          for (int it = tid; it < TY * CX; it += AS_THREADS) {
-            const int ey = it / CX, cx = it % CX;
-            T za[P + 1], zb[P + 1];
+          T za[P + 1], zb[P + 1];
+#pragma unroll
+          for (int b = 0; b <= P; ++b) {
+            za[b] = ZA[kz * NCOL + (my_ey + b) * CX + my_cx];
+            zb[b] = ZB[kz * NCOL + (my_ey + b) * CX + my_cx];
+          }
+#pragma unroll
+          for (int ky = 0; ky < Q; ++ky) {
+            T y0v = T(0), y1v = T(0), y2v = T(0);
 #pragma unroll
             for (int b = 0; b <= P; ++b) {
-              za[b] = ZA[kz * NCOL + (ey + b) * CX + cx];
-              zb[b] = ZB[kz * NCOL + (ey + b) * CX + cx];
+              const T nyv = NYs[my_ey * L::NT + (ky * (P + 1) + b) * 2 + 0];
+              const T dny = NYs[my_ey * L::NT + (ky * (P + 1) + b) * 2 + 1];
+              y0v += nyv * za[b];
+              y1v += dny * za[b];
+              y2v += nyv * zb[b];
             }
-#pragma unroll
-            for (int ky = 0; ky < Q; ++ky) {
-              T y0v = T(0), y1v = T(0), y2v = T(0);
-#pragma unroll
-              for (int b = 0; b <= P; ++b) {
-                const T nyv = NYs[ey * L::NT + (ky * (P + 1) + b) * 2 + 0];
-                const T dny = NYs[ey * L::NT + (ky * (P + 1) + b) * 2 + 1];
-                y0v += nyv * za[b];
-                y1v += dny * za[b];
-                y2v += nyv * zb[b];
-              }
-              const int qy = ey * Q + ky;
-              Y0[qy * CX + cx] = y0v;
-              Y1[qy * CX + cx] = y1v;
-              Y2[qy * CX + cx] = y2v;
-            }
+            const int qy = my_ey * Q + ky;
+            Y0[qy * CX + my_cx] = y0v;
+            Y1[qy * CX + my_cx] = y1v;
+            Y2[qy * CX + my_cx] = y2v;
           }
           __syncthreads();
         }
@@ -259,7 +302,7 @@ __global__ void __launch_bounds__(AS_THREADS)
         // ---- x interpolation + integrand + x test contraction (warp per row) ----
         for (int qy = warp; qy < QY; qy += AS_THREADS / 32) {
           const int ey_l = qy / Q;
-          const bool elem_ok = (x0 + lane < Ex) && (y0 + ey_l < Ey);
+          const bool elem_ok = lane_elem && (y0 + ey_l < Ey);
           const T jwyz = JWYs[qy] * JWZs[kz];
           T h0[P + 1], h1[P + 1], h2[P + 1];
 #pragma unroll
@@ -268,9 +311,9 @@ __global__ void __launch_bounds__(AS_THREADS)
           if (HEAT) {
 #pragma unroll
             for (int b = 0; b <= P; ++b) {
-              yv0[b] = Y0[qy * CX + lane + b];
-              yv1[b] = Y1[qy * CX + lane + b];
-              yv2[b] = Y2[qy * CX + lane + b];
+              yv0[b] = lane_elem ? Y0[qy * CX + lane + b] : T(0);
+              yv1[b] = lane_elem ? Y1[qy * CX + lane + b] : T(0);
+              yv2[b] = lane_elem ? Y2[qy * CX + lane + b] : T(0);
             }
           }
           const long long qyg = (long long)y0 * Q + qy;
@@ -288,130 +331,129 @@ __global__ void __launch_bounds__(AS_THREADS)
                 duy += nx[kx][b][0] * yv1[b];
                 duz += nx[kx][b][0] * yv2[b];
               }
-              T fv = T(0), kv = kappa;
+              T fv = T(0);
               if (HAS_F) fv = elem_ok ? (T)a.fqp[qidx] : T(0);
-              if (HAS_K) kv = elem_ok ? (T)a.kqp[qidx] : T(0);
-              // INCR: increment form, the mass term J W v u is left out (its
-              // exact-quadrature value M u is added back analytically)
-              const T g0 = INCR ? (HAS_F ? s * dt * fv : T(0)) : (HAS_F ? s * (uu + dt * fv) : s * uu);
-              const T c = -dt * kv * s;
+              T c;
+              if (HAS_K) c = -dt * (elem_ok ? (T)a.kqp[qidx] : T(0)) * s;
+              else c = ndtk * s;
               const T g1 = c * dux, g2 = c * duy, g3 = c * duz;
-              l2_layer += s * uu * uu;
+              l2_item += s * uu * uu;
+              if (G0_ZERO) {
 #pragma unroll
-              for (int b = 0; b <= P; ++b) {
-                h0[b] += nx[kx][b][0] * g0 + nx[kx][b][1] * g1;
-                h1[b] += nx[kx][b][0] * g2;
-                h2[b] += nx[kx][b][0] * g3;
+                for (int b = 0; b <= P; ++b) {
+                  h0[b] += nx[kx][b][1] * g1;
+                  h1[b] += nx[kx][b][0] * g2;
+                  h2[b] += nx[kx][b][0] * g3;
+                }
+              } else {
+                // INCR: the mass term J W v u is left out (its exact-quadrature
+                // value M u is added back analytically)
+                const T g0 = INCR ? s * dt * fv : (HAS_F ? s * (uu + dt * fv) : s * uu);
+#pragma unroll
+                for (int b = 0; b <= P; ++b) {
+                  h0[b] += nx[kx][b][0] * g0 + nx[kx][b][1] * g1;
+                  h1[b] += nx[kx][b][0] * g2;
+                  h2[b] += nx[kx][b][0] * g3;
+                }
               }
             } else {
               const T fv = (HAS_F && elem_ok) ? (T)a.fqp[qidx] : (HAS_F ? T(0) : T(1));
               const T g0 = s * fv;
-              l2_layer += s * fv * fv;
+              l2_item += s * fv * fv;
 #pragma unroll
               for (int b = 0; b <= P; ++b) h0[b] += nx[kx][b][0] * g0;
             }
           }
-          // combine the p+1 local contributions of neighbouring elements (lanes)
-          {
-            T v0 = h0[0], v1 = h1[0], v2 = h2[0];
+          // column cx = lane receives local function b of element lane - b
+          T v0 = h0[0], v1 = h1[0], v2 = h2[0];
 #pragma unroll
-            for (int b = 1; b <= P; ++b) {
-              const T s0 = __shfl_up_sync(0xffffffffu, h0[b], b);
-              const T s1 = HEAT ? __shfl_up_sync(0xffffffffu, h1[b], b) : T(0);
-              const T s2 = HEAT ? __shfl_up_sync(0xffffffffu, h2[b], b) : T(0);
-              if (lane >= b) { v0 += s0; v1 += s1; v2 += s2; }
-            }
-            H0[qy * CX + lane] = v0;
-            if (HEAT) { H1[qy * CX + lane] = v1; H2[qy * CX + lane] = v2; }
-#pragma unroll
-            for (int j = 0; j < P; ++j) {
-              T e0 = T(0), e1 = T(0), e2 = T(0);
-#pragma unroll
-              for (int b = j + 1; b <= P; ++b) {
-                e0 += __shfl_sync(0xffffffffu, h0[b], TX + j - b);
-                if (HEAT) {
-                  e1 += __shfl_sync(0xffffffffu, h1[b], TX + j - b);
-                  e2 += __shfl_sync(0xffffffffu, h2[b], TX + j - b);
-                }
-              }
-              if (lane == 0) {
-                H0[qy * CX + TX + j] = e0;
-                if (HEAT) { H1[qy * CX + TX + j] = e1; H2[qy * CX + TX + j] = e2; }
-              }
-            }
+          for (int b = 1; b <= P; ++b) {
+            const T s0 = __shfl_up_sync(0xffffffffu, h0[b], b);
+            const T s1 = HEAT ? __shfl_up_sync(0xffffffffu, h1[b], b) : T(0);
+            const T s2 = HEAT ? __shfl_up_sync(0xffffffffu, h2[b], b) : T(0);
+            if (lane >= b) { v0 += s0; v1 += s1; v2 += s2; }
           }
+          H0[qy * CX + lane] = v0;
+          if (HEAT) { H1[qy * CX + lane] = v1; H2[qy * CX + lane] = v2; }
         }
         __syncthreads();
 
-        // ---- y test contraction + z test contraction into per-thread sums ----
+        // ---- y test contraction of this thread's element row, then z ----
+        {
+          T i0[P + 1], i1[P + 1];
 #pragma unroll
-        for (int s = 0; s < 2; ++s) {
-          const int it = tid + s * AS_THREADS;
-          if (it < NCOL) {
-            const int cy = it / CX, cx = it % CX;
-            T i0 = T(0), i1 = T(0);
-            const int eylo = max(0, cy - P), eyhi = min(TY - 1, cy);
-            for (int ey = eylo; ey <= eyhi; ++ey) {
-              const int b = cy - ey;
+          for (int by = 0; by <= P; ++by) { i0[by] = T(0); i1[by] = T(0); }
 #pragma unroll
-              for (int ky = 0; ky < Q; ++ky) {
-                const int qy = ey * Q + ky;
-                const T nyv = NYs[ey * L::NT + (ky * (P + 1) + b) * 2 + 0];
-                if (HEAT) {
-                  const T dny = NYs[ey * L::NT + (ky * (P + 1) + b) * 2 + 1];
-                  i0 += nyv * H0[qy * CX + cx] + dny * H1[qy * CX + cx];
-                  i1 += nyv * H2[qy * CX + cx];
-                } else {
-                  i0 += nyv * H0[qy * CX + cx];
-                }
+          for (int ky = 0; ky < Q; ++ky) {
+            const int qy = my_ey * Q + ky;
+            const T hv0 = H0[qy * CX + my_cx];
+            const T hv1 = HEAT ? H1[qy * CX + my_cx] : T(0);
+            const T hv2 = HEAT ? H2[qy * CX + my_cx] : T(0);
+#pragma unroll
+            for (int by = 0; by <= P; ++by) {
+              const T nyv = NYs[my_ey * L::NT + (ky * (P + 1) + by) * 2 + 0];
+              if (HEAT) {
+                const T dny = NYs[my_ey * L::NT + (ky * (P + 1) + by) * 2 + 1];
+                i0[by] += nyv * hv0 + dny * hv1;
+                i1[by] += nyv * hv2;
+              } else {
+                i0[by] += nyv * hv0;
               }
             }
+          }
 #pragma unroll
-            for (int b = 0; b <= P; ++b) {
-              if (HEAT)
-                acc[s][b] += NZs[(kz * (P + 1) + b) * 2 + 0] * i0 + NZs[(kz * (P + 1) + b) * 2 + 1] * i1;
-              else
-                acc[s][b] += NZs[(kz * (P + 1) + b) * 2 + 0] * i0;
+          for (int bz = 0; bz <= P; ++bz) {
+            const T nz0 = NZs[(kz * (P + 1) + bz) * 2 + 0];
+            const T nz1 = NZs[(kz * (P + 1) + bz) * 2 + 1];
+#pragma unroll
+            for (int by = 0; by <= P; ++by) {
+              if (HEAT) acc[by][bz] += nz0 * i0[by] + nz1 * i1[by];
+              else acc[by][bz] += nz0 * i0[by];
             }
           }
         }
-        __syncthreads();
+        if (!HEAT) __syncthreads();
       }  // kz
 
-      l2_thread += (double)l2_layer;
-
-      // FP64 accumulation of this layer's per-element sums into DOF planes ez..ez+P
+      // accumulate this layer's element partials into the DOF planes, one
+      // element-row offset at a time so no two threads touch the same entry
 #pragma unroll
-      for (int s = 0; s < 2; ++s) {
-        const int it = tid + s * AS_THREADS;
-        if (it < NCOL) {
+      for (int by = 0; by <= P; ++by) {
+        const int row = my_ey + by;
 #pragma unroll
-          for (int b = 0; b <= P; ++b) {
-            fring[((ez + b) % RF) * NCOL + it] += (double)acc[s][b];
-            acc[s][b] = T(0);
-          }
+        for (int bz = 0; bz <= P; ++bz) {
+          const int o = ((ez + bz) % RF) * NCOL + row * CX + my_cx;
+          if (F32) two_sum_add(frhi[o], frlo[o], (float)acc[by][bz]);
+          else fr64[o] += (double)acc[by][bz];
         }
+        __syncthreads();
       }
-      __syncthreads();
 
       // DOF plane ez is complete: write it out and clear its ring slot
       {
         const int cz = ez;
         const bool ownz = (cz < ez1) || lastz;
-        double* plane = fring + (cz % RF) * NCOL;
+        const int slot = (cz % RF) * NCOL;
         for (int it = tid; it < NCOL; it += AS_THREADS) {
           const int cy = it / CX, cx = it % CX;
           const int x = x0 + cx, y = y0 + cy;
+          double v;
+          if (F32) {
+            v = f2d_exact(frhi[slot + it]) + f2d_exact(frlo[slot + it]);
+            frhi[slot + it] = 0.f;
+            frlo[slot + it] = 0.f;
+          } else {
+            v = fr64[slot + it];
+            fr64[slot + it] = 0.0;
+          }
           if (x < Nx && y < Ny) {
             const bool ownx = (cx < TX) || lastx, owny = (cy < TY) || lasty;
             const int cls = (ownx ? 0 : 1) | (owny ? 0 : 2) | (ownz ? 0 : 4);
             double* dst = (cls == 0) ? a.F : a.shadow + (size_t)(cls - 1) * a.shadow_stride;
-            const double v = plane[it];
             dst[(size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * cz)] = v;
             const unsigned long long vb = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
             amax_bits = vb > amax_bits ? vb : amax_bits;
           }
-          plane[it] = 0.0;
         }
       }
       __syncthreads();
@@ -420,21 +462,22 @@ __global__ void __launch_bounds__(AS_THREADS)
     // remaining planes ez1 .. ez1+P-1
     for (int cz = ez1; cz < ez1 + P; ++cz) {
       const bool ownz = lastz;
-      const double* plane = fring + (cz % RF) * NCOL;
+      const int slot = (cz % RF) * NCOL;
       for (int it = tid; it < NCOL; it += AS_THREADS) {
         const int cy = it / CX, cx = it % CX;
         const int x = x0 + cx, y = y0 + cy;
         if (x < Nx && y < Ny && cz < g.N[2]) {
+          const double v = F32 ? f2d_exact(frhi[slot + it]) + f2d_exact(frlo[slot + it]) : fr64[slot + it];
           const bool ownx = (cx < TX) || lastx, owny = (cy < TY) || lasty;
           const int cls = (ownx ? 0 : 1) | (owny ? 0 : 2) | (ownz ? 0 : 4);
           double* dst = (cls == 0) ? a.F : a.shadow + (size_t)(cls - 1) * a.shadow_stride;
-          const double v = plane[it];
           dst[(size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * cz)] = v;
           const unsigned long long vb = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
           amax_bits = vb > amax_bits ? vb : amax_bits;
         }
       }
     }
+    l2_thread += (double)l2_item;
     cp_async_wait<0>();
   }  // item
 
@@ -503,7 +546,8 @@ __global__ void k_fixup(const FixupArgs a) {
   }
   const long long rows = (long long)Ny * Nz;
   const int wpb = blockDim.x / 32;
-  const int nxz = a.nix - 1;  // x slabs start at x = k*AS_TX, k = 1..nix-1
+  const int TX = as_tx(P);
+  const int nxz = a.nix - 1;  // x slabs start at x = k*TX, k = 1..nix-1
   for (long long row = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); row < rows;
        row += (long long)gridDim.x * wpb) {
     const int y = (int)(row % Ny), z = (int)(row / Ny);
@@ -512,9 +556,9 @@ __global__ void k_fixup(const FixupArgs a) {
     const size_t rb = (size_t)g.PX * ((size_t)y + (size_t)Ny * z);
     const int count = (zy || zz) ? Nx : nxz * P;
     for (int t = lane; t < count; t += 32) {
-      const int x = (zy || zz) ? t : (t / P + 1) * AS_TX + (t % P);
+      const int x = (zy || zz) ? t : (t / P + 1) * TX + (t % P);
       if (x >= Nx) continue;
-      const bool zx = in_slab(x, AS_TX, P, a.nix);
+      const bool zx = in_slab(x, TX, P, a.nix);
       const int zone = (zx ? 1 : 0) | (zy ? 2 : 0) | (zz ? 4 : 0);
       if (zone == 0) continue;
       const size_t o = rb + (size_t)x;
@@ -528,7 +572,7 @@ __global__ void k_fixup(const FixupArgs a) {
 
 template <int P, typename T, int FORM, bool HF, bool HK, bool INCR>
 static cudaError_t launch_one(const AssembleArgs& a, const void* tx, const void* ty, const void* tz,
-                              int grid, cudaStream_t s) {
+                              int grid, int* used_grid, cudaStream_t s) {
   using L = AsmLayout<P, T>;
   Tabs3<T> tb;
   tb.x = *static_cast<const AxisTab<T>*>(tx);
@@ -538,43 +582,54 @@ static cudaError_t launch_one(const AssembleArgs& a, const void* tx, const void*
   const size_t bytes = L::bytes;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e != cudaSuccess) return e;
-  kern<<<grid, AS_THREADS, bytes, s>>>(a, tb);
+  // persistent: the resident CTA count (registers and shared memory), at most `grid`
+  int per_sm = 0, dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, AS_THREADS, bytes);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  const int items = a.nix * a.niy * a.niz;
+  int g = std::min(std::min(grid, items), nsm * per_sm);
+  if (g < 1) g = 1;
+  *used_grid = g;
+  kern<<<g, AS_THREADS, bytes, s>>>(a, tb);
   return cudaGetLastError();
 }
 
 template <int P, typename T, bool INCR>
 static cudaError_t dispatch_heat(const AssembleArgs& a, const void* tx, const void* ty, const void* tz,
-                                 int grid, cudaStream_t s) {
+                                 int grid, int* used_grid, cudaStream_t s) {
   const bool hf = a.fqp != nullptr, hk = a.kqp != nullptr;
-  if (hf && hk) return launch_one<P, T, ADS_FORM_HEAT, true, true, INCR>(a, tx, ty, tz, grid, s);
-  if (hf) return launch_one<P, T, ADS_FORM_HEAT, true, false, INCR>(a, tx, ty, tz, grid, s);
-  if (hk) return launch_one<P, T, ADS_FORM_HEAT, false, true, INCR>(a, tx, ty, tz, grid, s);
-  return launch_one<P, T, ADS_FORM_HEAT, false, false, INCR>(a, tx, ty, tz, grid, s);
+  if (hf && hk) return launch_one<P, T, ADS_FORM_HEAT, true, true, INCR>(a, tx, ty, tz, grid, used_grid, s);
+  if (hf) return launch_one<P, T, ADS_FORM_HEAT, true, false, INCR>(a, tx, ty, tz, grid, used_grid, s);
+  if (hk) return launch_one<P, T, ADS_FORM_HEAT, false, true, INCR>(a, tx, ty, tz, grid, used_grid, s);
+  return launch_one<P, T, ADS_FORM_HEAT, false, false, INCR>(a, tx, ty, tz, grid, used_grid, s);
 }
 
 template <int P>
 static cudaError_t dispatch_form(bool fp32, bool incr, const AssembleArgs& a, const void* tx,
-                                 const void* ty, const void* tz, int grid, cudaStream_t s) {
+                                 const void* ty, const void* tz, int grid, int* used_grid, cudaStream_t s) {
   const bool hf = a.fqp != nullptr;
   if (a.form == ADS_FORM_PROJECT) {
     if (fp32)
-      return hf ? launch_one<P, float, ADS_FORM_PROJECT, true, false, false>(a, tx, ty, tz, grid, s)
-                : launch_one<P, float, ADS_FORM_PROJECT, false, false, false>(a, tx, ty, tz, grid, s);
-    return hf ? launch_one<P, double, ADS_FORM_PROJECT, true, false, false>(a, tx, ty, tz, grid, s)
-              : launch_one<P, double, ADS_FORM_PROJECT, false, false, false>(a, tx, ty, tz, grid, s);
+      return hf ? launch_one<P, float, ADS_FORM_PROJECT, true, false, false>(a, tx, ty, tz, grid, used_grid, s)
+                : launch_one<P, float, ADS_FORM_PROJECT, false, false, false>(a, tx, ty, tz, grid, used_grid, s);
+    return hf ? launch_one<P, double, ADS_FORM_PROJECT, true, false, false>(a, tx, ty, tz, grid, used_grid, s)
+              : launch_one<P, double, ADS_FORM_PROJECT, false, false, false>(a, tx, ty, tz, grid, used_grid, s);
   }
-  if (fp32) return incr ? dispatch_heat<P, float, true>(a, tx, ty, tz, grid, s)
-                        : dispatch_heat<P, float, false>(a, tx, ty, tz, grid, s);
-  return dispatch_heat<P, double, false>(a, tx, ty, tz, grid, s);
+  if (fp32) return incr ? dispatch_heat<P, float, true>(a, tx, ty, tz, grid, used_grid, s)
+                        : dispatch_heat<P, float, false>(a, tx, ty, tz, grid, used_grid, s);
+  return dispatch_heat<P, double, false>(a, tx, ty, tz, grid, used_grid, s);
 }
 
 cudaError_t launch_assemble(bool fp32, bool incr, const AssembleArgs& a, const void* tx, const void* ty,
-                            const void* tz, int grid, cudaStream_t s) {
+                            const void* tz, int grid, int* used_grid, cudaStream_t s) {
   switch (a.g.P) {
-    case 1: return dispatch_form<1>(fp32, incr, a, tx, ty, tz, grid, s);
-    case 2: return dispatch_form<2>(fp32, incr, a, tx, ty, tz, grid, s);
-    case 3: return dispatch_form<3>(fp32, incr, a, tx, ty, tz, grid, s);
-    case 4: return dispatch_form<4>(fp32, incr, a, tx, ty, tz, grid, s);
+    case 1: return dispatch_form<1>(fp32, incr, a, tx, ty, tz, grid, used_grid, s);
+    case 2: return dispatch_form<2>(fp32, incr, a, tx, ty, tz, grid, used_grid, s);
+    case 3: return dispatch_form<3>(fp32, incr, a, tx, ty, tz, grid, used_grid, s);
+    case 4: return dispatch_form<4>(fp32, incr, a, tx, ty, tz, grid, used_grid, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -114,9 +114,51 @@ __device__ __forceinline__ void bulk_wait_read() {
   asm volatile("cp.async.bulk.wait_group.read %0;\n" ::"n"(N) : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Conversions without the FP64 pipe (GB300 runs FP64 at 1/64 of FP32): the
+// power-of-two scale 2^sexp is folded into the exponent field.
+// ---------------------------------------------------------------------------
+// double -> float, round to nearest even, times 2^sexp
+__device__ __forceinline__ float d2f_scaled(double d, int sexp) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int e = (int)((b >> 52) & 0x7ffull) + sexp;  // biased double exponent after scaling
+  const int ef = e - 896;                              // biased float exponent (1023 - 127)
+  if (((b >> 52) & 0x7ffull) == 0ull || ((b >> 52) & 0x7ffull) == 0x7ffull || ef < 1 || ef > 254)
+    return (float)(d * ldexp(1.0, sexp));  // zero, denormal, inf/nan or out of float range
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  const unsigned long long m = b & 0xfffffffffffffull;
+  const unsigned m23 = (unsigned)(m >> 29);
+  const unsigned rem = (unsigned)(m & 0x1fffffffull);
+  unsigned r = sign | ((unsigned)ef << 23) | m23;
+  if (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) r += 1u;  // carry rounds into the exponent
+  return __uint_as_float(r);
+}
+// float -> double (exact), times 2^sexp
+__device__ __forceinline__ double f2d_scaled(float f, int sexp) {
+  const unsigned b = __float_as_uint(f);
+  const int e = (int)((b >> 23) & 0xffu);
+  const int ed = e + 896 + sexp;
+  if (e == 0 || e == 0xff || ed < 1 || ed > 2046) return (double)f * ldexp(1.0, sexp);
+  const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) | ((unsigned long long)ed << 52) |
+                                  ((unsigned long long)(b & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+template <typename TC, typename TIn>
+__device__ __forceinline__ TC load_in(TIn v, int sexp, TC scale) {
+  if constexpr (sizeof(TIn) == 8 && sizeof(TC) == 4) return d2f_scaled((double)v, sexp);
+  else return (TC)v * scale;
+}
+__device__ __forceinline__ int pow2_exp(double s) {
+  return (int)(((unsigned long long)__double_as_longlong(s) >> 52) & 0x7ffull) - 1023;
+}
+
+constexpr int SW_BLK = 8;  // steps per software-pipelined block
+
 // One warp per CTA, persistent over tiles of 32 lines.  Shared memory holds
 // the staged lines S (the forward pass overwrites them with y in place), a
-// ring of SW_RING transposed output chunks, and the factor rows.
+// ring of SW_RING transposed output chunks, and the factor rows.  The
+// recurrences run in blocks of SW_BLK steps: all loads of a block first,
+// then the dependent FMA chain, then the stores.
 template <typename TIn, typename TC, int P, int MODE, bool TRANS>
 __global__ void __launch_bounds__(SW_LANES)
     k_sweep(const __grid_constant__ CUtensorMap tmin, const __grid_constant__ CUtensorMap tmout,
@@ -136,7 +178,6 @@ __global__ void __launch_bounds__(SW_LANES)
   uint64_t* bar = reinterpret_cast<uint64_t*>(p0 + SweepSmem<TIn, TC>::s_bytes(nchunk) +
                                               SweepSmem<TIn, TC>::t_bytes() + SweepSmem<TIn, TC>::f_bytes(P, L));
 
-  // factor rows -> shared memory, once per CTA
   if (MODE != 3) {
     const TC* fac = static_cast<const TC*>(a.fac);
     for (int idx = j; idx < (2 * P + 2) * L; idx += SW_LANES) Fs[idx] = fac[idx];
@@ -148,20 +189,23 @@ __global__ void __launch_bounds__(SW_LANES)
   __syncwarp();
 
   const double isd = (a.in_scale_dev != nullptr) ? *a.in_scale_dev : a.in_scale;
-  const bool scaled = (isd != 1.0);
+  const int in_exp = pow2_exp(isd);
   const TC in_scale = (TC)isd;
   const double osd = (a.out_scale_dev != nullptr) ? *a.out_scale_dev : a.out_scale;
+  const int out_exp = pow2_exp(osd);
+  const TC* F1 = Fs + L;               // f[1]
+  const TC* BS = Fs + (P + 1) * L;     // bs
+  const TC* G1 = Fs + (P + 2) * L;     // g[1]
 
-  const int ntiles = a.tiles_lane * ((MODE == 1 || MODE == 2) ? a.out_third_extent : a.third_extent);
+  const int ntiles = a.tiles_lane * a.third_extent;
   unsigned phase = 0;
+  constexpr int RAMP = SW_LANES - 1;
 
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int tl = tile % a.tiles_lane;
     const int t3 = tile / a.tiles_lane;
     const int lane_base = tl * SW_LANES;
 
-    // S is rewritten by the async proxy: order the generic accesses of the
-    // previous tile before the new load
     fence_proxy_async();
     __syncwarp();
     if (j == 0) {
@@ -184,95 +228,163 @@ __global__ void __launch_bounds__(SW_LANES)
       for (int m = 0; m < P; ++m) prev[m] = TC(0);
       auto fstep = [&](int i) {
         const int si = s_index(i, j);
-        TC b = (TC)S[si];
-        if (scaled) b *= in_scale;
+        const TC b = load_in<TC>(S[si], in_exp, in_scale);
         TC y = TRANS ? Fs[i] * b : b;
 #pragma unroll
         for (int m = P; m >= 2; --m) y -= Fs[m * L + i] * prev[m - 1];
-        y -= Fs[L + i] * prev[0];
+        y -= F1[i] * prev[0];
 #pragma unroll
         for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
         prev[0] = y;
         S[si] = (TIn)y;
       };
-      const int ramp = SW_LANES - 1;
-      for (int s = 0; s < ramp; ++s) {
+      int s = 0;
+      for (; s < RAMP && s < L + RAMP; ++s) {
         const int i = s - j;
         if (i >= 0 && i < L) fstep(i);
       }
-#pragma unroll 4
-      for (int s = ramp; s < L; ++s) fstep(s - j);
-      for (int s = (L > ramp ? L : ramp); s < L + ramp; ++s) {
+      // steady state, all lanes active: blocks of SW_BLK steps
+      for (; s + SW_BLK <= L; s += SW_BLK) {
+        TC bv[SW_BLK], fv[SW_BLK][P + 1];
+        int si[SW_BLK];
+#pragma unroll
+        for (int t = 0; t < SW_BLK; ++t) {
+          const int i = s + t - j;
+          si[t] = s_index(i, j);
+          bv[t] = load_in<TC>(S[si[t]], in_exp, in_scale);
+          fv[t][0] = TRANS ? Fs[i] : TC(1);
+#pragma unroll
+          for (int m = 1; m <= P; ++m) fv[t][m] = Fs[m * L + i];
+        }
+#pragma unroll
+        for (int t = 0; t < SW_BLK; ++t) {
+          TC y = TRANS ? fv[t][0] * bv[t] : bv[t];
+#pragma unroll
+          for (int m = P; m >= 2; --m) y -= fv[t][m] * prev[m - 1];
+          y -= fv[t][1] * prev[0];
+#pragma unroll
+          for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
+          prev[0] = y;
+          bv[t] = y;
+        }
+#pragma unroll
+        for (int t = 0; t < SW_BLK; ++t) S[si[t]] = (TIn)bv[t];
+      }
+      for (; s < L + RAMP; ++s) {
         const int i = s - j;
         if (i >= 0 && i < L) fstep(i);
       }
     }
 
     // ---- backward recurrence: x_i = bs_i y_i - sum_m g[m]_i x_{i+m}, written
-    //      transposed into the output ring; a chunk leaves as soon as the
-    //      slowest lane (31) has passed its lowest position ----
+    //      transposed into the output ring.  Chunk c is complete right after
+    //      step L-1-c*CH+31 (lane 31 passes its lowest position); the loop
+    //      runs in segments that end exactly at those steps. ----
     {
       TC nxt[P];
 #pragma unroll
       for (int m = 0; m < P; ++m) nxt[m] = TC(0);
-      int next_done = nchunk - 1;    // next chunk to complete
-      int next_start = nchunk - 2;   // next chunk lane 0 starts writing (top one starts at s = 0)
-      const int steps = L + SW_LANES - 1;
-      for (int s = 0; s < steps; ++s) {
-        // before lane 0 enters chunk next_start, its ring slot must be free
-        if (next_start >= 0 && s == L - (next_start + 1) * SW_CH) {
-          if (MODE == 0 || MODE == 3) {
-            if (next_start + SW_RING <= nchunk - 1 && j == 0) bulk_wait_read<1>();
+      auto tslot = [&](int i) -> TC* {
+        return T + ((i / SW_CH) % SW_RING) * (SW_CH * SW_LANES) + (i % SW_CH) * SW_LANES + j;
+      };
+      auto bstep = [&](int i) {
+        TC x;
+        if (MODE == 3) {
+          x = load_in<TC>(S[s_index(i, j)], 0, TC(1));
+        } else {
+          const TC y = (TC)S[s_index(i, j)];
+          x = TRANS ? y : BS[i] * y;
+#pragma unroll
+          for (int m = P; m >= 2; --m) x -= Fs[(P + 1 + m) * L + i] * nxt[m - 1];
+          x -= G1[i] * nxt[0];
+#pragma unroll
+          for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
+          nxt[0] = x;
+        }
+        *tslot(i) = x;
+      };
+      auto run = [&](int sa, int sb) {
+        int s = sa;
+        const int lo = (sa > RAMP) ? sa : RAMP;  // steady range [lo, hi): every lane in range
+        const int hi = (sb < L) ? sb : L;
+        for (; s < sb && s < lo; ++s) {
+          const int i = L - 1 - (s - j);
+          if (i >= 0 && i < L) bstep(i);
+        }
+        for (; s + SW_BLK <= hi; s += SW_BLK) {
+          TC yv[SW_BLK], gv[SW_BLK][P + 1];
+#pragma unroll
+          for (int t = 0; t < SW_BLK; ++t) {
+            const int i = L - 1 - (s + t - j);
+            if (MODE == 3) yv[t] = load_in<TC>(S[s_index(i, j)], 0, TC(1));
+            else yv[t] = (TC)S[s_index(i, j)];
+            if (MODE != 3) {
+              gv[t][0] = TRANS ? TC(1) : BS[i];
+#pragma unroll
+              for (int m = 1; m <= P; ++m) gv[t][m] = Fs[(P + 1 + m) * L + i];
+            }
+          }
+          if (MODE != 3) {
+#pragma unroll
+            for (int t = 0; t < SW_BLK; ++t) {
+              TC x = TRANS ? yv[t] : gv[t][0] * yv[t];
+#pragma unroll
+              for (int m = P; m >= 2; --m) x -= gv[t][m] * nxt[m - 1];
+              x -= gv[t][1] * nxt[0];
+#pragma unroll
+              for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
+              nxt[0] = x;
+              yv[t] = x;
+            }
+          }
+#pragma unroll
+          for (int t = 0; t < SW_BLK; ++t) *tslot(L - 1 - (s + t - j)) = yv[t];
+        }
+        for (; s < sb; ++s) {
+          const int i = L - 1 - (s - j);
+          if (i >= 0 && i < L) bstep(i);
+        }
+      };
+      int s = 0;
+      for (int c = nchunk - 1; c >= 0; --c) {
+        const int se = L - 1 - c * SW_CH + (SW_LANES - 1);
+        run(s, se + 1);
+        s = se + 1;
+        TC* slot = T + (c % SW_RING) * (SW_CH * SW_LANES);
+        if (MODE == 0 || MODE == 3) {
+          fence_proxy_async();
+          __syncwarp();
+          if (j == 0) {
+            if (a.out_line_dim == 1) tma_store_3d(&tmout, lane_base, c * SW_CH, t3, slot);
+            else tma_store_3d(&tmout, lane_base, t3, c * SW_CH, slot);
+            bulk_commit();
+            // lane 0 enters chunk c-2 (slot of chunk c+1) two steps after the
+            // next completion; keep only this chunk's store outstanding
+            bulk_wait_read<1>();
           }
           __syncwarp();
-          --next_start;
-        }
-        const int i = L - 1 - (s - j);
-        if (i >= 0 && i < L) {
-          TC x;
-          if (MODE == 3) {
-            x = (TC)S[s_index(i, j)];
-          } else {
-            const TC y = (TC)S[s_index(i, j)];
-            x = TRANS ? y : Fs[(P + 1) * L + i] * y;
+        } else {
+          __syncwarp();
+          // final z sweep: lanes are x, positions are z, t3 is y; rows of 32 x are coalesced
+          const int x = lane_base + j;
+          if (x < a.lanes_total) {
+            double* o = a.out + (size_t)x + (size_t)a.out_pitch * (size_t)t3 + (size_t)a.out_slice * (size_t)(c * SW_CH);
+            const int r1 = min(SW_CH, L - c * SW_CH);
+            double old[SW_CH];
+            if (MODE == 2) {
 #pragma unroll
-            for (int m = P; m >= 2; --m) x -= Fs[(P + 1 + m) * L + i] * nxt[m - 1];
-            x -= Fs[(P + 2) * L + i] * nxt[0];
-#pragma unroll
-            for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
-            nxt[0] = x;
-          }
-          T[((i / SW_CH) % SW_RING) * (SW_CH * SW_LANES) + (i % SW_CH) * SW_LANES + j] = x;
-        }
-        // chunk next_done is complete after lane 31 wrote its lowest position
-        if (next_done >= 0 && s == L - 1 - next_done * SW_CH + (SW_LANES - 1)) {
-          const int c = next_done;
-          TC* slot = T + (c % SW_RING) * (SW_CH * SW_LANES);
-          if (MODE == 0 || MODE == 3) {
-            fence_proxy_async();
-            __syncwarp();
-            if (j == 0) {
-              if (a.out_line_dim == 1) tma_store_3d(&tmout, lane_base, c * SW_CH, t3, slot);
-              else tma_store_3d(&tmout, lane_base, t3, c * SW_CH, slot);
-              bulk_commit();
+              for (int r = 0; r < SW_CH; ++r)
+                if (r < r1) old[r] = o[(size_t)a.out_slice * r];
             }
-          } else {
-            __syncwarp();
-            // final z sweep: lanes are x, positions are z, t3 is y
-            const int x = lane_base + j;
-            if (x < a.lanes_total) {
-              double* o = a.out + (size_t)x + (size_t)a.out_pitch * (size_t)t3;
-              const int r1 = min(SW_CH, L - c * SW_CH);
-              for (int r = 0; r < r1; ++r) {
-                const double v = osd * (double)slot[r * SW_LANES + j];
-                double* d = o + (size_t)a.out_slice * (size_t)(c * SW_CH + r);
-                if (MODE == 2) *d += v;
-                else *d = v;
+#pragma unroll
+            for (int r = 0; r < SW_CH; ++r) {
+              if (r < r1) {
+                const double v = f2d_scaled(slot[r * SW_LANES + j], out_exp);
+                o[(size_t)a.out_slice * r] = (MODE == 2) ? old[r] + v : v;
               }
             }
-            __syncwarp();
           }
-          --next_done;
+          __syncwarp();
         }
       }
     }
