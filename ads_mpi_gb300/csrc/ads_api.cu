@@ -374,15 +374,18 @@ int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready) {
   for (int k = 0; k < h->opts.max_refine; ++k) {
     ResidualArgs ra = residual_args(h, x, h->d_F, h->d_r);
     ra.skip_flag = conv;
+    ra.want_ff = (k == 0);
     RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
-    RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, true, h->d_scal, h->d_flags, h->stream));
+    RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, true, k == 0, h->d_scal, h->d_flags, h->stream));
     st = enqueue_solve32(h, &h->tm_r_in64, h->d_scal + SC_C_IN, h->d_scal + SC_C_OUT, 2, conv, "_corr", x);
     if (st) return st;
   }
   ResidualArgs ra = residual_args(h, x, h->d_F, h->d_r);
   ra.skip_flag = conv;
+  ra.want_ff = (h->opts.max_refine == 0);
   RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
-  RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, false, h->d_scal, h->d_flags, h->stream));
+  RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, false, h->opts.max_refine == 0,
+                                    h->d_scal, h->d_flags, h->stream));
   return ADS_OK;
 }
 

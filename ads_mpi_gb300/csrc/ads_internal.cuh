@@ -125,6 +125,7 @@ struct ResidualArgs {
   const double* band[3];  // per axis, (2P+1) x N: band[(m+P)*N + i] = M_{i,i+m}
   double* part;       // per CTA: [rr, ff, rmax]
   const int* skip_flag;
+  int want_ff;        // also reduce ||F||^2 (the first residual of a solve)
   int* err;
 };
 
@@ -171,7 +172,8 @@ enum FlagSlot {
 cudaError_t launch_residual(int P, const ResidualArgs& a, int grid, cudaStream_t s);
 // reduce residual partials; sets SC_RR, SC_RELRES, FL_CONV, correction scales and
 // (if count_iter and not converged) FL_ITERS += 1.  Skipped when FL_CONV is set.
-cudaError_t launch_decide(const double* part, int n, double tol, bool count_iter, double* scal,
+// use_ff: take ||F||^2 from the partials (and store it) instead of SC_FF
+cudaError_t launch_decide(const double* part, int n, double tol, bool count_iter, bool use_ff, double* scal,
                           int* flags, cudaStream_t s);
 // ||F||^2, max|F| and the first-solve scales
 cudaError_t launch_norm_f(const double* F, const Geometry& g, double* part, int nparts, double* scal,

@@ -217,9 +217,12 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
     }
     cp_async_commit();
 
+    // l2 partial: FP64 (FP64 mode) or a compensated (hi, lo) float pair
     T l2_item = T(0);
+    float l2_lo = 0.f;
 
     for (int ez = ez0; ez < ez1; ++ez) {
+      T l2_layer = T(0);
       // prefetch the plane the next layer adds
       if (HEAT && ez + 1 < ez1) issue_plane<P>(cring + ((ez + P + 1) % RC) * NCOL, a.u, g, x0, y0, ez + P + 1);
       cp_async_commit();
@@ -337,7 +340,7 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
               if (HAS_K) c = -dt * (elem_ok ? (T)a.kqp[qidx] : T(0)) * s;
               else c = ndtk * s;
               const T g1 = c * dux, g2 = c * duy, g3 = c * duz;
-              l2_item += s * uu * uu;
+              l2_layer += s * uu * uu;
               if (G0_ZERO) {
 #pragma unroll
                 for (int b = 0; b <= P; ++b) {
@@ -359,7 +362,7 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
             } else {
               const T fv = (HAS_F && elem_ok) ? (T)a.fqp[qidx] : (HAS_F ? T(0) : T(1));
               const T g0 = s * fv;
-              l2_item += s * fv * fv;
+              l2_layer += s * fv * fv;
 #pragma unroll
               for (int b = 0; b <= P; ++b) h0[b] += nx[kx][b][0] * g0;
             }
@@ -414,6 +417,9 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
         }
         if (!HEAT) __syncthreads();
       }  // kz
+
+      if constexpr (F32) two_sum_add(l2_item, l2_lo, l2_layer);
+      else l2_item += l2_layer;
 
       // accumulate this layer's element partials into the DOF planes, one
       // element-row offset at a time so no two threads touch the same entry
@@ -477,7 +483,7 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
         }
       }
     }
-    l2_thread += (double)l2_item;
+    l2_thread += (double)l2_item + (double)l2_lo;
     cp_async_wait<0>();
   }  // item
 

@@ -44,7 +44,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_residual(const ResidualArgs a) {
 #pragma unroll
     for (int m = 0; m < W; ++m) mx[m] = (x < Nx) ? bx[(size_t)m * Nx + x] : 0.0;
   }
-  double rr = 0.0, ff = 0.0, rmax = 0.0;
+  double rr = 0.0, ff = 0.0;
+  unsigned long long rmax_bits = 0ull;  // max |r| as the bits of a non-negative double
+  const bool want_ff = a.want_ff != 0;
 
   for (int zin = z0 - P; zin < z1 + P; ++zin) {
     if (zin >= 0 && zin < Nz) {
@@ -92,13 +94,14 @@ __global__ void __launch_bounds__(RS_THREADS) k_residual(const ResidualArgs a) {
         if (a.F != nullptr) {
           const double f = a.F[o];
           r = f - mu;
-          ff += f * f;
+          if (want_ff) ff += f * f;
         } else {
           r = mu;
         }
         a.r[o] = r;
         rr += r * r;
-        rmax = fmax(rmax, fabs(r));
+        const unsigned long long rb = (unsigned long long)__double_as_longlong(r) & 0x7fffffffffffffffull;
+        rmax_bits = rb > rmax_bits ? rb : rmax_bits;
       }
     }
   }
@@ -108,16 +111,23 @@ __global__ void __launch_bounds__(RS_THREADS) k_residual(const ResidualArgs a) {
   for (int o = 16; o > 0; o >>= 1) {
     rr += __shfl_down_sync(0xffffffffu, rr, o);
     ff += __shfl_down_sync(0xffffffffu, ff, o);
-    rmax = fmax(rmax, __shfl_down_sync(0xffffffffu, rmax, o));
+    const unsigned long long ob = __shfl_down_sync(0xffffffffu, rmax_bits, o);
+    rmax_bits = ob > rmax_bits ? ob : rmax_bits;
   }
-  if (lane == 0) { red[0][warp] = rr; red[1][warp] = ff; red[2][warp] = rmax; }
+  if (lane == 0) { red[0][warp] = rr; red[1][warp] = ff; red[2][warp] = __longlong_as_double((long long)rmax_bits); }
   __syncthreads();
   if (tid == 0) {
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-    for (int w = 0; w < RS_THREADS / 32; ++w) { a0 += red[0][w]; a1 += red[1][w]; a2 = fmax(a2, red[2][w]); }
+    double a0 = 0.0, a1 = 0.0;
+    unsigned long long m = 0ull;
+    for (int w = 0; w < RS_THREADS / 32; ++w) {
+      a0 += red[0][w];
+      a1 += red[1][w];
+      const unsigned long long b = (unsigned long long)__double_as_longlong(red[2][w]);
+      m = b > m ? b : m;
+    }
     a.part[3 * blockIdx.x + 0] = a0;
     a.part[3 * blockIdx.x + 1] = a1;
-    a.part[3 * blockIdx.x + 2] = a2;
+    a.part[3 * blockIdx.x + 2] = __longlong_as_double((long long)m);
   }
 }
 
@@ -140,7 +150,8 @@ __device__ __forceinline__ double pow2_exponent_scale(double v, int* e_out) {
   return ldexp(1.0, e);
 }
 
-__global__ void k_decide(const double* part, int n, double tol, int count_iter, double* scal, int* flags) {
+__global__ void k_decide(const double* part, int n, double tol, int count_iter, int use_ff, double* scal,
+                         int* flags) {
   __shared__ double s0[256], s1[256], s2[256];
   if (flags[FL_CONV] != 0) return;
   double rr = 0.0, ff = 0.0, rmax = 0.0;
@@ -160,7 +171,9 @@ __global__ void k_decide(const double* part, int n, double tol, int count_iter, 
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    rr = s0[0]; ff = s1[0]; rmax = s2[0];
+    rr = s0[0]; rmax = s2[0];
+    if (use_ff) { ff = s1[0]; scal[SC_FF] = ff; }
+    else ff = scal[SC_FF];
     scal[SC_RR] = rr;
     const double rel = (ff > 0.0) ? sqrt(rr / ff) : (rr > 0.0 ? INFINITY : 0.0);
     scal[SC_RELRES] = rel;
@@ -174,9 +187,9 @@ __global__ void k_decide(const double* part, int n, double tol, int count_iter, 
   }
 }
 
-cudaError_t launch_decide(const double* part, int n, double tol, bool count_iter, double* scal,
+cudaError_t launch_decide(const double* part, int n, double tol, bool count_iter, bool use_ff, double* scal,
                           int* flags, cudaStream_t s) {
-  k_decide<<<1, 256, 0, s>>>(part, n, tol, count_iter ? 1 : 0, scal, flags);
+  k_decide<<<1, 256, 0, s>>>(part, n, tol, count_iter ? 1 : 0, use_ff ? 1 : 0, scal, flags);
   return cudaGetLastError();
 }
 

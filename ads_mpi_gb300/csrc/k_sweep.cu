@@ -121,11 +121,13 @@ __device__ __forceinline__ void bulk_wait_read() {
 // double -> float, round to nearest even, times 2^sexp
 __device__ __forceinline__ float d2f_scaled(double d, int sexp) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const int e = (int)((b >> 52) & 0x7ffull) + sexp;  // biased double exponent after scaling
-  const int ef = e - 896;                              // biased float exponent (1023 - 127)
-  if (((b >> 52) & 0x7ffull) == 0ull || ((b >> 52) & 0x7ffull) == 0x7ffull || ef < 1 || ef > 254)
-    return (float)(d * ldexp(1.0, sexp));  // zero, denormal, inf/nan or out of float range
   const unsigned sign = (unsigned)(b >> 63) << 31;
+  const int ed = (int)((b >> 52) & 0x7ffull);
+  const int ef = ed + sexp - 896;  // biased float exponent after scaling (1023 - 127)
+  // values below the float range (and zeros, double denormals) flush to zero:
+  // with the scale putting max |v| in [0.5, 1) they are below 2^-126 of it
+  if (ed == 0 || ef < 1) return __uint_as_float(sign);
+  if (ed == 0x7ff || ef > 254) return (float)(d * ldexp(1.0, sexp));  // inf/nan/overflow
   const unsigned long long m = b & 0xfffffffffffffull;
   const unsigned m23 = (unsigned)(m >> 29);
   const unsigned rem = (unsigned)(m & 0x1fffffffull);
@@ -138,6 +140,7 @@ __device__ __forceinline__ double f2d_scaled(float f, int sexp) {
   const unsigned b = __float_as_uint(f);
   const int e = (int)((b >> 23) & 0xffu);
   const int ed = e + 896 + sexp;
+  if ((b & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)(b >> 31) << 63));
   if (e == 0 || e == 0xff || ed < 1 || ed > 2046) return (double)f * ldexp(1.0, sexp);
   const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) | ((unsigned long long)ed << 52) |
                                   ((unsigned long long)(b & 0x7fffffu) << 29);

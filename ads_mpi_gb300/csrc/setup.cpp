@@ -108,6 +108,7 @@ int axis_setup(int n, int p, AxisHost& a) {
   a.J.assign(a.E, 0.0);
   a.X.assign((size_t)a.E * q, 0.0);
   a.NN.assign((size_t)a.E * q * (p + 1) * 2, 0.0);
+  a.DD.assign((size_t)a.E * q * p, 0.0);
   a.JW.assign((size_t)a.E * q, 0.0);
   double Np[16], Nm[16];
   for (int e = 0; e < a.E; ++e) {
@@ -133,6 +134,10 @@ int axis_setup(int n, int p, AxisHost& a) {
         }
         a.NN[(((size_t)e * q + k) * (p + 1) + r) * 2 + 0] = Np[r];
         a.NN[(((size_t)e * q + k) * (p + 1) + r) * 2 + 1] = d;
+        if (r >= 1) {
+          const double den = a.U[j + p] - a.U[j];
+          a.DD[((size_t)e * q + k) * p + (r - 1)] = (den != 0.0) ? p * Nm[r - 1] / den : 0.0;
+        }
       }
     }
   }

@@ -13,6 +13,8 @@ struct AxisHost {
   std::vector<double> X;    // [E][q] Gauss points
   std::vector<double> JW;   // [E][q] J(e) W(k)
   std::vector<double> NN;   // [E][q][p+1][2]
+  std::vector<double> DD;   // [E][q][p]: D_b = p N_{j,p-1} / (U_{j+p} - U_j), j = O(e) + b, b = 1..p;
+                            // dN_b/dx = D_b - D_{b+1} (D_0 = D_{p+1} = 0)
   std::vector<double> band; // [(m+p)*N + i] = M[i][i+m]
 };
 
