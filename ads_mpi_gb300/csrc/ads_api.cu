@@ -66,6 +66,8 @@ struct ads_handle {
   double* d_jw64[3] = {nullptr, nullptr, nullptr};
   float* d_nn32[3] = {nullptr, nullptr, nullptr};
   float* d_jw32[3] = {nullptr, nullptr, nullptr};
+  double* d_dd64[3] = {nullptr, nullptr, nullptr};
+  float* d_dd32[3] = {nullptr, nullptr, nullptr};
   double* d_fac64[3] = {nullptr, nullptr, nullptr};
   double* d_tfac64[3] = {nullptr, nullptr, nullptr};
   float* d_fac32[3] = {nullptr, nullptr, nullptr};
@@ -315,9 +317,13 @@ int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool 
   AxisTab<double> t64[3];
   AxisTab<float> t32[3];
   for (int d = 0; d < 3; ++d) {
-    t64[d].nn = h->d_nn64[d]; t64[d].jw = h->d_jw64[d];
-    t32[d].nn = h->d_nn32[d]; t32[d].jw = h->d_jw32[d];
+    t64[d].nn = h->d_nn64[d]; t64[d].jw = h->d_jw64[d]; t64[d].dd = h->d_dd64[d];
+    t32[d].nn = h->d_nn32[d]; t32[d].jw = h->d_jw32[d]; t32[d].dd = h->d_dd32[d];
   }
+  // the FP32 heat assembly works on coefficients scaled by a power of two
+  if (fp32 && h->form == ADS_FORM_HEAT)
+    RUN(h, "uscale", 2, launch_uscale(u, (long long)h->n0, h->d_part, h->norm_parts, h->d_scal, h->stream));
+  a.uscale = h->d_scal + SC_USCALE;
   const void* tx = fp32 ? (const void*)&t32[0] : (const void*)&t64[0];
   const void* ty = fp32 ? (const void*)&t32[1] : (const void*)&t64[1];
   const void* tz = fp32 ? (const void*)&t32[2] : (const void*)&t64[2];
@@ -504,6 +510,7 @@ void free_all(ads_handle* h) {
   invalidate_graph(h);
   for (int d = 0; d < 3; ++d) {
     cudaFree(h->d_nn64[d]); cudaFree(h->d_jw64[d]); cudaFree(h->d_nn32[d]); cudaFree(h->d_jw32[d]);
+    cudaFree(h->d_dd64[d]); cudaFree(h->d_dd32[d]);
     cudaFree(h->d_fac64[d]); cudaFree(h->d_tfac64[d]); cudaFree(h->d_fac32[d]); cudaFree(h->d_band[d]);
   }
   cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_wA); cudaFree(h->d_wB);
@@ -547,11 +554,14 @@ int create_impl(ads_handle* h) {
     std::vector<double> fac, tfac;
     if (band_factor(a, fac, tfac)) return fail(h, ADS_ERR_ZERO_PIVOT, "zero pivot in the 1-D mass matrix");
     std::vector<float> nn32(a.NN.begin(), a.NN.end()), jw32(a.JW.begin(), a.JW.end()), fac32(fac.begin(), fac.end());
+    std::vector<float> dd32(a.DD.begin(), a.DD.end());
     int st;
     if ((st = upload(h, &h->d_nn64[d], a.NN))) return st;
     if ((st = upload(h, &h->d_jw64[d], a.JW))) return st;
     if ((st = upload(h, &h->d_nn32[d], nn32))) return st;
     if ((st = upload(h, &h->d_jw32[d], jw32))) return st;
+    if ((st = upload(h, &h->d_dd64[d], a.DD))) return st;
+    if ((st = upload(h, &h->d_dd32[d], dd32))) return st;
     if ((st = upload(h, &h->d_fac64[d], fac))) return st;
     if ((st = upload(h, &h->d_tfac64[d], tfac))) return st;
     if ((st = upload(h, &h->d_fac32[d], fac32))) return st;
@@ -970,7 +980,7 @@ int ads_heat_adjoint(ads_handle* h, int K, int ck, const double* u0, const doubl
     if (loss) *loss = 0.5 * Lval;
     if (!grad_u0 && !grad_kappa_qp) return ADS_OK;
     AxisTab<double> t64[3];
-    for (int d = 0; d < 3; ++d) { t64[d].nn = h->d_nn64[d]; t64[d].jw = h->d_jw64[d]; }
+    for (int d = 0; d < 3; ++d) { t64[d].nn = h->d_nn64[d]; t64[d].jw = h->d_jw64[d]; t64[d].dd = h->d_dd64[d]; }
     for (int c = ncp - 1; c >= 0; --c) {
       const int s0 = c * ck, s1 = std::min(s0 + ck, K);
       // recompute the segment's states u^{s0} .. u^{s1-1}

@@ -47,6 +47,7 @@ template <typename T>
 struct AxisTab {
   const T* nn;   // [E][Q][P+1][2]: value (d=0) and derivative (d=1) of local function a at point k
   const T* jw;   // [E][Q]: J(e) * W(k)
+  const T* dd;   // [E][Q][P]: difference weights D_b, b = 1..P (dN_b = D_b - D_{b+1})
 };
 
 // Factors of the banded LU of one 1-D matrix, as rows of length N:
@@ -81,6 +82,7 @@ struct AssembleArgs {
   const double* fqp;   // qp-grid layout (qx + QX*(qy + QY*qz)), may be null
   const double* kqp;   // same layout, may be null
   double* l2part;      // per CTA: l2 partial at [cta], max |written value| at [grid + cta]
+  const double* uscale;  // FP32 heat form: 2^-e with max |u| < 2^e (coefficients are scaled by it)
   int* err;
 };
 
@@ -159,6 +161,7 @@ enum ScalarSlot {
   SC_C_IN,          // correction: input scale
   SC_C_OUT,         // correction: output scale
   SC_DOT,           // result of launch_dot
+  SC_USCALE,        // 2^-e with max |u| < 2^e, for the FP32 assembly
   SC_COUNT = 16
 };
 enum FlagSlot {
@@ -179,6 +182,8 @@ cudaError_t launch_decide(const double* part, int n, double tol, bool count_iter
 cudaError_t launch_norm_f(const double* F, const Geometry& g, double* part, int nparts, double* scal,
                           cudaStream_t s);
 cudaError_t launch_step_reset(double* scal, int* flags, cudaStream_t s);
+// scal[SC_USCALE] = 2^-e for max |u| over n entries (power-of-two scale of the FP32 assembly)
+cudaError_t launch_uscale(const double* u, long long n, double* part, int nparts, double* scal, cudaStream_t s);
 cudaError_t launch_record(const double* scal, int* flags, double* hist, int cap, cudaStream_t s);
 
 // layout conversions between the per-point (kx,ky,kz,ex,ey,ez) layout and the
@@ -201,6 +206,66 @@ cudaError_t launch_kappa_grad(const Geometry& g, const double* u, const double* 
 cudaError_t measure_fma_peak(bool fp64, double* tflops);
 
 size_t assemble_smem_bytes(int P, bool fp32);
+
+// ---------------------------------------------------------------------------
+// FP64 <-> FP32 conversions with integer operations only (GB300 runs FP64 at
+// 1/64 of FP32, conversions included): power-of-two scale 2^sexp folded into
+// the exponent; results below the float range flush to zero.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float d2f_scaled(double d, int sexp) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  const int ed = (int)((b >> 52) & 0x7ffull);
+  const int ef = ed + sexp - 896;  // biased float exponent after scaling (1023 - 127)
+  if (ed == 0 || ef < 1) return __uint_as_float(sign);
+  if (ed == 0x7ff || ef > 254) return (float)(d * ldexp(1.0, sexp));  // inf/nan/overflow
+  const unsigned long long m = b & 0xfffffffffffffull;
+  const unsigned m23 = (unsigned)(m >> 29);
+  const unsigned rem = (unsigned)(m & 0x1fffffffull);
+  unsigned r = sign | ((unsigned)ef << 23) | m23;
+  if (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) r += 1u;  // carry rounds into the exponent
+  return __uint_as_float(r);
+}
+
+// float -> double (exact) times 2^sexp
+__device__ __forceinline__ double f2d_scaled(float f, int sexp) {
+  const unsigned b = __float_as_uint(f);
+  const int e = (int)((b >> 23) & 0xffu);
+  const int ed = e + 896 + sexp;
+  if ((b & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)(b >> 31) << 63));
+  if (e == 0 || e == 0xff || ed < 1 || ed > 2046) return (double)f * ldexp(1.0, sexp);
+  const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) | ((unsigned long long)ed << 52) |
+                                  ((unsigned long long)(b & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+// d * 2^sexp = hi + lo with hi the nearest float and lo the float nearest to
+// the remainder (hi + lo carries ~48 bits); both zero below the float range
+__device__ __forceinline__ void split_scaled(double d, int sexp, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  const int ed = (int)((b >> 52) & 0x7ffull);
+  const int ef = ed + sexp - 896;
+  lo = 0.f;
+  if (ed == 0 || ef < 1) { hi = __uint_as_float(sign); return; }
+  if (ed == 0x7ff || ef > 254) { hi = (float)(d * ldexp(1.0, sexp)); return; }
+  const unsigned long long m = b & 0xfffffffffffffull;
+  const unsigned m23 = (unsigned)(m >> 29);
+  const unsigned rem = (unsigned)(m & 0x1fffffffull);
+  const bool up = rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u));
+  hi = __uint_as_float((sign | ((unsigned)ef << 23) | m23) + (up ? 1u : 0u));
+  // remainder in units of the double's last mantissa bit, 2^(ef - 179)
+  const int rs = (int)rem - (up ? (1 << 29) : 0);
+  if (rs != 0 && ef >= 53) {
+    const float unit = __uint_as_float((unsigned)(ef - 52) << 23);
+    const float v = (float)rs * unit;
+    lo = sign ? -v : v;
+  }
+}
+
+__device__ __forceinline__ int pow2_exp(double s) {
+  return (int)(((unsigned long long)__double_as_longlong(s) >> 52) & 0x7ffull) - 1023;
+}
 size_t sweep_smem_bytes(int tin, int tc, int P, int L, int nchunk);
 
 }  // namespace ads

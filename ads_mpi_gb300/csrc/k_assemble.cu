@@ -65,20 +65,23 @@ struct AsmLayout {
   static constexpr int RF = P + 1;  // accumulator ring
   static constexpr int NT = Q * (P + 1) * 2;  // table entries per element
   static constexpr bool F32 = sizeof(T) == 4;
+  static constexpr int NZF = F32 ? 4 : 2;  // z fields: value, d/dz (+ y and x differences in FP32)
+  static constexpr int NYF = F32 ? 4 : 3;  // y fields
   static_assert(CX == 32, "footprint must be one warp wide");
   // offsets in bytes
   static constexpr size_t o_cring = 0;                                          // double [RC][NCOL]
-  static constexpr size_t o_tring = o_cring + sizeof(double) * RC * NCOL;       // T [RC][NCOL] (FP32 only)
-  static constexpr size_t o_fring = o_tring + (F32 ? sizeof(float) * RC * NCOL : 0);
+  static constexpr size_t o_tring = o_cring + sizeof(double) * RC * NCOL;       // float hi, lo [RC][NCOL] (FP32 only)
+  static constexpr size_t o_fring = o_tring + (F32 ? 2 * sizeof(float) * RC * NCOL : 0);
   static constexpr size_t fring_bytes = F32 ? 2 * sizeof(float) * RF * NCOL : sizeof(double) * RF * NCOL;
-  static constexpr size_t o_za = o_fring + fring_bytes;                         // T [Q][NCOL]
-  static constexpr size_t o_zb = o_za + sizeof(T) * Q * NCOL;
-  static constexpr size_t o_y = o_zb + sizeof(T) * Q * NCOL;                    // T [3][QY][CX]
-  static constexpr size_t o_h = o_y + sizeof(T) * 3 * QY * CX;                  // T [3][QY][CX]
+  static constexpr size_t o_za = o_fring + fring_bytes;                         // T [NZF][Q][NCOL]
+  static constexpr size_t o_y = o_za + sizeof(T) * NZF * Q * NCOL;              // T [NYF][QY][CX]
+  static constexpr size_t o_h = o_y + sizeof(T) * NYF * QY * CX;                // T [3][QY][CX]
   static constexpr size_t o_ny = o_h + sizeof(T) * 3 * QY * CX;
   static constexpr size_t o_jwy = o_ny + sizeof(T) * TY * NT;
-  static constexpr size_t o_nz = o_jwy + sizeof(T) * TY * Q;
-  static constexpr size_t o_jwz = o_nz + sizeof(T) * NT;
+  static constexpr size_t o_dy = o_jwy + sizeof(T) * TY * Q;                    // T [TY][Q][P]
+  static constexpr size_t o_nz = o_dy + sizeof(T) * TY * Q * P;
+  static constexpr size_t o_dz = o_nz + sizeof(T) * NT;                         // T [Q][P]
+  static constexpr size_t o_jwz = o_dz + sizeof(T) * Q * P;
   static constexpr size_t o_red = (o_jwz + sizeof(T) * Q + 15) / 16 * 16;
   static constexpr size_t bytes = o_red + 2 * sizeof(double) * (AS_THREADS / 32);
 };
@@ -101,18 +104,6 @@ __device__ __forceinline__ void issue_plane(double* ring_plane, const double* __
   }
 }
 
-// exact float -> double with integer operations (normal numbers; the rest
-// takes the conversion instruction)
-__device__ __forceinline__ double f2d_exact(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned e = (b >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu) return (double)f;
-  const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) |
-                                  ((unsigned long long)(e + 896u) << 52) |
-                                  ((unsigned long long)(b & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)bits);
-}
-
 // (hi, lo) += v without rounding loss (two-sum)
 __device__ __forceinline__ void two_sum_add(float& hi, float& lo, float v) {
   const float s = hi + v;
@@ -131,18 +122,29 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
   constexpr bool HEAT = (FORM == ADS_FORM_HEAT);
   constexpr bool F32 = L::F32;
   constexpr bool G0_ZERO = HEAT && INCR && !HAS_F;  // increment form without source: no v-term
+  // FP32 heat form: coefficients scaled by a power of two and split into
+  // float (hi, lo); the gradient is interpolated from coefficient differences
+  // (hi_a - hi_b) + (lo_a - lo_b), which carry no cancellation, with the
+  // difference weights D_b (dN_b = D_b - D_{b+1})
+  constexpr bool DIFF = F32 && HEAT;
 
   extern __shared__ __align__(16) unsigned char smem[];
   double* cring = reinterpret_cast<double*>(smem + L::o_cring);
-  float* tring = reinterpret_cast<float*>(smem + L::o_tring);
+  float* thi = reinterpret_cast<float*>(smem + L::o_tring);
+  float* tlo = thi + RC * NCOL;
   double* fr64 = reinterpret_cast<double*>(smem + L::o_fring);
   float* frhi = reinterpret_cast<float*>(smem + L::o_fring);
   float* frlo = frhi + RF * NCOL;
   T* ZA = reinterpret_cast<T*>(smem + L::o_za);
-  T* ZB = reinterpret_cast<T*>(smem + L::o_zb);
+  T* ZB = ZA + Q * NCOL;
+  T* ZAY = ZB + Q * NCOL;  // DIFF only
+  T* ZAX = ZAY + Q * NCOL;
   T* Y0 = reinterpret_cast<T*>(smem + L::o_y);
   T* Y1 = Y0 + QY * CX;
   T* Y2 = Y1 + QY * CX;
+  T* Y3 = Y2 + QY * CX;    // DIFF only
+  T* DYs = reinterpret_cast<T*>(smem + L::o_dy);
+  T* DZs = reinterpret_cast<T*>(smem + L::o_dz);
   T* H0 = reinterpret_cast<T*>(smem + L::o_h);
   T* H1 = H0 + QY * CX;
   T* H2 = H1 + QY * CX;
@@ -163,6 +165,8 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
   const int nitems = a.nix * a.niy * a.niz;
   // this thread's (element row, footprint column) for the y/z stages
   const int my_ey = tid / CX, my_cx = tid % CX;
+  // power-of-two scale of the coefficients (FP32 heat form)
+  const int uexp = DIFF ? pow2_exp(*a.uscale) : 0;  // coefficients are multiplied by 2^uexp
 
   double l2_thread = 0.0;
   // max |value| written by this thread, as the bit pattern of a non-negative
@@ -183,6 +187,7 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
     // per-lane x tables (element x0 + lane; lanes >= TX have no element)
     T nx[Q][P + 1][2];
     T jwx[Q];
+    T dx[DIFF ? Q : 1][DIFF ? P : 1];
     const bool lane_elem = (lane < TX) && (x0 + lane < Ex);
     {
       const int ex = x0 + lane;
@@ -194,6 +199,16 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
           nx[k][b][0] = lane_elem ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 0] : T(0);
           nx[k][b][1] = lane_elem ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 1] : T(0);
         }
+        if constexpr (DIFF) {
+#pragma unroll
+          for (int b = 0; b < P; ++b) dx[k][b] = lane_elem ? tb.x.dd[((size_t)ex * Q + k) * P + b] : T(0);
+        }
+      }
+    }
+    if (DIFF) {
+      for (int i = tid; i < TY * Q * P; i += AS_THREADS) {
+        const int ey = y0 + i / (Q * P);
+        DYs[i] = (ey < Ey) ? tb.y.dd[(size_t)ey * Q * P + (i % (Q * P))] : T(0);
       }
     }
     for (int i = tid; i < TY * L::NT; i += AS_THREADS) {
@@ -228,39 +243,73 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
       cp_async_commit();
       for (int i = tid; i < L::NT; i += AS_THREADS) NZs[i] = tb.z.nn[(size_t)ez * L::NT + i];
       for (int i = tid; i < Q; i += AS_THREADS) JWZs[i] = tb.z.jw[(size_t)ez * Q + i];
+      if (DIFF)
+        for (int i = tid; i < Q * P; i += AS_THREADS) DZs[i] = tb.z.dd[(size_t)ez * Q * P + i];
       cp_async_wait<1>();
       __syncthreads();
 
-      // FP32: convert each coefficient plane once, when it arrives
-      if (HEAT && F32) {
+      // FP32: split each coefficient plane once, when it arrives
+      if (DIFF) {
         const int zlo = (ez == ez0) ? ez : ez + P;
         for (int z = zlo; z <= ez + P; ++z) {
           const double* src = cring + (z % RC) * NCOL;
-          float* dst = tring + (z % RC) * NCOL;
-          for (int i = tid; i < NCOL; i += AS_THREADS) dst[i] = (float)src[i];
+          float* dh = thi + (z % RC) * NCOL;
+          float* dl = tlo + (z % RC) * NCOL;
+          for (int i = tid; i < NCOL; i += AS_THREADS) split_scaled(src[i], uexp, dh[i], dl[i]);
         }
         __syncthreads();
       }
 
-      // ---- z interpolation: ZA = sum_b Nz C, ZB = sum_b dNz C, per column ----
+      // ---- z interpolation, per column: ZA = sum_b Nz C, ZB = d/dz; in FP32
+      //      also the z-interpolated y and x coefficient differences ----
       if (HEAT) {
         for (int col = tid; col < NCOL; col += AS_THREADS) {
-          T c[P + 1];
-#pragma unroll
-          for (int b = 0; b <= P; ++b) {
-            if (F32) c[b] = (T)tring[((ez + b) % RC) * NCOL + col];
-            else c[b] = (T)cring[((ez + b) % RC) * NCOL + col];
-          }
-#pragma unroll
-          for (int kz = 0; kz < Q; ++kz) {
-            T za = T(0), zb = T(0);
+          if constexpr (DIFF) {
+            const int cy = col / CX, cx = col % CX;
+            T c[P + 1], dz[P + 1], dyv[P + 1], dxv[P + 1];
 #pragma unroll
             for (int b = 0; b <= P; ++b) {
-              za += NZs[(kz * (P + 1) + b) * 2 + 0] * c[b];
-              zb += NZs[(kz * (P + 1) + b) * 2 + 1] * c[b];
+              const int o = ((ez + b) % RC) * NCOL + col;
+              const float h = thi[o], l = tlo[o];
+              c[b] = h;
+              dyv[b] = (cy > 0) ? (h - thi[o - CX]) + (l - tlo[o - CX]) : T(0);
+              dxv[b] = (cx > 0) ? (h - thi[o - 1]) + (l - tlo[o - 1]) : T(0);
+              if (b > 0) {
+                const int op = ((ez + b - 1) % RC) * NCOL + col;
+                dz[b] = (h - thi[op]) + (l - tlo[op]);
+              }
             }
-            ZA[kz * NCOL + col] = za;
-            ZB[kz * NCOL + col] = zb;
+#pragma unroll
+            for (int kz = 0; kz < Q; ++kz) {
+              T za = T(0), zb = T(0), zy = T(0), zx = T(0);
+#pragma unroll
+              for (int b = 0; b <= P; ++b) {
+                const T nzv = NZs[(kz * (P + 1) + b) * 2 + 0];
+                za += nzv * c[b];
+                zy += nzv * dyv[b];
+                zx += nzv * dxv[b];
+                if (b > 0) zb += DZs[kz * P + (b - 1)] * dz[b];
+              }
+              ZA[kz * NCOL + col] = za;
+              ZB[kz * NCOL + col] = zb;
+              ZAY[kz * NCOL + col] = zy;
+              ZAX[kz * NCOL + col] = zx;
+            }
+          } else {
+            T c[P + 1];
+#pragma unroll
+            for (int b = 0; b <= P; ++b) c[b] = (T)cring[((ez + b) % RC) * NCOL + col];
+#pragma unroll
+            for (int kz = 0; kz < Q; ++kz) {
+              T za = T(0), zb = T(0);
+#pragma unroll
+              for (int b = 0; b <= P; ++b) {
+                za += NZs[(kz * (P + 1) + b) * 2 + 0] * c[b];
+                zb += NZs[(kz * (P + 1) + b) * 2 + 1] * c[b];
+              }
+              ZA[kz * NCOL + col] = za;
+              ZB[kz * NCOL + col] = zb;
+            }
           }
         }
         __syncthreads();
@@ -277,27 +326,37 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
       for (int kz = 0; kz < Q; ++kz) {
         // ---- y interpolation, one (element row, column) per thread ----
         if (HEAT) {
-          T za[P + 1], zb[P + 1];
+          T za[P + 1], zb[P + 1], zy[P + 1], zx[P + 1];
 #pragma unroll
           for (int b = 0; b <= P; ++b) {
             za[b] = ZA[kz * NCOL + (my_ey + b) * CX + my_cx];
             zb[b] = ZB[kz * NCOL + (my_ey + b) * CX + my_cx];
+            if constexpr (DIFF) {
+              zy[b] = ZAY[kz * NCOL + (my_ey + b) * CX + my_cx];
+              zx[b] = ZAX[kz * NCOL + (my_ey + b) * CX + my_cx];
+            }
           }
 #pragma unroll
           for (int ky = 0; ky < Q; ++ky) {
-            T y0v = T(0), y1v = T(0), y2v = T(0);
+            T y0v = T(0), y1v = T(0), y2v = T(0), y3v = T(0);
 #pragma unroll
             for (int b = 0; b <= P; ++b) {
               const T nyv = NYs[my_ey * L::NT + (ky * (P + 1) + b) * 2 + 0];
-              const T dny = NYs[my_ey * L::NT + (ky * (P + 1) + b) * 2 + 1];
               y0v += nyv * za[b];
-              y1v += dny * za[b];
               y2v += nyv * zb[b];
+              if constexpr (DIFF) {
+                y3v += nyv * zx[b];
+                if (b > 0) y1v += DYs[(my_ey * Q + ky) * P + (b - 1)] * zy[b];
+              } else {
+                const T dny = NYs[my_ey * L::NT + (ky * (P + 1) + b) * 2 + 1];
+                y1v += dny * za[b];
+              }
             }
             const int qy = my_ey * Q + ky;
             Y0[qy * CX + my_cx] = y0v;
             Y1[qy * CX + my_cx] = y1v;
             Y2[qy * CX + my_cx] = y2v;
+            if constexpr (DIFF) Y3[qy * CX + my_cx] = y3v;
           }
           __syncthreads();
         }
@@ -310,13 +369,14 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
           T h0[P + 1], h1[P + 1], h2[P + 1];
 #pragma unroll
           for (int b = 0; b <= P; ++b) { h0[b] = T(0); h1[b] = T(0); h2[b] = T(0); }
-          T yv0[P + 1], yv1[P + 1], yv2[P + 1];
+          T yv0[P + 1], yv1[P + 1], yv2[P + 1], yv3[P + 1];
           if (HEAT) {
 #pragma unroll
             for (int b = 0; b <= P; ++b) {
               yv0[b] = lane_elem ? Y0[qy * CX + lane + b] : T(0);
               yv1[b] = lane_elem ? Y1[qy * CX + lane + b] : T(0);
               yv2[b] = lane_elem ? Y2[qy * CX + lane + b] : T(0);
+              if constexpr (DIFF) yv3[b] = (lane_elem && b > 0) ? Y3[qy * CX + lane + b] : T(0);
             }
           }
           const long long qyg = (long long)y0 * Q + qy;
@@ -330,12 +390,20 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
 #pragma unroll
               for (int b = 0; b <= P; ++b) {
                 uu += nx[kx][b][0] * yv0[b];
-                dux += nx[kx][b][1] * yv0[b];
+                if constexpr (DIFF) {
+                  if (b > 0) dux += dx[kx][b - 1] * yv3[b];
+                } else {
+                  dux += nx[kx][b][1] * yv0[b];
+                }
                 duy += nx[kx][b][0] * yv1[b];
                 duz += nx[kx][b][0] * yv2[b];
               }
               T fv = T(0);
-              if (HAS_F) fv = elem_ok ? (T)a.fqp[qidx] : T(0);
+              if (HAS_F) {
+                // in FP32 the source carries the coefficients' scale 2^uexp
+                if constexpr (DIFF) fv = elem_ok ? d2f_scaled(a.fqp[qidx], uexp) : T(0);
+                else fv = elem_ok ? (T)a.fqp[qidx] : T(0);
+              }
               T c;
               if (HAS_K) c = -dt * (elem_ok ? (T)a.kqp[qidx] : T(0)) * s;
               else c = ndtk * s;
@@ -445,7 +513,7 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
           const int x = x0 + cx, y = y0 + cy;
           double v;
           if (F32) {
-            v = f2d_exact(frhi[slot + it]) + f2d_exact(frlo[slot + it]);
+            v = f2d_scaled(frhi[slot + it], -uexp) + f2d_scaled(frlo[slot + it], -uexp);
             frhi[slot + it] = 0.f;
             frlo[slot + it] = 0.f;
           } else {
@@ -473,7 +541,8 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
         const int cy = it / CX, cx = it % CX;
         const int x = x0 + cx, y = y0 + cy;
         if (x < Nx && y < Ny && cz < g.N[2]) {
-          const double v = F32 ? f2d_exact(frhi[slot + it]) + f2d_exact(frlo[slot + it]) : fr64[slot + it];
+          const double v = F32 ? f2d_scaled(frhi[slot + it], -uexp) + f2d_scaled(frlo[slot + it], -uexp)
+                               : fr64[slot + it];
           const bool ownx = (cx < TX) || lastx, owny = (cy < TY) || lasty;
           const int cls = (ownx ? 0 : 1) | (owny ? 0 : 2) | (ownz ? 0 : 4);
           double* dst = (cls == 0) ? a.F : a.shadow + (size_t)(cls - 1) * a.shadow_stride;
@@ -507,7 +576,8 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
       t += red[w];
       m = redm[w] > m ? redm[w] : m;
     }
-    a.l2part[blockIdx.x] = t;
+    // the FP32 heat form integrated (2^uexp u)^2
+    a.l2part[blockIdx.x] = DIFF ? t * ldexp(1.0, -2 * uexp) : t;
     a.l2part[gridDim.x + blockIdx.x] = __longlong_as_double((long long)m);
   }
 }

@@ -242,6 +242,47 @@ cudaError_t launch_norm_f(const double* F, const Geometry& g, double* part, int 
   return cudaGetLastError();
 }
 
+__global__ void k_umax_partial(const double* u, long long n, double* part) {
+  __shared__ unsigned long long sm[256];
+  unsigned long long m = 0ull;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(u[i]) & 0x7fffffffffffffffull;
+    m = b > m ? b : m;
+  }
+  sm[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sm[threadIdx.x] = sm[threadIdx.x + w] > sm[threadIdx.x] ? sm[threadIdx.x + w] : sm[threadIdx.x];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = __longlong_as_double((long long)sm[0]);
+}
+
+__global__ void k_uscale_final(const double* part, int n, double* scal) {
+  if (threadIdx.x >= 32) return;
+  unsigned long long m = 0ull;
+  for (int i = threadIdx.x; i < n; i += 32) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(part[i]);
+    m = b > m ? b : m;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ob = __shfl_down_sync(0xffffffffu, m, o);
+    m = ob > m ? ob : m;
+  }
+  if (threadIdx.x == 0) {
+    int e;
+    (void)pow2_exponent_scale(__longlong_as_double((long long)m), &e);
+    scal[SC_USCALE] = ldexp(1.0, -e);
+  }
+}
+
+cudaError_t launch_uscale(const double* u, long long n, double* part, int nparts, double* scal, cudaStream_t s) {
+  k_umax_partial<<<nparts, 256, 0, s>>>(u, n, part);
+  k_uscale_final<<<1, 32, 0, s>>>(part, nparts, scal);
+  return cudaGetLastError();
+}
+
 __global__ void k_step_reset(double* scal, int* flags) {
   if (threadIdx.x == 0) {
     flags[FL_CONV] = 0;

@@ -114,47 +114,24 @@ __device__ __forceinline__ void bulk_wait_read() {
   asm volatile("cp.async.bulk.wait_group.read %0;\n" ::"n"(N) : "memory");
 }
 
-// ---------------------------------------------------------------------------
-// Conversions without the FP64 pipe (GB300 runs FP64 at 1/64 of FP32): the
-// power-of-two scale 2^sexp is folded into the exponent field.
-// ---------------------------------------------------------------------------
-// double -> float, round to nearest even, times 2^sexp
-__device__ __forceinline__ float d2f_scaled(double d, int sexp) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const unsigned sign = (unsigned)(b >> 63) << 31;
-  const int ed = (int)((b >> 52) & 0x7ffull);
-  const int ef = ed + sexp - 896;  // biased float exponent after scaling (1023 - 127)
-  // values below the float range (and zeros, double denormals) flush to zero:
-  // with the scale putting max |v| in [0.5, 1) they are below 2^-126 of it
-  if (ed == 0 || ef < 1) return __uint_as_float(sign);
-  if (ed == 0x7ff || ef > 254) return (float)(d * ldexp(1.0, sexp));  // inf/nan/overflow
-  const unsigned long long m = b & 0xfffffffffffffull;
-  const unsigned m23 = (unsigned)(m >> 29);
-  const unsigned rem = (unsigned)(m & 0x1fffffffull);
-  unsigned r = sign | ((unsigned)ef << 23) | m23;
-  if (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) r += 1u;  // carry rounds into the exponent
-  return __uint_as_float(r);
-}
-// float -> double (exact), times 2^sexp
-__device__ __forceinline__ double f2d_scaled(float f, int sexp) {
-  const unsigned b = __float_as_uint(f);
-  const int e = (int)((b >> 23) & 0xffu);
-  const int ed = e + 896 + sexp;
-  if ((b & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)(b >> 31) << 63));
-  if (e == 0 || e == 0xff || ed < 1 || ed > 2046) return (double)f * ldexp(1.0, sexp);
-  const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) | ((unsigned long long)ed << 52) |
-                                  ((unsigned long long)(b & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)bits);
-}
 template <typename TC, typename TIn>
 __device__ __forceinline__ TC load_in(TIn v, int sexp, TC scale) {
   if constexpr (sizeof(TIn) == 8 && sizeof(TC) == 4) return d2f_scaled((double)v, sexp);
   else return (TC)v * scale;
 }
-__device__ __forceinline__ int pow2_exp(double s) {
-  return (int)(((unsigned long long)__double_as_longlong(s) >> 52) & 0x7ffull) - 1023;
+// The forward pass keeps y in place of its input.  An FP32 y in an FP64 input
+// slot goes into the slot's first word as it is: a float <-> double
+// conversion would run on the FP64 pipe (1/64 of the FP32 rate on GB300).
+template <typename TC, typename TIn>
+__device__ __forceinline__ void store_y(TIn* S, int si, TC y) {
+  if constexpr (sizeof(TIn) == 8 && sizeof(TC) == 4) reinterpret_cast<float*>(S + si)[0] = y;
+  else S[si] = (TIn)y;
 }
-
+template <typename TC, typename TIn>
+__device__ __forceinline__ TC load_y(const TIn* S, int si) {
+  if constexpr (sizeof(TIn) == 8 && sizeof(TC) == 4) return reinterpret_cast<const float*>(S + si)[0];
+  else return (TC)S[si];
+}
 constexpr int SW_BLK = 8;  // steps per software-pipelined block
 
 // One warp per CTA, persistent over tiles of 32 lines.  Shared memory holds
@@ -239,7 +216,7 @@ __global__ void __launch_bounds__(SW_LANES)
 #pragma unroll
         for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
         prev[0] = y;
-        S[si] = (TIn)y;
+        store_y(S, si, y);
       };
       int s = 0;
       for (; s < RAMP && s < L + RAMP; ++s) {
@@ -271,7 +248,7 @@ __global__ void __launch_bounds__(SW_LANES)
           bv[t] = y;
         }
 #pragma unroll
-        for (int t = 0; t < SW_BLK; ++t) S[si[t]] = (TIn)bv[t];
+        for (int t = 0; t < SW_BLK; ++t) store_y(S, si[t], bv[t]);
       }
       for (; s < L + RAMP; ++s) {
         const int i = s - j;
@@ -295,7 +272,7 @@ __global__ void __launch_bounds__(SW_LANES)
         if (MODE == 3) {
           x = load_in<TC>(S[s_index(i, j)], 0, TC(1));
         } else {
-          const TC y = (TC)S[s_index(i, j)];
+          const TC y = load_y<TC>(S, s_index(i, j));
           x = TRANS ? y : BS[i] * y;
 #pragma unroll
           for (int m = P; m >= 2; --m) x -= Fs[(P + 1 + m) * L + i] * nxt[m - 1];
@@ -320,7 +297,7 @@ __global__ void __launch_bounds__(SW_LANES)
           for (int t = 0; t < SW_BLK; ++t) {
             const int i = L - 1 - (s + t - j);
             if (MODE == 3) yv[t] = load_in<TC>(S[s_index(i, j)], 0, TC(1));
-            else yv[t] = (TC)S[s_index(i, j)];
+            else yv[t] = load_y<TC>(S, s_index(i, j));
             if (MODE != 3) {
               gv[t][0] = TRANS ? TC(1) : BS[i];
 #pragma unroll

@@ -285,11 +285,9 @@ def test_full_size_constant_state_is_steady(ads_mod, prec):
     g.set_coeffs(np.full(g.N, 2.5))
     g.set_form(ads_mod.FORM_HEAT, kappa=1.0, dt=1e-5)
     g.step()
-    # FP32: the B-spline derivative weights of an element sum to zero only up
-    # to rounding, so grad(constant) is ~eps32 * c * p / h and the stiffness
-    # term turns that into ~1e-6 relative noise in the increment
-    tol = 1e-12 if prec == 0 else 1e-5
-    assert np.abs(g.coeffs() - 2.5).max() < tol
+    # the FP32 form interpolates gradients from coefficient differences, which
+    # are exactly zero for a constant state: the step is exact in both modes
+    assert np.abs(g.coeffs() - 2.5).max() < 1e-12
     if prec == 1:
         assert g.stats()["rel_residual"] <= 1e-10
 
