@@ -66,6 +66,8 @@ ABI = [
     ("ads_reorder", [ctypes.c_void_p, ctypes.c_int, _dp, _dp], ctypes.c_int),
     ("ads_set_coeffs_device", [ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     ("ads_get_coeffs_device", [ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    ("ads_residual_noalloc", [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _dp],
+     ctypes.c_int),
     ("ads_heat_adjoint", [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
     ("ads_axis_setup", [ctypes.c_int, ctypes.c_int, _dp, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
     ("ads_fma_peak", [ctypes.c_int, ctypes.c_int, _dp], ctypes.c_int),

@@ -1101,3 +1101,23 @@ int ads_launch_count_reset(ads_handle* h) {
 }
 
 }  // extern "C"
+
+namespace ads {
+
+void handle_noalloc_view(ads_handle* h, NoallocView* v) {
+  v->dev = h->dev;
+  v->P = h->P;
+  v->grid = h->res_grid;
+  v->stream = h->stream;
+  v->args = residual_args(h, nullptr, nullptr, nullptr);
+  v->args.g.PX = h->g.N[0];
+  v->args.part = nullptr;
+  v->args.err = nullptr;
+  v->launches = &h->launches;
+}
+
+int handle_fail(ads_handle* h, int code, const std::string& msg) { return fail(h, code, msg); }
+
+int handle_cuda_fail(ads_handle* h, cudaError_t e, const char* where) { return cuda_fail(h, e, where); }
+
+}  // namespace ads

@@ -207,6 +207,19 @@ cudaError_t measure_fma_peak(bool fp64, double* tflops);
 
 size_t assemble_smem_bytes(int P, bool fp32);
 
+// What ads_residual_noalloc (noalloc.cu) reads from a handle: the residual
+// kernel's tiling, the mass bands and a geometry whose x pitch is the dense
+// Nx of caller-owned arrays.  No buffer of the handle is used.
+struct NoallocView {
+  int dev = 0, P = 0, grid = 0;
+  cudaStream_t stream = nullptr;
+  ResidualArgs args{};
+  long long* launches = nullptr;
+};
+void handle_noalloc_view(ads_handle* h, NoallocView* v);
+int handle_fail(ads_handle* h, int code, const std::string& msg);
+int handle_cuda_fail(ads_handle* h, cudaError_t e, const char* where);
+
 // ---------------------------------------------------------------------------
 // FP64 <-> FP32 conversions with integer operations only (GB300 runs FP64 at
 // 1/64 of FP32, conversions included): power-of-two scale 2^sexp folded into

@@ -136,6 +136,26 @@ int ads_reorder(ads_handle* h, int kind, const double* in, double* out);
 int ads_set_coeffs_device(ads_handle* h, const double* d_u);
 int ads_get_coeffs_device(ads_handle* h, double* d_u);
 
+/* No counterpart in the reference.  For callers that must not allocate device
+ * memory — a program whose device memory is all reserved up front by its own
+ * pool, or one that keeps other streams busy and cannot take the device-wide
+ * synchronisation of cudaFree — the residual r = F - (Mx(x)My(x)Mz) u of the
+ * handle's mass matrix on caller-owned device arrays (dense, x fastest, ndof
+ * doubles each; d_F may be NULL for r = M u; d_r may equal d_F but must not
+ * overlap d_u).  norms (host, may be NULL) receives ||r||^2, ||F||^2 and
+ * max|r|; when it is given the call waits for the handle's stream, otherwise
+ * it only enqueues.  Its working storage is a fixed device array compiled
+ * into the library (3 * ADS_NOALLOC_MAX_CTAS + 8 doubles, 196,672 bytes per
+ * GPU, held until exit); it calls no cudaMalloc, cudaFree or allocating
+ * library routine.  Sizes needing more than ADS_NOALLOC_MAX_CTAS residual
+ * tiles of 32 x 8 x 32 DOFs (about 67M DOFs) return ADS_ERR_ARG.  The array
+ * is shared by all calls on a device and keeps the last call's contents:
+ * calls that overlap on the GPU race on it.  The first call on each device
+ * looks up the array's address; make it before any stream capture. */
+#define ADS_NOALLOC_MAX_CTAS 8192
+int ads_residual_noalloc(ads_handle* h, const double* d_F, const double* d_u, double* d_r,
+                         double norms[3]);
+
 /* Adjoint of K explicit heat steps from u0 with the current HEAT form:
  * loss = 1/2 (u^K - u_target)^T (Mx(x)My(x)Mz) (u^K - u_target).
  * grad_u0 (ndof) and grad_kappa_qp (quadrature-point layout; only with a
