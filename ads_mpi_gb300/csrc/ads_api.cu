@@ -78,6 +78,7 @@ struct ads_handle {
   double* d_F = nullptr;
   double* d_r = nullptr;
   double* d_delta = nullptr;  // mixed: increment of the heat step
+  float* d_g32 = nullptr;     // mixed: the FP32 solve's scaled input (G, then each residual), L0
   double* d_wA = nullptr;  // L1 (double-sized; float view uses the same memory)
   double* d_wB = nullptr;  // L2
   double* d_shadow = nullptr;
@@ -97,9 +98,10 @@ struct ads_handle {
   int norm_parts = 0;
 
   // tensor maps
-  CUtensorMap tm_F_in64{}, tm_r_in64{}, tm_u_out64{}, tm_r_out64{};
-  CUtensorMap tm_wA_out64{}, tm_wA_in64{}, tm_wB_out64{}, tm_wB_in64{};
-  CUtensorMap tm_wA_out32{}, tm_wA_in32{}, tm_wB_out32{}, tm_wB_in32{};
+  // TMA store maps of the sweeps' transposed outputs
+  CUtensorMap tm_u_out64{}, tm_r_out64{};
+  CUtensorMap tm_wA_out64{}, tm_wB_out64{};
+  CUtensorMap tm_wA_out32{}, tm_wB_out32{};
 
   // form
   bool has_form = false;
@@ -220,34 +222,36 @@ bool encode(CUtensorMap* m, void* base, bool fp32, cuuint64_t d0, cuuint64_t d1,
 
 // Layout maps: L0 dims (Nx,Ny,Nz) pitch PX; L1 (Ny,Nx,Nz) pitch PY; L2 (Nz,Nx,Ny) pitch PZ.
 // Sweep input boxes are (CH, lanes...) and output boxes (32 lanes, line...).
-bool make_l0_in(const ads_handle* h, CUtensorMap* m, void* base, bool f32) {
-  return encode(m, base, f32, h->g.N[0], h->g.N[1], h->g.N[2], h->g.PX, SW_CH, SW_LANES, 1);
-}
 bool make_l0_out(const ads_handle* h, CUtensorMap* m, void* base, bool f32) {
   return encode(m, base, f32, h->g.N[0], h->g.N[1], h->g.N[2], h->g.PX, SW_LANES, 1, SW_CH);
 }
 bool make_l1_out(const ads_handle* h, CUtensorMap* m, void* base, bool f32) {
   return encode(m, base, f32, h->g.N[1], h->g.N[0], h->g.N[2], h->g.PY, SW_LANES, SW_CH, 1);
 }
-bool make_l1_in(const ads_handle* h, CUtensorMap* m, void* base, bool f32) {
-  return encode(m, base, f32, h->g.N[1], h->g.N[0], h->g.N[2], h->g.PY, SW_CH, 1, SW_LANES);
-}
 bool make_l2_out(const ads_handle* h, CUtensorMap* m, void* base, bool f32) {
   return encode(m, base, f32, h->g.N[2], h->g.N[0], h->g.N[1], h->g.PZ, SW_LANES, 1, SW_CH);
 }
-bool make_l2_in(const ads_handle* h, CUtensorMap* m, void* base, bool f32) {
-  return encode(m, base, f32, h->g.N[2], h->g.N[0], h->g.N[1], h->g.PZ, SW_CH, SW_LANES, 1);
-}
 
-// sweep along `axis` (0: x, L0->L1; 1: y, L1->L2; 2: z, L2->L0)
-SweepArgs sweep_args(const ads_handle* h, int axis, const void* fac) {
+// sweep along `axis` (0: x, L0->L1; 1: y, L1->L2; 2: z, L2->L0) reading `in`,
+// an array in that axis' input layout (L0, L1 or L2)
+SweepArgs sweep_args(const ads_handle* h, int axis, const void* fac, const void* in) {
   SweepArgs a{};
   const int* N = h->g.N;
+  const Geometry& g = h->g;
   a.L = N[axis];
-  a.nchunk = (a.L + SW_CH - 1) / SW_CH;
-  if (axis == 0) { a.lanes_total = N[1]; a.lane_dim = 1; a.out_line_dim = 1; a.third_extent = N[2]; }
-  if (axis == 1) { a.lanes_total = N[2]; a.lane_dim = 2; a.out_line_dim = 2; a.third_extent = N[0]; }
-  if (axis == 2) { a.lanes_total = N[0]; a.lane_dim = 1; a.out_line_dim = 2; a.third_extent = N[1]; }
+  a.in = in;
+  if (axis == 0) {  // lines y, tiles over z: x + PX (y + Ny z)
+    a.lanes_total = N[1]; a.lane_dim = 1; a.out_line_dim = 1; a.third_extent = N[2];
+    a.in_ls = g.PX; a.in_t3s = g.PX * (long long)N[1];
+  }
+  if (axis == 1) {  // lines z, tiles over x: y + PY (x + Nx z)
+    a.lanes_total = N[2]; a.lane_dim = 2; a.out_line_dim = 2; a.third_extent = N[0];
+    a.in_ls = g.PY * (long long)N[0]; a.in_t3s = g.PY;
+  }
+  if (axis == 2) {  // lines x, tiles over y: z + PZ (x + Nx y)
+    a.lanes_total = N[0]; a.lane_dim = 1; a.out_line_dim = 2; a.third_extent = N[1];
+    a.in_ls = g.PZ; a.in_t3s = g.PZ * (long long)N[0];
+  }
   a.out_third_extent = a.third_extent;
   a.tiles_lane = (a.lanes_total + SW_LANES - 1) / SW_LANES;
   a.fac = fac;
@@ -332,72 +336,82 @@ int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool 
       launch_assemble(fp32, incr, a, tx, ty, tz, h->asm_grid, &used, h->stream));
   FixupArgs f = fixup_args(h, F);
   f.nl2 = used;
+  if (fp32 && incr) f.g32 = h->d_g32;  // the heat increment also feeds the FP32 solve as float
   RUN(h, "fixup", 1, launch_fixup(f, h->stream));
   return ADS_OK;
 }
 
-// FP64 Kronecker solve: F (L0) -> out (L0 via the map tm_out)
-int enqueue_solve64(ads_handle* h, const CUtensorMap* tm_in, const CUtensorMap* tm_out, bool trans) {
+// FP64 Kronecker solve: in (L0) -> out (L0 via the map tm_out)
+int enqueue_solve64(ads_handle* h, const double* in, const CUtensorMap* tm_out, bool trans) {
   double* const* fac = trans ? h->d_tfac64 : h->d_fac64;
-  SweepArgs ax = sweep_args(h, 0, fac[0]);
-  RUN(h, "sweep_x_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, tm_in, &h->tm_wA_out64, ax, sweep_grid(h, 0), h->stream));
-  SweepArgs ay = sweep_args(h, 1, fac[1]);
-  RUN(h, "sweep_y_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, &h->tm_wA_in64, &h->tm_wB_out64, ay, sweep_grid(h, 1), h->stream));
-  SweepArgs az = sweep_args(h, 2, fac[2]);
-  RUN(h, "sweep_z_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, &h->tm_wB_in64, tm_out, az, sweep_grid(h, 2), h->stream));
+  SweepArgs ax = sweep_args(h, 0, fac[0], in);
+  RUN(h, "sweep_x_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, &h->tm_wA_out64, ax, sweep_grid(h, 0), h->stream));
+  SweepArgs ay = sweep_args(h, 1, fac[1], h->d_wA);
+  RUN(h, "sweep_y_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, &h->tm_wB_out64, ay, sweep_grid(h, 1), h->stream));
+  SweepArgs az = sweep_args(h, 2, fac[2], h->d_wB);
+  RUN(h, "sweep_z_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, tm_out, az, sweep_grid(h, 2), h->stream));
   return ADS_OK;
 }
 
-// FP32 Kronecker solve of a double input (L0) into out: mode 1 (out = s x) or 2 (out += s x)
-int enqueue_solve32(ads_handle* h, const CUtensorMap* tm_in, const double* in_scale, const double* out_scale,
+// FP32 Kronecker solve of an L0 input (tin 0: double, scaled by *in_scale on
+// load; tin 1: float, already scaled) into out: mode 1 (out = s x) or 2 (out += s x)
+int enqueue_solve32(ads_handle* h, const void* in, int tin, const double* in_scale, const double* out_scale,
                     int final_mode, const int* skip, const char* tag, double* out) {
-  SweepArgs ax = sweep_args(h, 0, h->d_fac32[0]);
+  SweepArgs ax = sweep_args(h, 0, h->d_fac32[0], in);
   ax.in_scale_dev = in_scale;
   ax.skip_flag = skip;
   std::string nx = std::string("sweep_x_f32") + tag, ny = std::string("sweep_y_f32") + tag,
               nz = std::string("sweep_z_f32") + tag;
-  RUN(h, nx.c_str(), 1, launch_sweep(h->P, 0, 1, 0, false, tm_in, &h->tm_wA_out32, ax, sweep_grid(h, 0), h->stream));
-  SweepArgs ay = sweep_args(h, 1, h->d_fac32[1]);
+  RUN(h, nx.c_str(), 1, launch_sweep(h->P, tin, 1, 0, false, &h->tm_wA_out32, ax, sweep_grid(h, 0), h->stream));
+  SweepArgs ay = sweep_args(h, 1, h->d_fac32[1], h->d_wA);
   ay.skip_flag = skip;
-  RUN(h, ny.c_str(), 1, launch_sweep(h->P, 1, 1, 0, false, &h->tm_wA_in32, &h->tm_wB_out32, ay, sweep_grid(h, 1), h->stream));
-  SweepArgs az = sweep_args(h, 2, h->d_fac32[2]);
+  RUN(h, ny.c_str(), 1, launch_sweep(h->P, 1, 1, 0, false, &h->tm_wB_out32, ay, sweep_grid(h, 1), h->stream));
+  SweepArgs az = sweep_args(h, 2, h->d_fac32[2], h->d_wB);
   az.out_scale_dev = out_scale;
   az.skip_flag = skip;
   az.out = out;
-  RUN(h, nz.c_str(), 1, launch_sweep(h->P, 1, 1, final_mode, false, &h->tm_wB_in32, &h->tm_wB_in32, az, sweep_grid(h, 2), h->stream));
+  RUN(h, nz.c_str(), 1, launch_sweep(h->P, 1, 1, final_mode, false, &h->tm_wB_out32, az,  /* map unused */ sweep_grid(h, 2), h->stream));
   return ADS_OK;
 }
 
 // Mixed-precision Kronecker solve of d_F into x with FP64 iterative refinement:
 // x = M^{-1} F by FP32 sweeps, then up to max_refine corrections from the FP64
 // residual F - M x, stopping once ||F - M x|| <= refine_tol ||F||.
-int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready) {
+int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready, bool f32_input) {
   // the first solve's scale comes from the assembly (fixup) or, for a caller's F, from a norm pass
   if (!scales_ready) RUN(h, "norm_f", 2, launch_norm_f(h->d_F, h->g, h->d_part, h->norm_parts, h->d_scal, h->stream));
-  int st = enqueue_solve32(h, &h->tm_F_in64, h->d_scal + SC_IN_SCALE, h->d_scal + SC_OUT_SCALE, 1, nullptr, "", x);
+  // f32_input: the fixup wrote F * 2^-e as float into d_g32, and each residual
+  // is written there with the same scale, so every x sweep reads FP32
+  const double* in_s = h->d_scal + SC_IN_SCALE;
+  const double* out_s = h->d_scal + SC_OUT_SCALE;
+  int st = f32_input ? enqueue_solve32(h, h->d_g32, 1, nullptr, out_s, 1, nullptr, "", x)
+                     : enqueue_solve32(h, h->d_F, 0, in_s, out_s, 1, nullptr, "", x);
   if (st) return st;
   const int* conv = h->d_flags + FL_CONV;
-  for (int k = 0; k < h->opts.max_refine; ++k) {
+  auto residual = [&](bool want_ff) -> int {
     ResidualArgs ra = residual_args(h, x, h->d_F, h->d_r);
     ra.skip_flag = conv;
-    ra.want_ff = (k == 0);
+    ra.want_ff = want_ff;
+    if (f32_input) { ra.r32 = h->d_g32; ra.r32_scale = in_s; }
     RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
+    return ADS_OK;
+  };
+  for (int k = 0; k < h->opts.max_refine; ++k) {
+    if ((st = residual(k == 0))) return st;
     RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, true, k == 0, h->d_scal, h->d_flags, h->stream));
-    st = enqueue_solve32(h, &h->tm_r_in64, h->d_scal + SC_C_IN, h->d_scal + SC_C_OUT, 2, conv, "_corr", x);
+    st = f32_input ? enqueue_solve32(h, h->d_g32, 1, nullptr, out_s, 2, conv, "_corr", x)
+                   : enqueue_solve32(h, h->d_r, 0, h->d_scal + SC_C_IN, h->d_scal + SC_C_OUT, 2, conv, "_corr", x);
     if (st) return st;
   }
-  ResidualArgs ra = residual_args(h, x, h->d_F, h->d_r);
-  ra.skip_flag = conv;
-  ra.want_ff = (h->opts.max_refine == 0);
-  RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
+  if ((st = residual(h->opts.max_refine == 0))) return st;
   RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, false, h->opts.max_refine == 0,
                                     h->d_scal, h->d_flags, h->stream));
   return ADS_OK;
 }
 
 int enqueue_solve(ads_handle* h) {
-  if (h->opts.precision == ADS_PREC_MIXED) return enqueue_solve_mixed(h, h->d_u, false);
-  return enqueue_solve64(h, &h->tm_F_in64, &h->tm_u_out64, false);
+  if (h->opts.precision == ADS_PREC_MIXED) return enqueue_solve_mixed(h, h->d_u, false, false);
+  return enqueue_solve64(h, h->d_F, &h->tm_u_out64, false);
 }
 
 // one Step (src/ADS.F90:437-461): FormUn+Form3DRHS, three sweeps, R := F.
@@ -412,14 +426,14 @@ int enqueue_step(ads_handle* h) {
   int st;
   if (h->opts.precision == ADS_PREC_MIXED && h->form == ADS_FORM_HEAT) {
     if ((st = enqueue_assemble(h, h->d_u, h->d_F, true, true, true))) return st;
-    if ((st = enqueue_solve_mixed(h, h->d_delta, true))) return st;
-    RUN(h, "update", 1, launch_axpby(h->d_u, h->d_delta, 1.0, 1.0, (long long)h->n0, h->stream));
+    if ((st = enqueue_solve_mixed(h, h->d_delta, true, true))) return st;
+    RUN(h, "update", 1, launch_add(h->d_u, h->d_delta, (long long)h->n0, h->stream));
   } else if (h->opts.precision == ADS_PREC_MIXED) {
     if ((st = enqueue_assemble(h, h->d_u, h->d_F, false, false, true))) return st;
-    if ((st = enqueue_solve_mixed(h, h->d_u, true))) return st;
+    if ((st = enqueue_solve_mixed(h, h->d_u, true, false))) return st;
   } else {
     if ((st = enqueue_assemble(h, h->d_u, h->d_F, false, false, true))) return st;
-    if ((st = enqueue_solve64(h, &h->tm_F_in64, &h->tm_u_out64, false))) return st;
+    if ((st = enqueue_solve64(h, h->d_F, &h->tm_u_out64, false))) return st;
   }
   RUN(h, "record", 1, launch_record(h->d_scal, h->d_flags, h->d_hist, h->hist_cap, h->stream));
   return ADS_OK;
@@ -513,7 +527,7 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_dd64[d]); cudaFree(h->d_dd32[d]);
     cudaFree(h->d_fac64[d]); cudaFree(h->d_tfac64[d]); cudaFree(h->d_fac32[d]); cudaFree(h->d_band[d]);
   }
-  cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_wA); cudaFree(h->d_wB);
+  cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_g32); cudaFree(h->d_wA); cudaFree(h->d_wB);
   cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_l2part);
   cudaFree(h->d_part); cudaFree(h->d_scal); cudaFree(h->d_flags); cudaFree(h->d_hist);
   if (h->ev0) cudaEventDestroy(h->ev0);
@@ -540,7 +554,7 @@ int create_impl(ads_handle* h) {
   g.Q = h->Q;
   for (int d = 0; d < 3; ++d) { g.E[d] = h->ax[d].E; g.N[d] = h->ax[d].N; }
   for (int d = 0; d < 3; ++d)
-    if (g.N[d] > 448) return fail(h, ADS_ERR_UNSUPPORTED, "the GPU sweeps support at most 448 DOFs per axis");
+    if (g.N[d] > ADS_MAX_AXIS_DOFS) return fail(h, ADS_ERR_UNSUPPORTED, "the GPU sweeps support at most 448 DOFs per axis");
   g.PX = round_up(g.N[0], 8);
   g.PY = round_up(g.N[1], 8);
   g.PZ = round_up(g.N[2], 8);
@@ -578,6 +592,11 @@ int create_impl(ads_handle* h) {
   if ((st = zalloc(&h->d_F, h->n0))) return st;
   if ((st = zalloc(&h->d_r, h->n0))) return st;
   if (h->opts.precision == ADS_PREC_MIXED && (st = zalloc(&h->d_delta, h->n0))) return st;
+  if (h->opts.precision == ADS_PREC_MIXED) {
+    double* g32 = nullptr;
+    if ((st = zalloc(&g32, (h->n0 + 1) / 2))) return st;
+    h->d_g32 = reinterpret_cast<float*>(g32);
+  }
   if ((st = zalloc(&h->d_wA, h->n1))) return st;
   if ((st = zalloc(&h->d_wB, h->n2))) return st;
   if ((st = zalloc(&h->d_shadow, 7 * h->n0))) return st;
@@ -617,18 +636,12 @@ int create_impl(ads_handle* h) {
   if ((st = ensure_hist(h, 64))) return st;
 
   bool ok = true;
-  ok &= make_l0_in(h, &h->tm_F_in64, h->d_F, false);
-  ok &= make_l0_in(h, &h->tm_r_in64, h->d_r, false);
   ok &= make_l0_out(h, &h->tm_u_out64, h->d_u, false);
   ok &= make_l0_out(h, &h->tm_r_out64, h->d_r, false);
   ok &= make_l1_out(h, &h->tm_wA_out64, h->d_wA, false);
-  ok &= make_l1_in(h, &h->tm_wA_in64, h->d_wA, false);
   ok &= make_l2_out(h, &h->tm_wB_out64, h->d_wB, false);
-  ok &= make_l2_in(h, &h->tm_wB_in64, h->d_wB, false);
   ok &= make_l1_out(h, &h->tm_wA_out32, h->d_wA, true);
-  ok &= make_l1_in(h, &h->tm_wA_in32, h->d_wA, true);
   ok &= make_l2_out(h, &h->tm_wB_out32, h->d_wB, true);
-  ok &= make_l2_in(h, &h->tm_wB_in32, h->d_wB, true);
   if (!ok) return fail(h, ADS_ERR_CUDA, "cuTensorMapEncodeTiled rejected a layout");
   return ADS_OK;
 }
@@ -887,26 +900,27 @@ int ads_reorder(ads_handle* h, int kind, const double* in, double* out) {
   ADS_CUDA(h, cudaSetDevice(h->dev));
   const Geometry& g = h->g;
   const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
-  const CUtensorMap *tin, *tout;
+  const CUtensorMap* tout;
+  const double* src;
   double* dst;
   int axis;
   if (kind == ADS_REORDER_FOR_Y) {  // L0 -> L1
     ADS_CUDA(h, cudaMemcpy2DAsync(h->d_F, g.PX * 8, in, (size_t)Nx * 8, (size_t)Nx * 8, (size_t)Ny * Nz,
                                   cudaMemcpyHostToDevice, h->stream));
-    tin = &h->tm_F_in64; tout = &h->tm_wA_out64; dst = h->d_wA; axis = 0;
+    src = h->d_F; tout = &h->tm_wA_out64; dst = h->d_wA; axis = 0;
   } else if (kind == ADS_REORDER_FOR_Z) {  // L1 -> L2
     ADS_CUDA(h, cudaMemcpy2DAsync(h->d_wA, g.PY * 8, in, (size_t)Ny * 8, (size_t)Ny * 8, (size_t)Nx * Nz,
                                   cudaMemcpyHostToDevice, h->stream));
-    tin = &h->tm_wA_in64; tout = &h->tm_wB_out64; dst = h->d_wB; axis = 1;
+    src = h->d_wA; tout = &h->tm_wB_out64; dst = h->d_wB; axis = 1;
   } else if (kind == ADS_REORDER_FOR_X) {  // L2 -> L0
     ADS_CUDA(h, cudaMemcpy2DAsync(h->d_wB, g.PZ * 8, in, (size_t)Nz * 8, (size_t)Nz * 8, (size_t)Nx * Ny,
                                   cudaMemcpyHostToDevice, h->stream));
-    tin = &h->tm_wB_in64; tout = &h->tm_r_out64; dst = h->d_r; axis = 2;
+    src = h->d_wB; tout = &h->tm_r_out64; dst = h->d_r; axis = 2;
   } else {
     return fail(h, ADS_ERR_ARG, "unknown reorder kind");
   }
-  SweepArgs a = sweep_args(h, axis, h->d_fac64[axis]);
-  RUN(h, "transpose_f64", 1, launch_sweep(h->P, 0, 0, 3, false, tin, tout, a, sweep_grid(h, axis), h->stream));
+  SweepArgs a = sweep_args(h, axis, h->d_fac64[axis], src);
+  RUN(h, "transpose_f64", 1, launch_sweep(h->P, 0, 0, 3, false, tout, a, sweep_grid(h, axis), h->stream));
   if (kind == ADS_REORDER_FOR_Y) {
     ADS_CUDA(h, cudaMemcpy2DAsync(out, (size_t)Ny * 8, dst, g.PY * 8, (size_t)Ny * 8, (size_t)Nx * Nz,
                                   cudaMemcpyDeviceToHost, h->stream));
@@ -949,8 +963,8 @@ int ads_heat_adjoint(ads_handle* h, int K, int ck, const double* u0, const doubl
     cleanup();
     return fail(h, ADS_ERR_ALLOC, "adjoint buffers");
   }
-  CUtensorMap tm_lam_in, tm_mu_out;
-  if (!make_l0_in(h, &tm_lam_in, lam, false) || !make_l0_out(h, &tm_mu_out, mu, false)) {
+  CUtensorMap tm_mu_out;
+  if (!make_l0_out(h, &tm_mu_out, mu, false)) {
     cleanup();
     return fail(h, ADS_ERR_CUDA, "adjoint tensor maps");
   }
@@ -992,7 +1006,7 @@ int ads_heat_adjoint(ads_handle* h, int K, int ck, const double* u0, const doubl
       }
       for (int n = s1 - 1; n >= s0; --n) {
         // mu = M^{-T} lambda (transposed sweeps, FP64)
-        if ((s = enqueue_solve64(h, &tm_lam_in, &tm_mu_out, true))) return s;
+        if ((s = enqueue_solve64(h, lam, &tm_mu_out, true))) return s;
         if (gk) RUN(h, "kappa_grad", 1, launch_kappa_grad(h->g, seg + (size_t)(n - s0) * n0, mu, h->dt, gk, t64[0], t64[1], t64[2], h->stream));
         // lambda = A^T mu: the heat operator is symmetric, so the same assembly
         // kernels apply it (the source term does not depend on u and is left out)

@@ -23,9 +23,11 @@ constexpr int AS_TY = 8;
 constexpr int AS_THREADS = 256;
 __host__ __device__ constexpr int as_tx(int p) { return 32 - p; }
 
-// Banded sweeps: one warp solves SW_LANES lines; lines are staged through
-// shared memory in chunks of SW_CH positions (TMA boxes).
+// Banded sweeps: one warp solves SW_LANES lines staged in shared memory; the
+// transposed output leaves in chunks of SW_CH positions (TMA store boxes).
 constexpr int SW_LANES = 32;
+// largest DOF count per axis the GPU kernels take (sweep shared memory, fixup tables)
+constexpr int ADS_MAX_AXIS_DOFS = 448;
 constexpr int SW_CH = 32;
 
 // Residual (Kronecker mat-vec) tile in x/y, streamed along z.
@@ -95,11 +97,14 @@ struct FixupArgs {
   const double* l2part;  // [nl2] l2 partials, then [nl2] max |value| partials
   int nl2;
   double* scal;          // device scalars (SC_*)
+  float* g32;            // if set: every entry of the final F also as float(F * SC_IN_SCALE)
 };
 
 struct SweepArgs {
   int L;            // line length
-  int nchunk;       // ceil(L / SW_CH)
+  const void* in;   // input array (TIn): position p of line l of the tile at (l, t3) is
+                    // in[t3 * in_t3s + l * in_ls + p]; lines padded to a multiple of 8 entries
+  long long in_ls, in_t3s;
   int lanes_total;  // extent of the lane dimension
   int tiles_lane;   // ceil(lanes_total / SW_LANES)
   int lane_dim;     // 1 or 2: which input tensor dimension carries the lanes
@@ -124,6 +129,8 @@ struct ResidualArgs {
   const double* u;    // L0
   const double* F;    // L0 (may be null: plain mat-vec)
   double* r;          // L0 output: F - M u (or M u)
+  float* r32;         // if set, r is written here as float(r * *r32_scale) instead
+  const double* r32_scale;
   const double* band[3];  // per axis, (2P+1) x N: band[(m+P)*N + i] = M_{i,i+m}
   double* part;       // per CTA: [rr, ff, rmax]
   const int* skip_flag;
@@ -146,8 +153,9 @@ cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s);
 // mode: 0 = TMA store to the next layout, 1 = final store to L0 (u = s*x),
 //       2 = final accumulate into L0 (u += s*x), 3 = identity transpose (no solve)
 // tin: 0 = double input, 1 = float input; tc: 0 = double compute, 1 = float compute
-cudaError_t launch_sweep(int P, int tin, int tc, int mode, bool trans, const CUtensorMap* tmin,
-                         const CUtensorMap* tmout, const SweepArgs& a, int grid, cudaStream_t s);
+// The input is read through a.in (set with sweep_input in the host code).
+cudaError_t launch_sweep(int P, int tin, int tc, int mode, bool trans, const CUtensorMap* tmout,
+                         const SweepArgs& a, int grid, cudaStream_t s);
 
 // device scalar slots (double) and flag slots (int) of a handle
 enum ScalarSlot {
@@ -191,6 +199,8 @@ cudaError_t launch_record(const double* scal, int* flags, double* hist, int cap,
 cudaError_t launch_qp_to_grid(const double* src, double* dst, const Geometry& g, cudaStream_t s);
 cudaError_t launch_grid_to_qp(const double* src, double* dst, const Geometry& g, cudaStream_t s);
 // y = alpha*x + beta*y over n entries
+// y += x
+cudaError_t launch_add(double* y, const double* x, long long n, cudaStream_t s);
 cudaError_t launch_axpby(double* y, const double* x, double alpha, double beta, long long n,
                          cudaStream_t s);
 // out = sum x*y over n entries (deterministic two-stage)
@@ -222,34 +232,45 @@ int handle_cuda_fail(ads_handle* h, cudaError_t e, const char* where);
 
 // ---------------------------------------------------------------------------
 // FP64 <-> FP32 conversions with integer operations only (GB300 runs FP64 at
-// 1/64 of FP32, conversions included): power-of-two scale 2^sexp folded into
-// the exponent; results below the float range flush to zero.
+// 1/64 of the FP32 rate, conversions included), with a power-of-two scale
+// 2^sexp folded into the exponent.  Every case is integer work, so no FP64
+// instruction is ever issued for them: values below the target's normal range
+// flush to signed zero, overflow gives infinity, inf and NaN map to inf and
+// (quiet) NaN.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float d2f_scaled(double d, int sexp) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(d);
   const unsigned sign = (unsigned)(b >> 63) << 31;
   const int ed = (int)((b >> 52) & 0x7ffull);
+  const unsigned long long m = b & 0xfffffffffffffull;
+  if (ed == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m != 0ull ? 0x400000u : 0u));
   const int ef = ed + sexp - 896;  // biased float exponent after scaling (1023 - 127)
   if (ed == 0 || ef < 1) return __uint_as_float(sign);
-  if (ed == 0x7ff || ef > 254) return (float)(d * ldexp(1.0, sexp));  // inf/nan/overflow
-  const unsigned long long m = b & 0xfffffffffffffull;
+  if (ef > 254) return __uint_as_float(sign | 0x7f800000u);
   const unsigned m23 = (unsigned)(m >> 29);
   const unsigned rem = (unsigned)(m & 0x1fffffffull);
   unsigned r = sign | ((unsigned)ef << 23) | m23;
-  if (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) r += 1u;  // carry rounds into the exponent
+  if (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) r += 1u;  // a carry rounds into the exponent
   return __uint_as_float(r);
 }
 
 // float -> double (exact) times 2^sexp
 __device__ __forceinline__ double f2d_scaled(float f, int sexp) {
   const unsigned b = __float_as_uint(f);
-  const int e = (int)((b >> 23) & 0xffu);
+  const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
+  int e = (int)((b >> 23) & 0xffu);
+  unsigned m23 = b & 0x7fffffu;
+  if (e == 0xff) return __longlong_as_double((long long)(sign | (0x7ffull << 52) | ((unsigned long long)m23 << 29)));
+  if (e == 0) {
+    if (m23 == 0u) return __longlong_as_double((long long)sign);
+    const int sh = __clz(m23) - 8;  // float subnormal: normalise
+    m23 = (m23 << sh) & 0x7fffffu;
+    e = 1 - sh;
+  }
   const int ed = e + 896 + sexp;
-  if ((b & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)(b >> 31) << 63));
-  if (e == 0 || e == 0xff || ed < 1 || ed > 2046) return (double)f * ldexp(1.0, sexp);
-  const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) | ((unsigned long long)ed << 52) |
-                                  ((unsigned long long)(b & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)bits);
+  if (ed < 1) return __longlong_as_double((long long)sign);
+  if (ed > 2046) return __longlong_as_double((long long)(sign | (0x7ffull << 52)));
+  return __longlong_as_double((long long)(sign | ((unsigned long long)ed << 52) | ((unsigned long long)m23 << 29)));
 }
 
 // d * 2^sexp = hi + lo with hi the nearest float and lo the float nearest to
@@ -258,11 +279,12 @@ __device__ __forceinline__ void split_scaled(double d, int sexp, float& hi, floa
   const unsigned long long b = (unsigned long long)__double_as_longlong(d);
   const unsigned sign = (unsigned)(b >> 63) << 31;
   const int ed = (int)((b >> 52) & 0x7ffull);
-  const int ef = ed + sexp - 896;
-  lo = 0.f;
-  if (ed == 0 || ef < 1) { hi = __uint_as_float(sign); return; }
-  if (ed == 0x7ff || ef > 254) { hi = (float)(d * ldexp(1.0, sexp)); return; }
   const unsigned long long m = b & 0xfffffffffffffull;
+  lo = 0.f;
+  if (ed == 0x7ff) { hi = __uint_as_float(sign | 0x7f800000u | (m != 0ull ? 0x400000u : 0u)); return; }
+  const int ef = ed + sexp - 896;
+  if (ed == 0 || ef < 1) { hi = __uint_as_float(sign); return; }
+  if (ef > 254) { hi = __uint_as_float(sign | 0x7f800000u); return; }
   const unsigned m23 = (unsigned)(m >> 29);
   const unsigned rem = (unsigned)(m & 0x1fffffffull);
   const bool up = rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u));
@@ -279,6 +301,6 @@ __device__ __forceinline__ void split_scaled(double d, int sexp, float& hi, floa
 __device__ __forceinline__ int pow2_exp(double s) {
   return (int)(((unsigned long long)__double_as_longlong(s) >> 52) & 0x7ffull) - 1023;
 }
-size_t sweep_smem_bytes(int tin, int tc, int P, int L, int nchunk);
+size_t sweep_smem_bytes(int tin, int tc, int P, int L);
 
 }  // namespace ads

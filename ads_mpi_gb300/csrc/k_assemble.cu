@@ -596,7 +596,9 @@ __global__ void k_fixup(const FixupArgs a) {
   const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
   const int P = g.P;
   const int lane = threadIdx.x & 31;
-  if (blockIdx.x == 0 && threadIdx.x < 32) {
+  __shared__ int s_exp;
+  // with g32 every block needs the scale, so every block reduces the partials
+  if ((blockIdx.x == 0 || a.g32 != nullptr) && threadIdx.x < 32) {
     double t = 0.0;
     unsigned long long m = 0ull;
     for (int i = lane; i < a.nl2; i += 32) {
@@ -611,22 +613,65 @@ __global__ void k_fixup(const FixupArgs a) {
       m = ob > m ? ob : m;
     }
     if (lane == 0) {
-      a.scal[SC_L2] = t;
       const double fm = __longlong_as_double((long long)m);
-      a.scal[SC_FMAX] = fm;
       int e = 0;
       if (fm > 0.0 && fm <= 1.7976931348623157e308) (void)frexp(fm, &e);
-      a.scal[SC_OUT_SCALE] = ldexp(1.0, e);
-      a.scal[SC_IN_SCALE] = ldexp(1.0, -e);
+      s_exp = e;
+      if (blockIdx.x == 0) {
+        a.scal[SC_L2] = t;
+        a.scal[SC_FMAX] = fm;
+        a.scal[SC_OUT_SCALE] = ldexp(1.0, e);
+        a.scal[SC_IN_SCALE] = ldexp(1.0, -e);
+      }
     }
   }
-  const long long rows = (long long)Ny * Nz;
+  if (a.g32 != nullptr) {
+    // full pass: F += spill slabs where they apply, and every entry of the
+    // final F as float(F * 2^-e), the FP32 solve's scaled input.  One thread
+    // per 4 consecutive x of a row (32-byte aligned: pitches are multiples
+    // of 8); x-slab membership comes from a per-block table.
+    __shared__ unsigned char xzone[ADS_MAX_AXIS_DOFS + 8];
+    const int TX = as_tx(P);
+    for (int x = threadIdx.x; x < (int)g.PX; x += blockDim.x) xzone[x] = (x < Nx && in_slab(x, TX, P, a.nix)) ? 1 : 0;
+    __syncthreads();
+    const int sexp = -s_exp;
+    // 32-bit index arithmetic throughout: 64-bit division runs on the FP64
+    // pipe (at most 448 x 448 rows of 112 quads)
+    const int nq = (int)(g.PX / 4);
+    const int items = Ny * Nz * nq;
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < items; it += gridDim.x * blockDim.x) {
+      const int row = it / nq;
+      const int x0 = (it - row * nq) * 4;
+      const int z = row / Ny, y = row - z * Ny;
+      const size_t o = (size_t)g.PX * (size_t)row + (size_t)x0;
+      const double2 v01 = *reinterpret_cast<const double2*>(a.F + o);
+      const double2 v23 = *reinterpret_cast<const double2*>(a.F + o + 2);
+      double v[4] = {v01.x, v01.y, v23.x, v23.y};
+      const int zyz = (in_slab(y, AS_TY, P, a.niy) ? 2 : 0) | (in_slab(z, a.zc, P, a.niz) ? 4 : 0);
+      const bool anyx = (xzone[x0] | xzone[x0 + 1] | xzone[x0 + 2] | xzone[x0 + 3]) != 0;
+      if ((zyz != 0 || anyx) && x0 < Nx) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int zone = zyz | xzone[x0 + k];
+          if (zone != 0 && x0 + k < Nx) {
+            for (int cls = 1; cls < 8; ++cls)
+              if ((cls & zone) == cls) v[k] += a.shadow[(size_t)(cls - 1) * a.shadow_stride + o + k];
+          }
+        }
+        *reinterpret_cast<double2*>(a.F + o) = make_double2(v[0], v[1]);
+        *reinterpret_cast<double2*>(a.F + o + 2) = make_double2(v[2], v[3]);
+      }
+      *reinterpret_cast<float4*>(a.g32 + o) =
+          make_float4(d2f_scaled(v[0], sexp), d2f_scaled(v[1], sexp), d2f_scaled(v[2], sexp), d2f_scaled(v[3], sexp));
+    }
+    return;
+  }
+  const int rows = Ny * Nz;
   const int wpb = blockDim.x / 32;
   const int TX = as_tx(P);
   const int nxz = a.nix - 1;  // x slabs start at x = k*TX, k = 1..nix-1
-  for (long long row = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); row < rows;
-       row += (long long)gridDim.x * wpb) {
-    const int y = (int)(row % Ny), z = (int)(row / Ny);
+  for (int row = blockIdx.x * wpb + (threadIdx.x >> 5); row < rows; row += gridDim.x * wpb) {
+    const int z = row / Ny, y = row - z * Ny;
     const bool zy = in_slab(y, AS_TY, P, a.niy);
     const bool zz = in_slab(z, a.zc, P, a.niz);
     const size_t rb = (size_t)g.PX * ((size_t)y + (size_t)Ny * z);

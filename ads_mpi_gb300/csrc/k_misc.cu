@@ -47,6 +47,8 @@ __global__ void __launch_bounds__(RS_THREADS) k_residual(const ResidualArgs a) {
   double rr = 0.0, ff = 0.0;
   unsigned long long rmax_bits = 0ull;  // max |r| as the bits of a non-negative double
   const bool want_ff = a.want_ff != 0;
+  const bool r32e_on = a.r32 != nullptr;
+  const int r32e = r32e_on ? pow2_exp(*a.r32_scale) : 0;
 
   for (int zin = z0 - P; zin < z1 + P; ++zin) {
     if (zin >= 0 && zin < Nz) {
@@ -98,7 +100,8 @@ __global__ void __launch_bounds__(RS_THREADS) k_residual(const ResidualArgs a) {
         } else {
           r = mu;
         }
-        a.r[o] = r;
+        if (r32e_on) a.r32[o] = d2f_scaled(r, r32e);
+        else a.r[o] = r;
         rr += r * r;
         const unsigned long long rb = (unsigned long long)__double_as_longlong(r) & 0x7fffffffffffffffull;
         rmax_bits = rb > rmax_bits ? rb : rmax_bits;
@@ -361,6 +364,22 @@ __global__ void k_axpby(double* y, const double* x, double alpha, double beta, l
 cudaError_t launch_axpby(double* y, const double* x, double alpha, double beta, long long n,
                          cudaStream_t s) {
   k_axpby<<<blocks_for(n), 256, 0, s>>>(y, x, alpha, beta, n);
+  return cudaGetLastError();
+}
+
+// y += x (n a multiple of 2)
+__global__ void k_add(double* y, const double* x, int n2) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n2; q += gridDim.x * blockDim.x) {
+    const double2 a = reinterpret_cast<const double2*>(x)[q];
+    double2 b = reinterpret_cast<double2*>(y)[q];
+    b.x += a.x;
+    b.y += a.y;
+    reinterpret_cast<double2*>(y)[q] = b;
+  }
+}
+cudaError_t launch_add(double* y, const double* x, long long n, cudaStream_t s) {
+  const int n2 = (int)(n / 2);
+  k_add<<<blocks_for(n2), 256, 0, s>>>(y, x, n2);
   return cudaGetLastError();
 }
 

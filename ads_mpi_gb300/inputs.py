@@ -35,11 +35,8 @@ def gaussian_bumps(x, y, z, seed=0, n=16, width=0.05):
     return np.ascontiguousarray(f, dtype=np.float64)
 
 
-def gaussian_random_field(x, y, z, seed=0, sigma=0.5, corr=0.1, grid=64):
-    """Stationary Gaussian random field with squared-exponential covariance
-    sigma^2 exp(-|r|^2 / (2 corr^2)) on the periodic unit cube: white noise is
-    filtered in Fourier space on a uniform `grid`^3 mesh, normalised to variance
-    sigma^2, and evaluated at (x, y, z) by trilinear interpolation."""
+def _grf_grid(seed, sigma, corr, grid):
+    """The field of gaussian_random_field on its grid^3 mesh (cell vertices i/grid)."""
     rng = np.random.default_rng(seed)
     noise = rng.standard_normal((grid, grid, grid))
     k = np.fft.fftfreq(grid, d=1.0 / grid) * 2 * np.pi
@@ -48,7 +45,52 @@ def gaussian_random_field(x, y, z, seed=0, sigma=0.5, corr=0.1, grid=64):
     amp = np.exp(-0.25 * corr * corr * (kx * kx + ky * ky + kz * kz))
     g = np.real(np.fft.ifftn(np.fft.fftn(noise) * amp))
     g = g - g.mean()
-    g = g * (sigma / g.std())
+    return g * (sigma / g.std())
+
+
+def _trilinear_weights(X, grid):
+    """Dense (points, grid) matrix of the periodic linear interpolation weights."""
+    x = np.asarray(X, dtype=np.float64).reshape(-1) * grid
+    i0 = np.floor(x).astype(np.int64)
+    f = x - i0
+    W = np.zeros((x.size, grid))
+    r = np.arange(x.size)
+    np.add.at(W, (r, i0 % grid), 1.0 - f)
+    np.add.at(W, (r, (i0 + 1) % grid), f)
+    return W
+
+
+def gaussian_random_field_qp(Xx, Xy, Xz, seed=0, sigma=0.5, corr=0.1, grid=64, device=None):
+    """gaussian_random_field on the tensor grid of quadrature points: the same
+    field and trilinear interpolation, applied axis by axis (the weights are
+    separable).  Xx, Xy, Xz are the per-axis point tables (E, q); the result has
+    the per-point layout shape (Ez, Ey, Ex, q, q, q).  Uses torch on `device`
+    when given."""
+    g = _grf_grid(seed, sigma, corr, grid)
+    Wx, Wy, Wz = (_trilinear_weights(X, grid) for X in (Xx, Xy, Xz))
+    Ex, q = np.asarray(Xx).shape
+    Ey, Ez = np.asarray(Xy).shape[0], np.asarray(Xz).shape[0]
+    if device is not None:
+        import torch
+        tg = torch.as_tensor(g, device=device)
+        wx, wy, wz = (torch.as_tensor(W, device=device) for W in (Wx, Wy, Wz))
+        t = torch.einsum("ai,ijk->ajk", wx, tg)
+        t = torch.einsum("bj,ajk->abk", wy, t)
+        t = torch.einsum("ck,abk->cba", wz, t)          # (QZ, QY, QX)
+        t = t.reshape(Ez, q, Ey, q, Ex, q).permute(0, 2, 4, 1, 3, 5).contiguous()
+        return t.cpu().numpy()
+    t = np.einsum("ai,ijk->ajk", Wx, g)
+    t = np.einsum("bj,ajk->abk", Wy, t)
+    t = np.einsum("ck,abk->cba", Wz, t)
+    return np.ascontiguousarray(t.reshape(Ez, q, Ey, q, Ex, q).transpose(0, 2, 4, 1, 3, 5))
+
+
+def gaussian_random_field(x, y, z, seed=0, sigma=0.5, corr=0.1, grid=64):
+    """Stationary Gaussian random field with squared-exponential covariance
+    sigma^2 exp(-|r|^2 / (2 corr^2)) on the periodic unit cube: white noise is
+    filtered in Fourier space on a uniform `grid`^3 mesh, normalised to variance
+    sigma^2, and evaluated at (x, y, z) by trilinear interpolation."""
+    g = _grf_grid(seed, sigma, corr, grid)
     # trilinear interpolation on the periodic grid (cell-vertex at i/grid)
     X = np.asarray(x) * grid
     Y = np.asarray(y) * grid

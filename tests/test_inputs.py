@@ -47,3 +47,19 @@ def test_separable_bumps_match_direct():
     b = inputs.gaussian_bumps_separable(Xx, Xy, Xz, seed=5)
     assert a.shape == b.shape
     assert np.abs(a - b).max() < 1e-13
+
+
+def test_random_field_on_qp_grid_matches_pointwise():
+    """The separable quadrature-grid evaluation of the Gaussian random field
+    equals the pointwise trilinear evaluation at the same points."""
+    from ads_mpi_gb300 import inputs
+    rng = np.random.default_rng(3)
+    q = 3
+    Xx, Xy, Xz = (np.sort(rng.uniform(0, 1, (e, q)), axis=None).reshape(e, q) for e in (4, 3, 5))
+    a = inputs.gaussian_random_field_qp(Xx, Xy, Xz, seed=1, grid=16)
+    x = Xx[None, None, :, None, None, :]
+    y = Xy[None, :, None, None, :, None]
+    z = Xz[:, None, None, :, None, None]
+    b = inputs.gaussian_random_field(x, y, z, seed=1, grid=16)
+    assert a.shape == (5, 3, 4, q, q, q)
+    assert np.allclose(a, b, rtol=1e-12, atol=1e-12)
