@@ -85,6 +85,7 @@ struct ads_handle {
   double* d_fqp = nullptr;
   double* d_kqp = nullptr;
   double* d_l2part = nullptr;
+  unsigned char* d_slab = nullptr;  // spill-slab flags per DOF index (x, y, z)
   double* d_part = nullptr;
   double* d_scal = nullptr;
   int* d_flags = nullptr;
@@ -300,6 +301,7 @@ FixupArgs fixup_args(const ads_handle* h, double* F) {
   f.l2part = h->d_l2part;
   f.nl2 = h->asm_grid;
   f.scal = h->d_scal;
+  f.slab = h->d_slab;
   return f;
 }
 
@@ -337,7 +339,7 @@ int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool 
   FixupArgs f = fixup_args(h, F);
   f.nl2 = used;
   if (fp32 && incr) f.g32 = h->d_g32;  // the heat increment also feeds the FP32 solve as float
-  RUN(h, "fixup", 1, launch_fixup(f, h->stream));
+  RUN(h, "fixup", 2, launch_fixup(f, h->stream));
   return ADS_OK;
 }
 
@@ -528,7 +530,7 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_fac64[d]); cudaFree(h->d_tfac64[d]); cudaFree(h->d_fac32[d]); cudaFree(h->d_band[d]);
   }
   cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_g32); cudaFree(h->d_wA); cudaFree(h->d_wB);
-  cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_l2part);
+  cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_l2part); cudaFree(h->d_slab);
   cudaFree(h->d_part); cudaFree(h->d_scal); cudaFree(h->d_flags); cudaFree(h->d_hist);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -625,6 +627,17 @@ int create_impl(ads_handle* h) {
     h->res_zc = std::min(g.N[2], 32);
     h->res_niz = (g.N[2] + h->res_zc - 1) / h->res_zc;
     h->res_grid = h->res_nix * h->res_niy * h->res_niz;
+  }
+  {
+    // spill-slab membership of each DOF index (the assembly's bricks spill the
+    // first p DOFs of every brick after the first one into the shadows)
+    auto in_slab = [&](int v, int tile, int nitems) { return v >= tile && (v % tile) < h->P && (v / tile) <= nitems - 1; };
+    std::vector<unsigned char> sl((size_t)g.N[0] + g.N[1] + g.N[2], 0);
+    for (int x = 0; x < g.N[0]; ++x) sl[x] = in_slab(x, as_tx(h->P), h->asm_nix) ? 1 : 0;
+    for (int y = 0; y < g.N[1]; ++y) sl[g.N[0] + y] = in_slab(y, AS_TY, h->asm_niy) ? 1 : 0;
+    for (int z = 0; z < g.N[2]; ++z) sl[g.N[0] + g.N[1] + z] = in_slab(z, h->asm_zc, h->asm_niz) ? 1 : 0;
+    ADS_CUDA(h, cudaMalloc(&h->d_slab, sl.size()));
+    ADS_CUDA(h, cudaMemcpy(h->d_slab, sl.data(), sl.size(), cudaMemcpyHostToDevice));
   }
   h->norm_parts = 4 * nsm;
   h->npart = std::max(3 * h->res_grid, 2 * h->norm_parts);

@@ -98,6 +98,7 @@ struct FixupArgs {
   int nl2;
   double* scal;          // device scalars (SC_*)
   float* g32;            // if set: every entry of the final F also as float(F * SC_IN_SCALE)
+  const unsigned char* slab;  // 1 where a DOF index lies in a spill slab: x [Nx], then y [Ny], then z [Nz]
 };
 
 struct SweepArgs {

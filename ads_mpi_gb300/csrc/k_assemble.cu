@@ -582,112 +582,72 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
   }
 }
 
-// F += shadow contributions, in class order.  One warp per (y, z) row: the
-// whole row when y or z lies in a spill slab, else only the x slabs.  Block 0
-// also finishes the l2norm and the power-of-two scale of the FP32 solve
-// (from the largest value the assembly wrote, which is within a factor 8 of
-// max |F|: a DOF sums at most 8 written parts).
-__device__ __forceinline__ bool in_slab(int v, int tile, int P, int nitems) {
-  return v >= tile && (v % tile) < P && (v / tile) <= nitems - 1;
+// The assembly's partials: the l2norm, max |F| and the power-of-two scale of
+// the FP32 solve (from the largest value the assembly wrote, which is within a
+// factor 8 of max |F|: a DOF sums at most 8 written parts).
+__global__ void k_fixup_scale(const FixupArgs a) {
+  const int lane = threadIdx.x & 31;
+  double t = 0.0;
+  unsigned long long m = 0ull;
+  for (int i = lane; i < a.nl2; i += 32) {
+    t += a.l2part[i];
+    const unsigned long long b = (unsigned long long)__double_as_longlong(a.l2part[a.nl2 + i]);
+    m = b > m ? b : m;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    t += __shfl_down_sync(0xffffffffu, t, o);
+    const unsigned long long ob = __shfl_down_sync(0xffffffffu, m, o);
+    m = ob > m ? ob : m;
+  }
+  if (lane == 0) {
+    const double fm = __longlong_as_double((long long)m);
+    int e = 0;
+    if (fm > 0.0 && fm <= 1.7976931348623157e308) (void)frexp(fm, &e);
+    a.scal[SC_L2] = t;
+    a.scal[SC_FMAX] = fm;
+    a.scal[SC_OUT_SCALE] = ldexp(1.0, e);
+    a.scal[SC_IN_SCALE] = ldexp(1.0, -e);
+  }
 }
 
+// F += shadow contributions, in class order.  One CTA per (y, z) row, one
+// thread per 4 consecutive x (32-byte aligned: pitches are multiples of 8).
+// Slab membership comes from per-axis byte tables (no integer division in the
+// kernel).  With g32 set (the mixed heat step) every entry of the final F is
+// also written as float(F * 2^-e), the FP32 solve's scaled input; otherwise
+// only quads with a slab entry are read.
 __global__ void k_fixup(const FixupArgs a) {
   const Geometry& g = a.g;
-  const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
-  const int P = g.P;
-  const int lane = threadIdx.x & 31;
-  __shared__ int s_exp;
-  // with g32 every block needs the scale, so every block reduces the partials
-  if ((blockIdx.x == 0 || a.g32 != nullptr) && threadIdx.x < 32) {
-    double t = 0.0;
-    unsigned long long m = 0ull;
-    for (int i = lane; i < a.nl2; i += 32) {
-      t += a.l2part[i];
-      const unsigned long long b = (unsigned long long)__double_as_longlong(a.l2part[a.nl2 + i]);
-      m = b > m ? b : m;
-    }
+  const int Nx = g.N[0], Ny = g.N[1];
+  const int y = blockIdx.y, z = blockIdx.z;
+  const int x0 = 4 * threadIdx.x;
+  if (x0 >= (int)g.PX) return;
+  const int zyz = (a.slab[Nx + y] ? 2 : 0) | (a.slab[Nx + Ny + z] ? 4 : 0);
+  int zx[4];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      t += __shfl_down_sync(0xffffffffu, t, o);
-      const unsigned long long ob = __shfl_down_sync(0xffffffffu, m, o);
-      m = ob > m ? ob : m;
-    }
-    if (lane == 0) {
-      const double fm = __longlong_as_double((long long)m);
-      int e = 0;
-      if (fm > 0.0 && fm <= 1.7976931348623157e308) (void)frexp(fm, &e);
-      s_exp = e;
-      if (blockIdx.x == 0) {
-        a.scal[SC_L2] = t;
-        a.scal[SC_FMAX] = fm;
-        a.scal[SC_OUT_SCALE] = ldexp(1.0, e);
-        a.scal[SC_IN_SCALE] = ldexp(1.0, -e);
+  for (int k = 0; k < 4; ++k) zx[k] = (x0 + k < Nx) ? (zyz | a.slab[x0 + k]) : 0;
+  const bool any = (zx[0] | zx[1] | zx[2] | zx[3]) != 0;
+  if (a.g32 == nullptr && !any) return;
+  const size_t o = (size_t)g.PX * ((size_t)y + (size_t)Ny * z) + (size_t)x0;
+  const double2 v01 = *reinterpret_cast<const double2*>(a.F + o);
+  const double2 v23 = *reinterpret_cast<const double2*>(a.F + o + 2);
+  double v[4] = {v01.x, v01.y, v23.x, v23.y};
+  if (any) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (zx[k] != 0) {
+        for (int cls = 1; cls < 8; ++cls)
+          if ((cls & zx[k]) == cls) v[k] += a.shadow[(size_t)(cls - 1) * a.shadow_stride + o + k];
       }
     }
+    *reinterpret_cast<double2*>(a.F + o) = make_double2(v[0], v[1]);
+    *reinterpret_cast<double2*>(a.F + o + 2) = make_double2(v[2], v[3]);
   }
   if (a.g32 != nullptr) {
-    // full pass: F += spill slabs where they apply, and every entry of the
-    // final F as float(F * 2^-e), the FP32 solve's scaled input.  One thread
-    // per 4 consecutive x of a row (32-byte aligned: pitches are multiples
-    // of 8); x-slab membership comes from a per-block table.
-    __shared__ unsigned char xzone[ADS_MAX_AXIS_DOFS + 8];
-    const int TX = as_tx(P);
-    for (int x = threadIdx.x; x < (int)g.PX; x += blockDim.x) xzone[x] = (x < Nx && in_slab(x, TX, P, a.nix)) ? 1 : 0;
-    __syncthreads();
-    const int sexp = -s_exp;
-    // 32-bit index arithmetic throughout: 64-bit division runs on the FP64
-    // pipe (at most 448 x 448 rows of 112 quads)
-    const int nq = (int)(g.PX / 4);
-    const int items = Ny * Nz * nq;
-    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < items; it += gridDim.x * blockDim.x) {
-      const int row = it / nq;
-      const int x0 = (it - row * nq) * 4;
-      const int z = row / Ny, y = row - z * Ny;
-      const size_t o = (size_t)g.PX * (size_t)row + (size_t)x0;
-      const double2 v01 = *reinterpret_cast<const double2*>(a.F + o);
-      const double2 v23 = *reinterpret_cast<const double2*>(a.F + o + 2);
-      double v[4] = {v01.x, v01.y, v23.x, v23.y};
-      const int zyz = (in_slab(y, AS_TY, P, a.niy) ? 2 : 0) | (in_slab(z, a.zc, P, a.niz) ? 4 : 0);
-      const bool anyx = (xzone[x0] | xzone[x0 + 1] | xzone[x0 + 2] | xzone[x0 + 3]) != 0;
-      if ((zyz != 0 || anyx) && x0 < Nx) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int zone = zyz | xzone[x0 + k];
-          if (zone != 0 && x0 + k < Nx) {
-            for (int cls = 1; cls < 8; ++cls)
-              if ((cls & zone) == cls) v[k] += a.shadow[(size_t)(cls - 1) * a.shadow_stride + o + k];
-          }
-        }
-        *reinterpret_cast<double2*>(a.F + o) = make_double2(v[0], v[1]);
-        *reinterpret_cast<double2*>(a.F + o + 2) = make_double2(v[2], v[3]);
-      }
-      *reinterpret_cast<float4*>(a.g32 + o) =
-          make_float4(d2f_scaled(v[0], sexp), d2f_scaled(v[1], sexp), d2f_scaled(v[2], sexp), d2f_scaled(v[3], sexp));
-    }
-    return;
-  }
-  const int rows = Ny * Nz;
-  const int wpb = blockDim.x / 32;
-  const int TX = as_tx(P);
-  const int nxz = a.nix - 1;  // x slabs start at x = k*TX, k = 1..nix-1
-  for (int row = blockIdx.x * wpb + (threadIdx.x >> 5); row < rows; row += gridDim.x * wpb) {
-    const int z = row / Ny, y = row - z * Ny;
-    const bool zy = in_slab(y, AS_TY, P, a.niy);
-    const bool zz = in_slab(z, a.zc, P, a.niz);
-    const size_t rb = (size_t)g.PX * ((size_t)y + (size_t)Ny * z);
-    const int count = (zy || zz) ? Nx : nxz * P;
-    for (int t = lane; t < count; t += 32) {
-      const int x = (zy || zz) ? t : (t / P + 1) * TX + (t % P);
-      if (x >= Nx) continue;
-      const bool zx = in_slab(x, TX, P, a.nix);
-      const int zone = (zx ? 1 : 0) | (zy ? 2 : 0) | (zz ? 4 : 0);
-      if (zone == 0) continue;
-      const size_t o = rb + (size_t)x;
-      double v = a.F[o];
-      for (int cls = 1; cls < 8; ++cls)
-        if ((cls & zone) == cls) v += a.shadow[(size_t)(cls - 1) * a.shadow_stride + o];
-      a.F[o] = v;
-    }
+    const int sexp = pow2_exp(a.scal[SC_IN_SCALE]);
+    *reinterpret_cast<float4*>(a.g32 + o) =
+        make_float4(d2f_scaled(v[0], sexp), d2f_scaled(v[1], sexp), d2f_scaled(v[2], sexp), d2f_scaled(v[3], sexp));
   }
 }
 
@@ -766,11 +726,10 @@ size_t assemble_smem_bytes(int P, bool fp32) {
 }
 
 cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s) {
-  const long long rows = (long long)a.g.N[1] * a.g.N[2];
-  long long blocks = (rows + 7) / 8;
-  if (blocks > 152 * 8) blocks = 152 * 8;
-  if (blocks < 1) blocks = 1;
-  k_fixup<<<(int)blocks, 256, 0, s>>>(a);
+  k_fixup_scale<<<1, 32, 0, s>>>(a);
+  const int nq = (int)(a.g.PX / 4);
+  const dim3 grid(1, a.g.N[1], a.g.N[2]);
+  k_fixup<<<grid, (nq + 31) / 32 * 32, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -45,6 +45,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_residual(const ResidualArgs a) {
     for (int m = 0; m < W; ++m) mx[m] = (x < Nx) ? bx[(size_t)m * Nx + x] : 0.0;
   }
   double rr = 0.0, ff = 0.0;
+  float rr32 = 0.f, ff32 = 0.f;  // scaled by 2^(2 r32e) (FP32 output mode)
   unsigned long long rmax_bits = 0ull;  // max |r| as the bits of a non-negative double
   const bool want_ff = a.want_ff != 0;
   const bool r32e_on = a.r32 != nullptr;
@@ -96,17 +97,36 @@ __global__ void __launch_bounds__(RS_THREADS) k_residual(const ResidualArgs a) {
         if (a.F != nullptr) {
           const double f = a.F[o];
           r = f - mu;
-          if (want_ff) ff += f * f;
+          if (want_ff) {
+            if (r32e_on) {
+              const float fs = d2f_scaled(f, r32e);
+              ff32 = fmaf(fs, fs, ff32);
+            } else {
+              ff += f * f;
+            }
+          }
         } else {
           r = mu;
         }
-        if (r32e_on) a.r32[o] = d2f_scaled(r, r32e);
-        else a.r[o] = r;
-        rr += r * r;
+        if (r32e_on) {
+          // the FP32 solve's input; the norms only steer the refinement, so
+          // they are accumulated from it in FP32 (per thread) to spare the
+          // FP64 pipe
+          const float rs = d2f_scaled(r, r32e);
+          a.r32[o] = rs;
+          rr32 = fmaf(rs, rs, rr32);
+        } else {
+          a.r[o] = r;
+          rr += r * r;
+        }
         const unsigned long long rb = (unsigned long long)__double_as_longlong(r) & 0x7fffffffffffffffull;
         rmax_bits = rb > rmax_bits ? rb : rmax_bits;
       }
     }
+  }
+  if (r32e_on) {
+    rr = f2d_scaled(rr32, -2 * r32e);
+    ff = f2d_scaled(ff32, -2 * r32e);
   }
   // block reduction (fixed order)
   const int lane = tid & 31, warp = tid >> 5;

@@ -81,10 +81,12 @@ struct SweepSmem {
   __host__ __device__ static size_t total(int P, int L) { return 128 + s_bytes(L) + t_bytes() + f_bytes(P, L); }
 };
 
+// An input of the compute type is used as it is (launch_sweep rejects an
+// input scale for it); an FP64 input of an FP32 solve is scaled by 2^sexp.
 template <typename TC, typename TIn>
 __device__ __forceinline__ TC load_in(TIn v, int sexp, TC scale) {
   if constexpr (sizeof(TIn) == 8 && sizeof(TC) == 4) return d2f_scaled((double)v, sexp);
-  else return (TC)v * scale;
+  else return (TC)v;
 }
 // The forward pass keeps y in place of its input.  An FP32 y in an FP64 input
 // slot goes into the slot's first word as it is: a float <-> double
@@ -464,6 +466,7 @@ size_t sweep_smem_bytes(int tin, int tc, int P, int L) {
 cudaError_t launch_sweep(int P, int tin, int tc, int mode, bool trans, const CUtensorMap* tmout,
                          const SweepArgs& a, int grid, cudaStream_t s) {
   if (a.in == nullptr) return cudaErrorInvalidValue;
+  if (tin == tc && (a.in_scale != 1.0 || a.in_scale_dev != nullptr)) return cudaErrorInvalidValue;
   switch (P) {
     case 1: return launch_mode<1>(tin, tc, mode, trans, tmout, a, grid, s);
     case 2: return launch_mode<2>(tin, tc, mode, trans, tmout, a, grid, s);

@@ -21,6 +21,7 @@ runs N independent replicas, one per rank; value = all ranks' DOF-updates
 divided by the slowest rank's time.
 """
 import argparse
+import math
 import json
 import os
 import statistics
@@ -272,6 +273,17 @@ def run_only(args, local):
     print(json.dumps({"only": args.only, "elements": E, "degree": p, "kernels_ms": t}), flush=True)
 
 
+def finite_or_none(v):
+    """JSON-safe copy: non-finite floats become null."""
+    if isinstance(v, dict):
+        return {k: finite_or_none(x) for k, x in v.items()}
+    if isinstance(v, (list, tuple)):
+        return [finite_or_none(x) for x in v]
+    if isinstance(v, float) and not math.isfinite(v):
+        return None
+    return v
+
+
 def aux_runs(args, dev):
     """The other configurations of the workload family, measured after the
     headline step (rank 0 only): the FP64 adjoint at 96^3 (50 steps,
@@ -303,64 +315,85 @@ def aux_runs(args, dev):
         g.step()
         return g.coeffs()
 
-    # ---- adjoint, 96^3 p=2, FP64, 50 steps, checkpoint every 10 ----
-    E, p, K, ck = 96, 2, 50, 10
-    n = (E + p - 1,) * 3
-    g = A.ADS(n, (p, p, p), precision=A.PREC_FP64, device=dev)
-    u0 = bumps_state(g, args.seed)
-    ut_src = bumps_state(g, args.seed + 1)   # perturbed initial state
-    g.set_form(A.FORM_HEAT, kappa=1.0, dt=dtv)
-    g.set_coeffs(ut_src)
-    g.steps(K)
-    u_target = g.coeffs()
-    (loss, gu, _), t_adj = sync_time(lambda: g.heat_adjoint(K, ck, u0, u_target, grad=True))
-    rng = np.random.default_rng(args.seed + 7)
-    h = 1e-6
-    worst = 0.0
-    fd_rows = []
-    for _ in range(8):
-        d = rng.standard_normal(g.N)
-        d /= np.linalg.norm(d)
-        lp, _, _ = g.heat_adjoint(K, ck, u0 + h * d, u_target, grad=False)
-        lm, _, _ = g.heat_adjoint(K, ck, u0 - h * d, u_target, grad=False)
-        fd = (lp - lm) / (2 * h)
-        ad = float(np.dot(gu, d))
-        rel = abs(fd - ad) / max(abs(fd), abs(ad), 1e-300)
-        worst = max(worst, rel)
-        fd_rows.append(rel)
+    # The configured dt = 1e-5 is beyond the explicit stability limit at these
+    # sizes (dt * lambda_max = 5.97 at 96^3 and 10.6 at 128^3 with kappa = 1):
+    # the loss then grows by ~|1 - dt lambda_max|^(2K), a finite difference at
+    # h = 1e-6 is swamped by the FP64 rounding of the loss, and at 128^3 / 100
+    # steps the gradient overflows.  Each check therefore runs at the
+    # configured dt and at a stable dt: 1e-6 for the adjoint
+    # (dt * lambda_max = 0.60), and for the variable conductivity 1.5 /
+    # lambda_max rounded to one digit, lambda_max scaled by the largest kappa.
+    def adjoint_check(dtv):
+        E, p, K, ck = 96, 2, 50, 10
+        n = (E + p - 1,) * 3
+        g = A.ADS(n, (p, p, p), precision=A.PREC_FP64, device=dev)
+        u0 = bumps_state(g, args.seed)
+        ut_src = bumps_state(g, args.seed + 1)   # perturbed initial state
+        g.set_form(A.FORM_HEAT, kappa=1.0, dt=dtv)
+        g.set_coeffs(ut_src)
+        g.steps(K)
+        u_target = g.coeffs()
+        (loss, gu, _), t_adj = sync_time(lambda: g.heat_adjoint(K, ck, u0, u_target, grad=True))
+        rng = np.random.default_rng(args.seed + 7)
+        h = 1e-6
+        rows = []
+        for _ in range(8):
+            d = rng.standard_normal(g.N)   # entries N(0, 1), h = 1e-6 per entry
+            lp, _, _ = g.heat_adjoint(K, ck, u0 + h * d, u_target, grad=False)
+            lm, _, _ = g.heat_adjoint(K, ck, u0 - h * d, u_target, grad=False)
+            fd = (lp - lm) / (2 * h)
+            ad = float(np.dot(gu, d))
+            rows.append(abs(fd - ad) / max(abs(fd), abs(ad), 1e-300))
+        g.cleanup()
+        return {"dt": dtv, "loss": loss, "forward_backward_s": t_adj, "fd_rel_err_max": max(rows),
+                "fd_rel_err": rows}
+
     out["adjoint_96p2"] = {
-        "config": f"heat {E}^3 p={p} FP64, {K} steps dt={dtv}, checkpoint every {ck}; loss 1/2||u^K - u_target||_M^2",
-        "loss": loss, "forward_backward_s": t_adj, "fd_h": h, "fd_directions": 8,
-        "fd_rel_err_max": worst, "fd_rel_err": fd_rows, "target_fd_rel_err": 1e-6}
-    g.cleanup()
+        "config": "heat 96^3 p=2 FP64, 50 steps, checkpoint every 10; loss 1/2||u^50 - u_target||_M^2, "
+                  "u_target from a seeded forward run of a perturbed initial state; central FD h=1e-6 along "
+                  "8 seeded random directions with N(0,1) entries",
+        "configured_dt": adjoint_check(dtv), "stable_dt": adjoint_check(1e-6), "target_fd_rel_err": 1e-6}
 
     # ---- variable conductivity, 128^3 p=2, 100 steps: dL/dg, g -> kappa = exp(g) ----
-    E, p, K, ck = 128, 2, 100, 10
+    E, p = 128, 2
     n = (E + p - 1,) * 3
-    g64 = A.ADS(n, (p, p, p), precision=A.PREC_FP64, device=dev)
-    X = [g64.qp_points(a) for a in range(3)]
+    g0 = A.ADS(n, (p, p, p), precision=A.PREC_FP64, device=dev)
+    X = [g0.qp_points(a) for a in range(3)]
+    g0.cleanup()
     gq = inputs.gaussian_random_field_qp(X[0], X[1], X[2], seed=args.seed, sigma=0.5, corr=0.1,
                                          device=f"cuda:{dev}")
     kappa = np.exp(gq).ravel()
-    u0 = bumps_state(g64, args.seed)
-    g64.set_coeffs(bumps_state(g64, args.seed + 1))
-    g64.set_form(A.FORM_HEAT, kappa_qp=kappa, dt=dtv)
-    g64.steps(K)
-    u_target = g64.coeffs()
-    (l64, _, gk64), t64 = sync_time(lambda: g64.heat_adjoint(K, ck, u0, u_target, grad=False, grad_kappa=True))
-    gmx = A.ADS(n, (p, p, p), precision=A.PREC_MIXED, refine_tol=1e-10, max_refine=3, device=dev)
-    gmx.set_form(A.FORM_HEAT, kappa_qp=kappa, dt=dtv)
-    (lmx, _, gkmx), tmx = sync_time(lambda: gmx.heat_adjoint(K, ck, u0, u_target, grad=False, grad_kappa=True))
-    dg64 = gk64 * kappa    # dL/dg = dL/dkappa * kappa
-    dgmx = gkmx * kappa
+    del gq
+    lam = 3 * 21.6 * E * E * float(kappa.max())   # lambda_max of M^-1 K, p = 2
+    dt_stable = float(f"{1.5 / lam:.0e}")
+
+    def kappa_check(dtv):
+        K, ck = 100, 10
+        g64 = A.ADS(n, (p, p, p), precision=A.PREC_FP64, device=dev)
+        u0 = bumps_state(g64, args.seed)
+        g64.set_coeffs(bumps_state(g64, args.seed + 1))
+        g64.set_form(A.FORM_HEAT, kappa_qp=kappa, dt=dtv)
+        g64.steps(K)
+        u_target = g64.coeffs()
+        (l64, _, gk64), t64 = sync_time(lambda: g64.heat_adjoint(K, ck, u0, u_target, grad=False, grad_kappa=True))
+        gmx = A.ADS(n, (p, p, p), precision=A.PREC_MIXED, refine_tol=1e-10, max_refine=3, device=dev)
+        gmx.set_form(A.FORM_HEAT, kappa_qp=kappa, dt=dtv)
+        (lmx, _, gkmx), tmx = sync_time(lambda: gmx.heat_adjoint(K, ck, u0, u_target, grad=False, grad_kappa=True))
+        dg64 = gk64 * kappa    # dL/dg = dL/dkappa * kappa
+        dgmx = gkmx * kappa
+        n64 = float(np.linalg.norm(dg64))
+        err = float(np.linalg.norm(dgmx - dg64) / n64) if np.isfinite(n64) and n64 > 0 else None
+        gmx.cleanup()
+        g64.cleanup()
+        return {"dt": dtv, "loss_mixed": lmx, "loss_fp64": l64, "dLdg_rel_l2_err_vs_fp64": err,
+                "dLdg_norm": n64, "forward_backward_s_mixed": tmx, "forward_backward_s_fp64": t64}
+
     out["var_kappa_128p2"] = {
-        "config": f"heat {E}^3 p={p}, kappa = exp(g), g Gaussian random field sigma 0.5 corr 0.1, {K} steps dt={dtv}",
-        "loss_mixed": lmx, "loss_fp64": l64,
-        "dLdg_rel_l2_err_vs_fp64": float(np.linalg.norm(dgmx - dg64) / max(np.linalg.norm(dg64), 1e-300)),
-        "dLdg_norm": float(np.linalg.norm(dg64)),
-        "forward_backward_s_mixed": tmx, "forward_backward_s_fp64": t64}
-    gmx.cleanup()
-    g64.cleanup()
+        "config": "heat 128^3 p=2, kappa = exp(g), g Gaussian random field sigma 0.5 corr 0.1 at the quadrature "
+                  "points, 100 steps, checkpoint every 10; mixed (FP32 + FP64 refinement) forward, FP64 adjoint, "
+                  "against an all-FP64 reference gradient",
+        "kappa_max": float(kappa.max()), "dt_lambda_max_at_configured_dt": dtv * lam,
+        "configured_dt": kappa_check(dtv), "stable_dt": kappa_check(dt_stable)}
 
     # ---- 256^3 p=3: mixed vs FP64 step time ----
     # initial coefficients: the seeded bumps at the Greville abscissae (a
@@ -596,7 +629,7 @@ def run_ours(args, world, rank, local):
         "kernel_ms_per_step": {k: v[0] / K for k, v in sorted(pm.items(), key=lambda kv: -kv[1][0])},
         "gpu_launches": res["mixed"]["launches"],
         "cpu_baseline": cpu,
-        "other_configs": aux,
+        "other_configs": finite_or_none(aux),
         "clocks": ck,
     }
     print(json.dumps(line), flush=True)
