@@ -86,6 +86,8 @@ struct ads_handle {
   double* d_kqp = nullptr;
   double* d_l2part = nullptr;
   unsigned char* d_slab = nullptr;  // spill-slab flags per DOF index (x, y, z)
+  int* d_xslab = nullptr;           // x indices of the x slabs
+  int nxslab = 0;
   double* d_part = nullptr;
   double* d_scal = nullptr;
   int* d_flags = nullptr;
@@ -302,6 +304,8 @@ FixupArgs fixup_args(const ads_handle* h, double* F) {
   f.nl2 = h->asm_grid;
   f.scal = h->d_scal;
   f.slab = h->d_slab;
+  f.xslab = h->d_xslab;
+  f.nxslab = h->nxslab;
   return f;
 }
 
@@ -530,7 +534,7 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_fac64[d]); cudaFree(h->d_tfac64[d]); cudaFree(h->d_fac32[d]); cudaFree(h->d_band[d]);
   }
   cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_g32); cudaFree(h->d_wA); cudaFree(h->d_wB);
-  cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_l2part); cudaFree(h->d_slab);
+  cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_l2part); cudaFree(h->d_slab); cudaFree(h->d_xslab);
   cudaFree(h->d_part); cudaFree(h->d_scal); cudaFree(h->d_flags); cudaFree(h->d_hist);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -638,6 +642,12 @@ int create_impl(ads_handle* h) {
     for (int z = 0; z < g.N[2]; ++z) sl[g.N[0] + g.N[1] + z] = in_slab(z, h->asm_zc, h->asm_niz) ? 1 : 0;
     ADS_CUDA(h, cudaMalloc(&h->d_slab, sl.size()));
     ADS_CUDA(h, cudaMemcpy(h->d_slab, sl.data(), sl.size(), cudaMemcpyHostToDevice));
+    std::vector<int> xs;
+    for (int x = 0; x < g.N[0]; ++x)
+      if (sl[x]) xs.push_back(x);
+    h->nxslab = (int)xs.size();
+    ADS_CUDA(h, cudaMalloc(&h->d_xslab, sizeof(int) * std::max<size_t>(xs.size(), 1)));
+    if (!xs.empty()) ADS_CUDA(h, cudaMemcpy(h->d_xslab, xs.data(), sizeof(int) * xs.size(), cudaMemcpyHostToDevice));
   }
   h->norm_parts = 4 * nsm;
   h->npart = std::max(3 * h->res_grid, 2 * h->norm_parts);

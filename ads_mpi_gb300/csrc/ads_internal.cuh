@@ -99,6 +99,8 @@ struct FixupArgs {
   double* scal;          // device scalars (SC_*)
   float* g32;            // if set: every entry of the final F also as float(F * SC_IN_SCALE)
   const unsigned char* slab;  // 1 where a DOF index lies in a spill slab: x [Nx], then y [Ny], then z [Nz]
+  const int* xslab;           // the x indices of the x slabs, ascending
+  int nxslab;
 };
 
 struct SweepArgs {
@@ -258,6 +260,15 @@ __device__ __forceinline__ float d2f_scaled(double d, int sexp) {
 // float -> double (exact) times 2^sexp
 __device__ __forceinline__ double f2d_scaled(float f, int sexp) {
   const unsigned b = __float_as_uint(f);
+  {
+    // common case first: a normal float whose scaled value is a normal double
+    const unsigned e8 = (b >> 23) & 0xffu;
+    const int edn = (int)e8 + 896 + sexp;
+    if (e8 - 1u < 254u && (unsigned)(edn - 1) < 2046u)
+      return __longlong_as_double((long long)(((unsigned long long)(b >> 31) << 63) |
+                                              ((unsigned long long)edn << 52) |
+                                              ((unsigned long long)(b & 0x7fffffu) << 29)));
+  }
   const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
   int e = (int)((b >> 23) & 0xffu);
   unsigned m23 = b & 0x7fffffu;

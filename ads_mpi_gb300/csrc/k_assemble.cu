@@ -611,35 +611,50 @@ __global__ void k_fixup_scale(const FixupArgs a) {
   }
 }
 
-// F += shadow contributions, in class order.  One CTA per (y, z) row, one
-// thread per 4 consecutive x (32-byte aligned: pitches are multiples of 8).
-// Slab membership comes from per-axis byte tables (no integer division in the
-// kernel).  With g32 set (the mixed heat step) every entry of the final F is
-// also written as float(F * 2^-e), the FP32 solve's scaled input; otherwise
-// only quads with a slab entry are read.
+// F += shadow contributions, in class order.  One CTA per (y, z) row.  FP64
+// adds issue per warp at 1/64 of the FP32 rate whatever the active lanes, so
+// the work is arranged to keep warp-level DADDs few: (1) the row's x-slab
+// entries (a host-built list of at most 2 per brick boundary) are finished by
+// one thread each; (2) if the row lies in a y or z slab, every other entry
+// adds the classes of that (row-uniform) zone, one thread per 4 consecutive x
+// (32-byte aligned: pitches are multiples of 8).  With g32 set (the mixed heat
+// step) every entry of the final F is also written as float(F * 2^-e), the
+// FP32 solve's scaled input.  No integer division in the kernel.
 __global__ void k_fixup(const FixupArgs a) {
   const Geometry& g = a.g;
   const int Nx = g.N[0], Ny = g.N[1];
   const int y = blockIdx.y, z = blockIdx.z;
+  const int zyz = (a.slab[Nx + y] ? 2 : 0) | (a.slab[Nx + Ny + z] ? 4 : 0);
+  const size_t rb = (size_t)g.PX * ((size_t)y + (size_t)Ny * z);
+  // (1) x-slab entries: zone = 1 | zyz, classes in fixed order
+  if ((int)threadIdx.x < a.nxslab) {
+    const size_t o = rb + (size_t)a.xslab[threadIdx.x];
+    const int zone = 1 | zyz;
+    double v = a.F[o];
+    for (int cls = 1; cls < 8; ++cls)
+      if ((cls & zone) == cls) v += a.shadow[(size_t)(cls - 1) * a.shadow_stride + o];
+    a.F[o] = v;
+  }
+  if (a.g32 == nullptr && zyz == 0) return;
+  __syncthreads();  // the x-slab entries are final before the row is read
   const int x0 = 4 * threadIdx.x;
   if (x0 >= (int)g.PX) return;
-  const int zyz = (a.slab[Nx + y] ? 2 : 0) | (a.slab[Nx + Ny + z] ? 4 : 0);
-  int zx[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) zx[k] = (x0 + k < Nx) ? (zyz | a.slab[x0 + k]) : 0;
-  const bool any = (zx[0] | zx[1] | zx[2] | zx[3]) != 0;
-  if (a.g32 == nullptr && !any) return;
-  const size_t o = (size_t)g.PX * ((size_t)y + (size_t)Ny * z) + (size_t)x0;
+  const size_t o = rb + (size_t)x0;
   const double2 v01 = *reinterpret_cast<const double2*>(a.F + o);
   const double2 v23 = *reinterpret_cast<const double2*>(a.F + o + 2);
   double v[4] = {v01.x, v01.y, v23.x, v23.y};
-  if (any) {
+  if (zyz != 0) {
+    // (2) entries not in an x slab (those are final already): classes of zyz
+    bool own[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      if (zx[k] != 0) {
-        for (int cls = 1; cls < 8; ++cls)
-          if ((cls & zx[k]) == cls) v[k] += a.shadow[(size_t)(cls - 1) * a.shadow_stride + o + k];
-      }
+    for (int k = 0; k < 4; ++k) own[k] = (x0 + k < Nx) && a.slab[x0 + k] == 0;
+#pragma unroll
+    for (int cls = 2; cls < 8; cls += 2) {
+      if ((cls & zyz) != cls) continue;  // row-uniform
+      const double* sh = a.shadow + (size_t)(cls - 1) * a.shadow_stride + o;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (own[k]) v[k] += sh[k];
     }
     *reinterpret_cast<double2*>(a.F + o) = make_double2(v[0], v[1]);
     *reinterpret_cast<double2*>(a.F + o + 2) = make_double2(v[2], v[3]);
@@ -728,8 +743,9 @@ size_t assemble_smem_bytes(int P, bool fp32) {
 cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s) {
   k_fixup_scale<<<1, 32, 0, s>>>(a);
   const int nq = (int)(a.g.PX / 4);
+  const int nthr = std::max(nq, a.nxslab);
   const dim3 grid(1, a.g.N[1], a.g.N[2]);
-  k_fixup<<<grid, (nq + 31) / 32 * 32, 0, s>>>(a);
+  k_fixup<<<grid, (nthr + 31) / 32 * 32, 0, s>>>(a);
   return cudaGetLastError();
 }
 

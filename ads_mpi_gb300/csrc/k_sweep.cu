@@ -292,20 +292,9 @@ __global__ void __launch_bounds__(SW_LANES)
         }
         T[((i & RMASK) << 5) + j] = x;
       };
-      // mode 2: the state values a chunk adds to are loaded one chunk ahead
       const int xo = lane_base + j;
       const bool xin = xo < a.lanes_total;
       double* const ocol = a.out + (size_t)xo + (size_t)a.out_pitch * (size_t)t3;
-      double oldv[MODE == 2 ? SW_CH : 1];
-      auto load_old = [&](int c) {
-        if constexpr (MODE == 2) {
-          const int r1 = min(SW_CH, L - c * SW_CH);
-          const double* o = ocol + (size_t)a.out_slice * (size_t)(c * SW_CH);
-#pragma unroll
-          for (int r = 0; r < SW_CH; ++r) oldv[r] = (xin && r < r1) ? o[(size_t)a.out_slice * r] : 0.0;
-        }
-      };
-      load_old(nchunk - 1);
       int s = 0;
       for (int c = nchunk - 1; c >= 0; --c) {
         const int se = L - 1 - c * SW_CH + RAMP;  // last step of chunk c
@@ -398,12 +387,15 @@ __global__ void __launch_bounds__(SW_LANES)
             for (int r = 0; r < SW_CH; ++r) {
               if (r < r1) {
                 const double v = out_value<TC>(slot[r * SW_LANES + j], out_exp);
-                if constexpr (MODE == 2) o[(size_t)a.out_slice * r] = oldv[r] + v;
+                // mode 2: a reduction performed at L2 (no return value), so
+                // neither the old value's load nor an FP64 add (1/64 rate,
+                // issued per warp) lands on this warp; each entry receives
+                // exactly one add per solve, so the result is deterministic
+                if constexpr (MODE == 2) atomicAdd(o + (size_t)a.out_slice * r, v);
                 else o[(size_t)a.out_slice * r] = v;
               }
             }
           }
-          if (c > 0) load_old(c - 1);
           __syncwarp();
         }
       }
