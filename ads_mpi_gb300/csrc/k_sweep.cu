@@ -292,9 +292,34 @@ __global__ void __launch_bounds__(SW_LANES)
         }
         T[((i & RMASK) << 5) + j] = x;
       };
+      // Modes 1/2 (final z sweep): lanes are x, positions are z, t3 is y; a
+      // completed chunk's rows (32 x each, coalesced) go out a few at a time
+      // during the following blocks of steps, so the conversions and stores
+      // fill issue slots the dependent recurrence leaves idle.  Each lane
+      // writes and reads only its own column of the ring slot.
       const int xo = lane_base + j;
       const bool xin = xo < a.lanes_total;
       double* const ocol = a.out + (size_t)xo + (size_t)a.out_pitch * (size_t)t3;
+      int pend = -1, prow = 0, prows = 0;  // chunk being written out, next row, its row count
+      auto emit_rows = [&](int n) {
+        if constexpr (MODE == 1 || MODE == 2) {
+          if (pend < 0) return;
+          const TC* slot = T + (pend & (SW_RING - 1)) * (SW_CH * SW_LANES);
+          double* o = ocol + (size_t)a.out_slice * (size_t)(pend * SW_CH);
+          for (int k = 0; k < n && prow < prows; ++k, ++prow) {
+            if (xin) {
+              const double v = out_value<TC>(slot[prow * SW_LANES + j], out_exp);
+              // mode 2: a reduction performed at L2 (no return value), so
+              // neither the old value's load nor an FP64 add (1/64 rate,
+              // issued per warp) lands on this warp; each entry receives
+              // exactly one add per solve, so the result is deterministic
+              if constexpr (MODE == 2) atomicAdd(o + (size_t)a.out_slice * prow, v);
+              else o[(size_t)a.out_slice * prow] = v;
+            }
+          }
+          if (prow >= prows) pend = -1;
+        }
+      };
       int s = 0;
       for (int c = nchunk - 1; c >= 0; --c) {
         const int se = L - 1 - c * SW_CH + RAMP;  // last step of chunk c
@@ -332,6 +357,7 @@ __global__ void __launch_bounds__(SW_LANES)
             }
 #pragma unroll
             for (int t = 0; t < SW_BLK; ++t) T[(((i0 - t) & RMASK) << 5) + j] = yv[t];
+            emit_rows(SW_BLK);
             s += SW_BLK;
           } else if (s + SW_BLK <= sb) {
             // ramp block: lanes outside their line read a clamped position,
@@ -357,6 +383,7 @@ __global__ void __launch_bounds__(SW_LANES)
               }
               if (act) T[((ic & RMASK) << 5) + j] = x;
             }
+            emit_rows(SW_BLK);
             s += SW_BLK;
           } else {
             const int i = L - 1 - (s - j);
@@ -378,27 +405,14 @@ __global__ void __launch_bounds__(SW_LANES)
           }
           __syncwarp();
         } else {
-          __syncwarp();
-          // final z sweep: lanes are x, positions are z, t3 is y; rows of 32 x are coalesced
-          if (xin) {
-            double* o = ocol + (size_t)a.out_slice * (size_t)(c * SW_CH);
-            const int r1 = min(SW_CH, L - c * SW_CH);
-#pragma unroll
-            for (int r = 0; r < SW_CH; ++r) {
-              if (r < r1) {
-                const double v = out_value<TC>(slot[r * SW_LANES + j], out_exp);
-                // mode 2: a reduction performed at L2 (no return value), so
-                // neither the old value's load nor an FP64 add (1/64 rate,
-                // issued per warp) lands on this warp; each entry receives
-                // exactly one add per solve, so the result is deterministic
-                if constexpr (MODE == 2) atomicAdd(o + (size_t)a.out_slice * r, v);
-                else o[(size_t)a.out_slice * r] = v;
-              }
-            }
-          }
-          __syncwarp();
+          // finish the previous chunk's rows, then queue this one
+          emit_rows(SW_CH);
+          pend = c;
+          prow = 0;
+          prows = min(SW_CH, L - c * SW_CH);
         }
       }
+      emit_rows(SW_CH);
     }
   }
   if (MODE == 0 || MODE == 3) {
