@@ -241,34 +241,34 @@ int handle_cuda_fail(ads_handle* h, cudaError_t e, const char* where);
 // flush to signed zero, overflow gives infinity, inf and NaN map to inf and
 // (quiet) NaN.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float d2f_scaled(double d, int sexp) {
+// The rare cases (zero, subnormal, inf, NaN, out of range) live in separate,
+// non-inlined functions so the common path is a short branch-free sequence.
+static __device__ __noinline__ float d2f_scaled_rare(double d, int sexp) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(d);
   const unsigned sign = (unsigned)(b >> 63) << 31;
   const int ed = (int)((b >> 52) & 0x7ffull);
   const unsigned long long m = b & 0xfffffffffffffull;
   if (ed == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m != 0ull ? 0x400000u : 0u));
-  const int ef = ed + sexp - 896;  // biased float exponent after scaling (1023 - 127)
+  const int ef = ed + sexp - 896;
   if (ed == 0 || ef < 1) return __uint_as_float(sign);
-  if (ef > 254) return __uint_as_float(sign | 0x7f800000u);
-  const unsigned m23 = (unsigned)(m >> 29);
-  const unsigned rem = (unsigned)(m & 0x1fffffffull);
+  return __uint_as_float(sign | 0x7f800000u);  // ef > 254: overflow
+}
+
+__device__ __forceinline__ float d2f_scaled(double d, int sexp) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int ed = (int)((b >> 52) & 0x7ffull);
+  const int ef = ed + sexp - 896;  // biased float exponent after scaling (1023 - 127)
+  if ((unsigned)(ed - 1) >= 2046u || (unsigned)(ef - 1) >= 254u) return d2f_scaled_rare(d, sexp);
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  const unsigned m23 = (unsigned)(b >> 29) & 0x7fffffu;
+  const unsigned rem = (unsigned)b & 0x1fffffffu;
   unsigned r = sign | ((unsigned)ef << 23) | m23;
   if (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) r += 1u;  // a carry rounds into the exponent
   return __uint_as_float(r);
 }
 
-// float -> double (exact) times 2^sexp
-__device__ __forceinline__ double f2d_scaled(float f, int sexp) {
+static __device__ __noinline__ double f2d_scaled_rare(float f, int sexp) {
   const unsigned b = __float_as_uint(f);
-  {
-    // common case first: a normal float whose scaled value is a normal double
-    const unsigned e8 = (b >> 23) & 0xffu;
-    const int edn = (int)e8 + 896 + sexp;
-    if (e8 - 1u < 254u && (unsigned)(edn - 1) < 2046u)
-      return __longlong_as_double((long long)(((unsigned long long)(b >> 31) << 63) |
-                                              ((unsigned long long)edn << 52) |
-                                              ((unsigned long long)(b & 0x7fffffu) << 29)));
-  }
   const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
   int e = (int)((b >> 23) & 0xffu);
   unsigned m23 = b & 0x7fffffu;
@@ -285,20 +285,30 @@ __device__ __forceinline__ double f2d_scaled(float f, int sexp) {
   return __longlong_as_double((long long)(sign | ((unsigned long long)ed << 52) | ((unsigned long long)m23 << 29)));
 }
 
+// float -> double (exact) times 2^sexp
+__device__ __forceinline__ double f2d_scaled(float f, int sexp) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e8 = (b >> 23) & 0xffu;
+  const int edn = (int)e8 + 896 + sexp;
+  if (e8 - 1u >= 254u || (unsigned)(edn - 1) >= 2046u) return f2d_scaled_rare(f, sexp);
+  return __longlong_as_double((long long)(((unsigned long long)(b >> 31) << 63) | ((unsigned long long)edn << 52) |
+                                          ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+
 // d * 2^sexp = hi + lo with hi the nearest float and lo the float nearest to
 // the remainder (hi + lo carries ~48 bits); both zero below the float range
 __device__ __forceinline__ void split_scaled(double d, int sexp, float& hi, float& lo) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const unsigned sign = (unsigned)(b >> 63) << 31;
   const int ed = (int)((b >> 52) & 0x7ffull);
-  const unsigned long long m = b & 0xfffffffffffffull;
-  lo = 0.f;
-  if (ed == 0x7ff) { hi = __uint_as_float(sign | 0x7f800000u | (m != 0ull ? 0x400000u : 0u)); return; }
   const int ef = ed + sexp - 896;
-  if (ed == 0 || ef < 1) { hi = __uint_as_float(sign); return; }
-  if (ef > 254) { hi = __uint_as_float(sign | 0x7f800000u); return; }
-  const unsigned m23 = (unsigned)(m >> 29);
-  const unsigned rem = (unsigned)(m & 0x1fffffffull);
+  lo = 0.f;
+  if ((unsigned)(ed - 1) >= 2046u || (unsigned)(ef - 1) >= 254u) {
+    hi = d2f_scaled_rare(d, sexp);  // zero, inf, NaN, under- or overflow: lo = 0
+    return;
+  }
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  const unsigned m23 = (unsigned)(b >> 29) & 0x7fffffu;
+  const unsigned rem = (unsigned)b & 0x1fffffffu;
   const bool up = rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u));
   hi = __uint_as_float((sign | ((unsigned)ef << 23) | m23) + (up ? 1u : 0u));
   // remainder in units of the double's last mantissa bit, 2^(ef - 179)

@@ -301,24 +301,31 @@ __global__ void __launch_bounds__(SW_LANES)
       const bool xin = xo < a.lanes_total;
       double* const ocol = a.out + (size_t)xo + (size_t)a.out_pitch * (size_t)t3;
       int pend = -1, prow = 0, prows = 0;  // chunk being written out, next row, its row count
-      auto emit_rows = [&](int n) {
+      const size_t os = (size_t)a.out_slice;
+      auto emit8 = [&]() {  // the next 8 rows of the pending chunk
         if constexpr (MODE == 1 || MODE == 2) {
           if (pend < 0) return;
-          const TC* slot = T + (pend & (SW_RING - 1)) * (SW_CH * SW_LANES);
-          double* o = ocol + (size_t)a.out_slice * (size_t)(pend * SW_CH);
-          for (int k = 0; k < n && prow < prows; ++k, ++prow) {
-            if (xin) {
-              const double v = out_value<TC>(slot[prow * SW_LANES + j], out_exp);
+          const TC* src = T + (pend & (SW_RING - 1)) * (SW_CH * SW_LANES) + prow * SW_LANES + j;
+          double* q = ocol + os * (size_t)(pend * SW_CH + prow);
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            if (xin && prow + t < prows) {
+              const double v = out_value<TC>(src[t * SW_LANES], out_exp);
               // mode 2: a reduction performed at L2 (no return value), so
               // neither the old value's load nor an FP64 add (1/64 rate,
               // issued per warp) lands on this warp; each entry receives
               // exactly one add per solve, so the result is deterministic
-              if constexpr (MODE == 2) atomicAdd(o + (size_t)a.out_slice * prow, v);
-              else o[(size_t)a.out_slice * prow] = v;
+              if constexpr (MODE == 2) atomicAdd(q, v);
+              else *q = v;
             }
+            q += os;
           }
+          prow += 8;
           if (prow >= prows) pend = -1;
         }
+      };
+      auto emit_rows = [&](int n) {
+        for (int k = 0; k < n; k += 8) emit8();
       };
       int s = 0;
       for (int c = nchunk - 1; c >= 0; --c) {
@@ -357,7 +364,7 @@ __global__ void __launch_bounds__(SW_LANES)
             }
 #pragma unroll
             for (int t = 0; t < SW_BLK; ++t) T[(((i0 - t) & RMASK) << 5) + j] = yv[t];
-            emit_rows(SW_BLK);
+            emit8();
             s += SW_BLK;
           } else if (s + SW_BLK <= sb) {
             // ramp block: lanes outside their line read a clamped position,
@@ -383,7 +390,7 @@ __global__ void __launch_bounds__(SW_LANES)
               }
               if (act) T[((ic & RMASK) << 5) + j] = x;
             }
-            emit_rows(SW_BLK);
+            emit8();
             s += SW_BLK;
           } else {
             const int i = L - 1 - (s - j);
