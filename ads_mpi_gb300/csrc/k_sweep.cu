@@ -64,7 +64,7 @@ __device__ __forceinline__ void cp_async_wait_group() {
 
 constexpr int SW_RING = 4;       // transposed output chunks per warp (power of two)
 constexpr int SW_GROUPS = 4;     // position groups of the staged input
-constexpr int SW_BLK = 8;        // steps per software-pipelined block
+constexpr int SW_BLK = 32;       // steps per software-pipelined block
 
 // Shared memory of one CTA (one warp): staged lines S[32][LS] (TIn), the
 // output ring T[SW_RING * 32 positions][32 lines] (TC), the factor rows
@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(SW_LANES)
             }
 #pragma unroll
             for (int t = 0; t < SW_BLK; ++t) T[(((i0 - t) & RMASK) << 5) + j] = yv[t];
-            emit8();
+            emit_rows(SW_BLK);
             s += SW_BLK;
           } else if (s + SW_BLK <= sb) {
             // ramp block: lanes outside their line read a clamped position,
@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(SW_LANES)
               }
               if (act) T[((ic & RMASK) << 5) + j] = x;
             }
-            emit8();
+            emit_rows(SW_BLK);
             s += SW_BLK;
           } else {
             const int i = L - 1 - (s - j);
