@@ -72,6 +72,7 @@ struct ads_handle {
   double* d_tfac64[3] = {nullptr, nullptr, nullptr};
   float* d_fac32[3] = {nullptr, nullptr, nullptr};
   double* d_band[3] = {nullptr, nullptr, nullptr};
+  float* d_band32[3] = {nullptr, nullptr, nullptr};  // FP32 copies for the updated residual
 
   // device buffers
   double* d_u = nullptr;
@@ -79,6 +80,7 @@ struct ads_handle {
   double* d_r = nullptr;
   double* d_delta = nullptr;  // mixed: increment of the heat step
   float* d_g32 = nullptr;     // mixed: the FP32 solve's scaled input (G, then each residual), L0
+  float* d_x32 = nullptr;     // mixed: the FP32 correction x1, L0
   double* d_wA = nullptr;  // L1 (double-sized; float view uses the same memory)
   double* d_wB = nullptr;  // L2
   double* d_shadow = nullptr;
@@ -105,6 +107,7 @@ struct ads_handle {
   CUtensorMap tm_u_out64{}, tm_r_out64{};
   CUtensorMap tm_wA_out64{}, tm_wB_out64{};
   CUtensorMap tm_wA_out32{}, tm_wB_out32{};
+  CUtensorMap tm_x32_out{};
 
   // form
   bool has_form = false;
@@ -360,7 +363,8 @@ int enqueue_solve64(ads_handle* h, const double* in, const CUtensorMap* tm_out, 
 }
 
 // FP32 Kronecker solve of an L0 input (tin 0: double, scaled by *in_scale on
-// load; tin 1: float, already scaled) into out: mode 1 (out = s x) or 2 (out += s x)
+// load; tin 1: float, already scaled): final_mode 1 writes out = s x (FP64),
+// final_mode 0 writes x itself (FP32) into d_x32
 int enqueue_solve32(ads_handle* h, const void* in, int tin, const double* in_scale, const double* out_scale,
                     int final_mode, const int* skip, const char* tag, double* out) {
   SweepArgs ax = sweep_args(h, 0, h->d_fac32[0], in);
@@ -376,18 +380,22 @@ int enqueue_solve32(ads_handle* h, const void* in, int tin, const double* in_sca
   az.out_scale_dev = out_scale;
   az.skip_flag = skip;
   az.out = out;
-  RUN(h, nz.c_str(), 1, launch_sweep(h->P, 1, 1, final_mode, false, &h->tm_wB_out32, az,  /* map unused */ sweep_grid(h, 2), h->stream));
+  const CUtensorMap* zmap = final_mode == 0 ? &h->tm_x32_out : &h->tm_wB_out32;  // the latter unused
+  RUN(h, nz.c_str(), 1, launch_sweep(h->P, 1, 1, final_mode, false, zmap, az, sweep_grid(h, 2), h->stream));
   return ADS_OK;
 }
 
 // Mixed-precision Kronecker solve of d_F into x with FP64 iterative refinement:
-// x = M^{-1} F by FP32 sweeps, then up to max_refine corrections from the FP64
-// residual F - M x, stopping once ||F - M x|| <= refine_tol ||F||.
+// x = M^{-1} F by FP32 sweeps, then up to max_refine rounds of: FP64 residual
+// r = F - M x, FP32 correction x1 = M^{-1} r, x += x1 and the updated residual
+// r - M x1 with its certified bound (k_resid_update, k_certify), stopping once
+// the bound, or an FP64 residual, is <= refine_tol ||F||.
+// f32_input: the fixup already wrote F 2^-e as float into d_g32 (the heat
+// increment); otherwise the first x sweep reads FP64 F and scales it on load.
+// Each FP64 residual is written to d_g32 with the same scale 2^-e.
 int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready, bool f32_input) {
   // the first solve's scale comes from the assembly (fixup) or, for a caller's F, from a norm pass
   if (!scales_ready) RUN(h, "norm_f", 2, launch_norm_f(h->d_F, h->g, h->d_part, h->norm_parts, h->d_scal, h->stream));
-  // f32_input: the fixup wrote F * 2^-e as float into d_g32, and each residual
-  // is written there with the same scale, so every x sweep reads FP32
   const double* in_s = h->d_scal + SC_IN_SCALE;
   const double* out_s = h->d_scal + SC_OUT_SCALE;
   int st = f32_input ? enqueue_solve32(h, h->d_g32, 1, nullptr, out_s, 1, nullptr, "", x)
@@ -398,16 +406,30 @@ int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready, bool f32_in
     ResidualArgs ra = residual_args(h, x, h->d_F, h->d_r);
     ra.skip_flag = conv;
     ra.want_ff = want_ff;
-    if (f32_input) { ra.r32 = h->d_g32; ra.r32_scale = in_s; }
+    ra.r32 = h->d_g32;
+    ra.r32_scale = in_s;
     RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
     return ADS_OK;
   };
+  UpdateArgs ua{};
+  ua.g = h->g;
+  ua.zc = h->res_zc;
+  ua.nix = h->res_nix; ua.niy = h->res_niy; ua.niz = h->res_niz;
+  ua.x1 = h->d_x32;
+  ua.r1 = h->d_g32;
+  ua.delta = x;
+  ua.out_scale = out_s;
+  for (int d = 0; d < 3; ++d) ua.band[d] = h->d_band32[d];
+  ua.part = h->d_part;
+  ua.skip_flag = conv;
+  const long long ndof = (long long)h->g.N[0] * h->g.N[1] * h->g.N[2];
   for (int k = 0; k < h->opts.max_refine; ++k) {
     if ((st = residual(k == 0))) return st;
     RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, true, k == 0, h->d_scal, h->d_flags, h->stream));
-    st = f32_input ? enqueue_solve32(h, h->d_g32, 1, nullptr, out_s, 2, conv, "_corr", x)
-                   : enqueue_solve32(h, h->d_r, 0, h->d_scal + SC_C_IN, h->d_scal + SC_C_OUT, 2, conv, "_corr", x);
-    if (st) return st;
+    if ((st = enqueue_solve32(h, h->d_g32, 1, nullptr, nullptr, 0, conv, "_corr", nullptr))) return st;
+    RUN(h, "resid_update", 1, launch_resid_update(h->P, ua, h->res_grid, h->stream));
+    RUN(h, "certify", 1, launch_certify(h->d_part, h->res_grid, h->P, ndof, h->opts.refine_tol, h->d_scal,
+                                        h->d_flags, h->stream));
   }
   if ((st = residual(h->opts.max_refine == 0))) return st;
   RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, false, h->opts.max_refine == 0,
@@ -532,8 +554,9 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_nn64[d]); cudaFree(h->d_jw64[d]); cudaFree(h->d_nn32[d]); cudaFree(h->d_jw32[d]);
     cudaFree(h->d_dd64[d]); cudaFree(h->d_dd32[d]);
     cudaFree(h->d_fac64[d]); cudaFree(h->d_tfac64[d]); cudaFree(h->d_fac32[d]); cudaFree(h->d_band[d]);
+    cudaFree(h->d_band32[d]);
   }
-  cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_g32); cudaFree(h->d_wA); cudaFree(h->d_wB);
+  cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_g32); cudaFree(h->d_x32); cudaFree(h->d_wA); cudaFree(h->d_wB);
   cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_l2part); cudaFree(h->d_slab); cudaFree(h->d_xslab);
   cudaFree(h->d_part); cudaFree(h->d_scal); cudaFree(h->d_flags); cudaFree(h->d_hist);
   if (h->ev0) cudaEventDestroy(h->ev0);
@@ -574,7 +597,7 @@ int create_impl(ads_handle* h) {
     std::vector<double> fac, tfac;
     if (band_factor(a, fac, tfac)) return fail(h, ADS_ERR_ZERO_PIVOT, "zero pivot in the 1-D mass matrix");
     std::vector<float> nn32(a.NN.begin(), a.NN.end()), jw32(a.JW.begin(), a.JW.end()), fac32(fac.begin(), fac.end());
-    std::vector<float> dd32(a.DD.begin(), a.DD.end());
+    std::vector<float> dd32(a.DD.begin(), a.DD.end()), band32(a.band.begin(), a.band.end());
     int st;
     if ((st = upload(h, &h->d_nn64[d], a.NN))) return st;
     if ((st = upload(h, &h->d_jw64[d], a.JW))) return st;
@@ -586,6 +609,7 @@ int create_impl(ads_handle* h) {
     if ((st = upload(h, &h->d_tfac64[d], tfac))) return st;
     if ((st = upload(h, &h->d_fac32[d], fac32))) return st;
     if ((st = upload(h, &h->d_band[d], a.band))) return st;
+    if ((st = upload(h, &h->d_band32[d], band32))) return st;
   }
 
   auto zalloc = [&](double** p, size_t n) -> int {
@@ -602,6 +626,9 @@ int create_impl(ads_handle* h) {
     double* g32 = nullptr;
     if ((st = zalloc(&g32, (h->n0 + 1) / 2))) return st;
     h->d_g32 = reinterpret_cast<float*>(g32);
+    double* x32 = nullptr;
+    if ((st = zalloc(&x32, (h->n0 + 1) / 2))) return st;
+    h->d_x32 = reinterpret_cast<float*>(x32);
   }
   if ((st = zalloc(&h->d_wA, h->n1))) return st;
   if ((st = zalloc(&h->d_wB, h->n2))) return st;
@@ -665,6 +692,7 @@ int create_impl(ads_handle* h) {
   ok &= make_l2_out(h, &h->tm_wB_out64, h->d_wB, false);
   ok &= make_l1_out(h, &h->tm_wA_out32, h->d_wA, true);
   ok &= make_l2_out(h, &h->tm_wB_out32, h->d_wB, true);
+  if (h->d_x32) ok &= make_l0_out(h, &h->tm_x32_out, h->d_x32, true);
   if (!ok) return fail(h, ADS_ERR_CUDA, "cuTensorMapEncodeTiled rejected a layout");
   return ADS_OK;
 }

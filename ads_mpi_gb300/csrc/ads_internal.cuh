@@ -141,6 +141,22 @@ struct ResidualArgs {
   int* err;
 };
 
+// Updated residual of an FP32 correction (mixed solve).  r1 = float(r 2^-e)
+// is the scaled FP64 residual that the correction x1 (FP32) was solved for:
+// delta += 2^e x1, and r2 = r1 - M x1 and a = M |x1| are formed in FP32 for
+// the certified bound of k_certify.
+struct UpdateArgs {
+  Geometry g;
+  int zc, nix, niy, niz;
+  const float* x1;           // L0: the correction's FP32 solution
+  const float* r1;           // L0: the scaled FP32 residual it solved for
+  double* delta;             // L0: += 2^e x1
+  const double* out_scale;   // 2^e
+  const float* band[3];      // FP32 copies (round to nearest) of the 1-D mass bands
+  double* part;              // per CTA: [sum (2^24 r2)^2, sum a^2, sum r1^2]
+  const int* skip_flag;
+};
+
 // ---------------------------------------------------------------------------
 // Kernel launchers (defined in the .cu files)
 // ---------------------------------------------------------------------------
@@ -153,8 +169,8 @@ cudaError_t launch_assemble(bool fp32, bool incr, const AssembleArgs& a, const v
 cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s);
 
 // kind: 0 = x sweep (L0 -> L1), 1 = y sweep (L1 -> L2), 2 = z sweep (L2 -> L0)
-// mode: 0 = TMA store to the next layout, 1 = final store to L0 (u = s*x),
-//       2 = final accumulate into L0 (u += s*x), 3 = identity transpose (no solve)
+// mode: 0 = TMA store to the next layout (for the z sweep: FP32 or FP64 L0 through
+//       tmout), 1 = final store to FP64 L0 (u = s*x), 3 = identity transpose (no solve)
 // tin: 0 = double input, 1 = float input; tc: 0 = double compute, 1 = float compute
 // The input is read through a.in (set with sweep_input in the host code).
 cudaError_t launch_sweep(int P, int tin, int tc, int mode, bool trans, const CUtensorMap* tmout,
@@ -169,8 +185,6 @@ enum ScalarSlot {
   SC_RELRES,        // ||r|| / ||F|| of the last residual
   SC_IN_SCALE,      // first solve: input scale 2^-e (max|F| ~ 2^e)
   SC_OUT_SCALE,     // first solve: output scale 2^e
-  SC_C_IN,          // correction: input scale
-  SC_C_OUT,         // correction: output scale
   SC_DOT,           // result of launch_dot
   SC_USCALE,        // 2^-e with max |u| < 2^e, for the FP32 assembly
   SC_COUNT = 16
@@ -184,11 +198,16 @@ enum FlagSlot {
 };
 
 cudaError_t launch_residual(int P, const ResidualArgs& a, int grid, cudaStream_t s);
-// reduce residual partials; sets SC_RR, SC_RELRES, FL_CONV, correction scales and
+// reduce residual partials; sets SC_RR, SC_RELRES, FL_CONV and
 // (if count_iter and not converged) FL_ITERS += 1.  Skipped when FL_CONV is set.
 // use_ff: take ||F||^2 from the partials (and store it) instead of SC_FF
 cudaError_t launch_decide(const double* part, int n, double tol, bool count_iter, bool use_ff, double* scal,
                           int* flags, cudaStream_t s);
+cudaError_t launch_resid_update(int P, const UpdateArgs& a, int grid, cudaStream_t s);
+// from the k_resid_update partials: SC_RELRES = an upper bound of ||F - M x|| / ||F||
+// after the correction, FL_CONV if it is <= tol.  Skipped when FL_CONV is set.
+cudaError_t launch_certify(const double* part, int n, int P, long long ndof, double tol, double* scal, int* flags,
+                           cudaStream_t s);
 // ||F||^2, max|F| and the first-solve scales
 cudaError_t launch_norm_f(const double* F, const Geometry& g, double* part, int nparts, double* scal,
                           cudaStream_t s);

@@ -175,36 +175,30 @@ __device__ __forceinline__ double pow2_exponent_scale(double v, int* e_out) {
 
 __global__ void k_decide(const double* part, int n, double tol, int count_iter, int use_ff, double* scal,
                          int* flags) {
-  __shared__ double s0[256], s1[256], s2[256];
+  __shared__ double s0[256], s1[256];
   if (flags[FL_CONV] != 0) return;
-  double rr = 0.0, ff = 0.0, rmax = 0.0;
+  double rr = 0.0, ff = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     rr += part[3 * i];
     ff += part[3 * i + 1];
-    rmax = fmax(rmax, part[3 * i + 2]);
   }
-  s0[threadIdx.x] = rr; s1[threadIdx.x] = ff; s2[threadIdx.x] = rmax;
+  s0[threadIdx.x] = rr; s1[threadIdx.x] = ff;
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w) {
       s0[threadIdx.x] += s0[threadIdx.x + w];
       s1[threadIdx.x] += s1[threadIdx.x + w];
-      s2[threadIdx.x] = fmax(s2[threadIdx.x], s2[threadIdx.x + w]);
     }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    rr = s0[0]; rmax = s2[0];
+    rr = s0[0];
     if (use_ff) { ff = s1[0]; scal[SC_FF] = ff; }
     else ff = scal[SC_FF];
     scal[SC_RR] = rr;
     const double rel = (ff > 0.0) ? sqrt(rr / ff) : (rr > 0.0 ? INFINITY : 0.0);
     scal[SC_RELRES] = rel;
     const bool conv = (rr <= tol * tol * ff);
-    int e;
-    const double sc = pow2_exponent_scale(rmax, &e);
-    scal[SC_C_OUT] = sc;
-    scal[SC_C_IN] = 1.0 / sc;
     if (conv) flags[FL_CONV] = 1;
     else if (count_iter) flags[FL_ITERS] += 1;
   }
@@ -213,6 +207,273 @@ __global__ void k_decide(const double* part, int n, double tol, int count_iter, 
 cudaError_t launch_decide(const double* part, int n, double tol, bool count_iter, bool use_ff, double* scal,
                           int* flags, cudaStream_t s) {
   k_decide<<<1, 256, 0, s>>>(part, n, tol, count_iter ? 1 : 0, use_ff ? 1 : 0, scal, flags);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Updated residual of an FP32 correction (mixed heat step).
+//
+// The correction x1 solves M x1 = r1 with r1 = float(r 2^-e) and r = F - M x
+// the FP64 residual.  The residual after adding 2^e x1 to x is
+//   F - M (x + 2^e x1) = 2^e (r 2^-e - M x1),
+// and since |r| is already ~1e-7 |F|, computing r1 - M x1 in FP32 leaves an
+// error ~1e-14 |F|, far below refine_tol, so the second FP64 residual of a
+// step is not needed to certify convergence.  The error is bounded
+// rigorously (k_certify): M has non-negative entries (B-splines are
+// non-negative), so each 1-D pass with FP32 band entries m' = fl(m) and an
+// FMA chain of 2P+1 terms returns (A + D) y with |D| <= g_{2P+2} A
+// (g_k = k u / (1 - k u), u = 2^-24), and three passes give
+//   |fl(M x1) - M x1| <= g_K M|x1|,   K = 3 (2P + 2),
+// with M|x1| <= a / (1 - g_K) for the computed a = fl(M |x1|).  With the
+// rounding of r1 itself (u |r1|) and of the subtraction (u |r2| / (1 - u)):
+//   ||r_true|| 2^-e <= (1 + u/(1-u)) ||r2|| + u ||r1|| + g_K/(1-g_K) ||a||.
+// The FP64 rounding of x + 2^e x1 and of the FP64 residual itself are not
+// counted, as for any FP64 residual.  Same tiling as k_residual.
+// ---------------------------------------------------------------------------
+// 4-byte global -> shared copy (cp.async); completion through commit/wait groups
+__device__ __forceinline__ void ru_cp4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void ru_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void ru_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// The kernel is bandwidth-light per plane, so its planes are staged ahead:
+// a ring of RU_RING halo planes of x1 (and each thread's r1 entry of the
+// matching output plane) is filled by cp.async RU_PD(P) planes ahead of the
+// one being reduced.  Halo entries outside the grid stay zero (set once).
+constexpr int RU_RING = 8;
+__host__ __device__ constexpr int ru_pd(int P) { return (7 - P) < 4 ? (7 - P) : 4; }
+
+template <int P>
+__global__ void __launch_bounds__(RS_THREADS) k_resid_update(const UpdateArgs a) {
+  constexpr int W = 2 * P + 1;
+  constexpr int HX = RS_TX + 2 * P, HY = RS_TY + 2 * P;
+  constexpr int PD = ru_pd(P);
+  // a slot is refilled PD planes ahead; it must not be one that is read while
+  // the refill is in flight: the plane being reduced (zin) or the output
+  // plane's centre (zin - P)
+  static_assert(PD >= 1 && PD + P <= RU_RING - 1, "prefetch distance");
+  // r1 of an output plane is in flight for PD rounds and read by its own thread
+  constexpr int R1R = (PD + 1 <= 4) ? 4 : 8;
+  constexpr int NYI = (RS_TY * HX + RS_THREADS - 1) / RS_THREADS;  // y-pass items per thread
+  constexpr int NH = (HY * HX + RS_THREADS - 1) / RS_THREADS;      // halo entries per thread
+  constexpr int ZMAX = 32 + 2 * P;                                  // input planes of a chunk (zc <= 32)
+  __shared__ float xin[RU_RING][HY * HX];
+  __shared__ float r1s_[R1R][RS_THREADS];
+  __shared__ float bys[RS_TY * HX], bya[RS_TY * HX];
+  __shared__ float cz[ZMAX * W];  // cz[(zin - z0 + P) * W + j] = Mz(zin - P + j, zin), 0 outside the grid
+  __shared__ double red[3][RS_THREADS / 32];
+
+  if (a.skip_flag != nullptr && *a.skip_flag != 0) return;
+  const Geometry& g = a.g;
+  const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
+  const int tid = threadIdx.x, tx = tid % RS_TX, ty = tid / RS_TX;
+  const int item = blockIdx.x;
+  const int ix = item % a.nix, iy = (item / a.nix) % a.niy, iz = item / (a.nix * a.niy);
+  const int x0 = ix * RS_TX, y0 = iy * RS_TY, z0 = iz * a.zc;
+  const int z1 = min(z0 + a.zc, Nz);
+  const int out_exp = pow2_exp(*a.out_scale);
+  const size_t plane = (size_t)g.PX * Ny;
+  const int xo = x0 + tx, yo = y0 + ty;
+  const bool own = xo < Nx && yo < Ny;
+  const size_t ocol = own ? (size_t)xo + (size_t)g.PX * yo : 0;
+
+  for (int it = tid; it < RU_RING * HY * HX; it += RS_THREADS) (&xin[0][0])[it] = 0.f;
+  for (int it = tid; it < (z1 - z0 + 2 * P) * W; it += RS_THREADS) {
+    const int zl = it / W, j = it % W;
+    const int zin = z0 - P + zl, zout = zin - P + j;
+    // band[(m + P) N + i] = M_{i, i+m}: row zout, column zin, m = P - j
+    cz[it] = (zin >= 0 && zin < Nz && zout >= 0 && zout < Nz) ? a.band[2][(size_t)(2 * P - j) * Nz + zout] : 0.f;
+  }
+
+  // the y-pass items of this thread (fixed for every plane): smem offset of
+  // their first halo row and their My rows
+  int yoff[NYI];
+  bool yact[NYI];
+  float byc[NYI][W];
+#pragma unroll
+  for (int k = 0; k < NYI; ++k) {
+    const int it = tid + k * RS_THREADS;
+    const int yy = it / HX, hx = it % HX;
+    const int y = y0 + yy;
+    yact[k] = it < RS_TY * HX;
+    yoff[k] = yact[k] ? yy * HX + hx : 0;
+#pragma unroll
+    for (int m = 0; m < W; ++m) byc[k][m] = (yact[k] && y < Ny) ? a.band[1][(size_t)m * Ny + y] : 0.f;
+  }
+  float mx[W];
+#pragma unroll
+  for (int m = 0; m < W; ++m) mx[m] = (xo < Nx) ? a.band[0][(size_t)m * Nx + xo] : 0.f;
+
+  // this thread's halo entries and their columns
+  size_t hcol[NH];
+  bool hok[NH];
+#pragma unroll
+  for (int k = 0; k < NH; ++k) {
+    const int it = tid + k * RS_THREADS;
+    const int hy = it / HX, hx = it % HX;
+    const int x = x0 - P + hx, y = y0 - P + hy;
+    hok[k] = it < HY * HX && x >= 0 && x < Nx && y >= 0 && y < Ny;
+    hcol[k] = hok[k] ? (size_t)x + (size_t)g.PX * y : 0;
+  }
+  __syncthreads();
+
+  // one commit group per input plane q: the x1 halo of plane q (none outside
+  // the grid) and r1 of output plane q - P (which exists also where q is
+  // beyond the grid: the last P planes of the last chunk)
+  auto fetch = [&](int q) {
+    if (q >= 0 && q < Nz && q < z1 + P) {
+      const int sl = q & (RU_RING - 1);
+      const size_t po = plane * (size_t)q;
+#pragma unroll
+      for (int k = 0; k < NH; ++k)
+        if (hok[k]) ru_cp4(&xin[sl][tid + k * RS_THREADS], a.x1 + hcol[k] + po);
+    }
+    const int qo = q - P;
+    if (own && qo >= z0 && qo < z1) ru_cp4(&r1s_[qo & (R1R - 1)][tid], a.r1 + ocol + plane * (size_t)qo);
+    ru_commit();
+  };
+
+  // acc[j]: partial sums of output plane zin - P + j (value and |.| channel)
+  float acs[W], act[W];
+#pragma unroll
+  for (int j = 0; j < W; ++j) { acs[j] = 0.f; act[j] = 0.f; }
+  float rr = 0.f, aa = 0.f, r1q = 0.f;
+
+#pragma unroll 1
+  for (int k = 0; k < PD; ++k) fetch(z0 - P + k);
+#pragma unroll 1
+  for (int zin = z0 - P; zin < z1 + P; ++zin) {
+    ru_wait<PD - 1>();  // plane zin has landed (this thread's copies)
+    __syncthreads();    // ... and everyone's; the slots read last round are free
+    fetch(zin + PD);
+    if (zin >= 0 && zin < Nz) {
+      const float* up = xin[zin & (RU_RING - 1)];
+#pragma unroll
+      for (int k = 0; k < NYI; ++k) {
+        if (yact[k]) {
+          float sv = 0.f, tv = 0.f;
+#pragma unroll
+          for (int m = 0; m < W; ++m) {
+            const float v = up[yoff[k] + m * HX];
+            sv = fmaf(byc[k][m], v, sv);
+            tv = fmaf(byc[k][m], fabsf(v), tv);
+          }
+          bys[tid + k * RS_THREADS] = sv;
+          bya[tid + k * RS_THREADS] = tv;
+        }
+      }
+      __syncthreads();
+      float sv = 0.f, tv = 0.f;
+#pragma unroll
+      for (int m = 0; m < W; ++m) {
+        sv = fmaf(mx[m], bys[ty * HX + tx + m], sv);
+        tv = fmaf(mx[m], bya[ty * HX + tx + m], tv);
+      }
+      const float* c = cz + (zin - z0 + P) * W;
+#pragma unroll
+      for (int j = 0; j < W; ++j) {
+        acs[j] = fmaf(c[j], sv, acs[j]);
+        act[j] = fmaf(c[j], tv, act[j]);
+      }
+    }
+    const int zout = zin - P;  // complete now
+    if (zout >= z0 && zout < z1 && own) {
+      const float r1 = r1s_[zout & (R1R - 1)][tid];
+      const float x1 = xin[zout & (RU_RING - 1)][(ty + P) * HX + tx + P];
+      const float r2 = (r1 - acs[0]) * 16777216.f;  // 2^24: keeps the squares of a converged residual normal
+      rr = fmaf(r2, r2, rr);
+      aa = fmaf(act[0], act[0], aa);
+      r1q = fmaf(r1, r1, r1q);
+      // a reduction performed at L2: neither a load of the old value nor an
+      // FP64 add on this SM; each entry receives exactly one add
+      atomicAdd(a.delta + ocol + plane * (size_t)zout, f2d_scaled(x1, out_exp));
+    }
+#pragma unroll
+    for (int j = 0; j < W - 1; ++j) { acs[j] = acs[j + 1]; act[j] = act[j + 1]; }
+    acs[W - 1] = 0.f;
+    act[W - 1] = 0.f;
+  }
+  ru_wait<0>();
+  double d0 = f2d_scaled(rr, -48), d1 = f2d_scaled(aa, 0), d2 = f2d_scaled(r1q, 0);
+  const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    d0 += __shfl_down_sync(0xffffffffu, d0, o);
+    d1 += __shfl_down_sync(0xffffffffu, d1, o);
+    d2 += __shfl_down_sync(0xffffffffu, d2, o);
+  }
+  if (lane == 0) { red[0][warp] = d0; red[1][warp] = d1; red[2][warp] = d2; }
+  __syncthreads();
+  if (tid == 0) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int w = 0; w < RS_THREADS / 32; ++w) { s0 += red[0][w]; s1 += red[1][w]; s2 += red[2][w]; }
+    a.part[3 * blockIdx.x + 0] = s0;
+    a.part[3 * blockIdx.x + 1] = s1;
+    a.part[3 * blockIdx.x + 2] = s2;
+  }
+}
+
+cudaError_t launch_resid_update(int P, const UpdateArgs& a, int grid, cudaStream_t s) {
+  switch (P) {
+    case 1: k_resid_update<1><<<grid, RS_THREADS, 0, s>>>(a); break;
+    case 2: k_resid_update<2><<<grid, RS_THREADS, 0, s>>>(a); break;
+    case 3: k_resid_update<3><<<grid, RS_THREADS, 0, s>>>(a); break;
+    case 4: k_resid_update<4><<<grid, RS_THREADS, 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// gK = g_K of the bound above; tiny (in the scaled units) covers underflow:
+// r1 entries below 2^-126 flushed to zero, subnormal FP32 results (2^-149 per
+// operation) and squares lost below the FP32 range in the norm sums (at most
+// sqrt(n) 2^-74.5 on a norm, 2^24 below it for ||r2||)
+__global__ void k_certify(const double* part, int n, double gK, double tiny, double tol, double* scal, int* flags) {
+  __shared__ double s0[256], s1[256], s2[256];
+  if (flags[FL_CONV] != 0) return;
+  double rr = 0.0, aa = 0.0, r1 = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    rr += part[3 * i];
+    aa += part[3 * i + 1];
+    r1 += part[3 * i + 2];
+  }
+  s0[threadIdx.x] = rr; s1[threadIdx.x] = aa; s2[threadIdx.x] = r1;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      s0[threadIdx.x] += s0[threadIdx.x + w];
+      s1[threadIdx.x] += s1[threadIdx.x + w];
+      s2[threadIdx.x] += s2[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double u = 0x1p-24;
+    // the per-thread FP32 sums of squares (at most 32 terms each) carry a
+    // relative error below 33 u; 1e-4 covers it with room
+    const double nr2 = sqrt(s0[0]), na = sqrt(s1[0]), nr1 = sqrt(s2[0]);
+    const double b = (1.0 + 1e-4) * ((1.0 + u / (1.0 - u)) * nr2 + u * nr1 + gK / (1.0 - gK) * na) + tiny;
+    const double bound = b * scal[SC_OUT_SCALE];  // back to the units of F
+    const double nf = sqrt(scal[SC_FF]);
+    scal[SC_RELRES] = (nf > 0.0) ? bound / nf : (bound > 0.0 ? INFINITY : 0.0);
+    // false for a NaN or infinite bound: the next round then takes an FP64 residual
+    if (bound <= tol * nf) flags[FL_CONV] = 1;
+  }
+}
+
+cudaError_t launch_certify(const double* part, int n, int P, long long ndof, double tol, double* scal, int* flags,
+                           cudaStream_t s) {
+  const double u = 0x1p-24;
+  const double K = 3.0 * (2 * P + 2);
+  const double gK = K * u / (1.0 - K * u);
+  const double tiny = sqrt((double)ndof) * 0x1p-90;
+  k_certify<<<1, 256, 0, s>>>(part, n, gK, tiny, tol, scal, flags);
   return cudaGetLastError();
 }
 

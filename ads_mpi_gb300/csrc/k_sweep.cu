@@ -24,8 +24,8 @@
 //   z sweep: L2 (z fastest) -> L0 (x fastest)   = solve + ReorderRHSForX
 //
 // Mode 3 skips the solve and is the plain staged transpose used by
-// ads_reorder.  Modes 1 and 2 finish the z sweep with coalesced plain stores
-// into the FP64 state (u = s*x, or u += s*x for a refinement correction).
+// ads_reorder.  Mode 1 finishes the z sweep with coalesced plain stores into
+// the FP64 state (u = s*x).
 // No wait in this kernel spins: cp.async and bulk-group waits complete in
 // hardware.
 #include "ads_internal.cuh"
@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(SW_LANES)
         }
         T[((i & RMASK) << 5) + j] = x;
       };
-      // Modes 1/2 (final z sweep): lanes are x, positions are z, t3 is y; a
+      // Mode 1 (final z sweep): lanes are x, positions are z, t3 is y; a
       // completed chunk's rows (32 x each, coalesced) go out a few at a time
       // during the following blocks of steps, so the conversions and stores
       // fill issue slots the dependent recurrence leaves idle.  Each lane
@@ -303,21 +303,13 @@ __global__ void __launch_bounds__(SW_LANES)
       int pend = -1, prow = 0, prows = 0;  // chunk being written out, next row, its row count
       const size_t os = (size_t)a.out_slice;
       auto emit8 = [&]() {  // the next 8 rows of the pending chunk
-        if constexpr (MODE == 1 || MODE == 2) {
+        if constexpr (MODE == 1) {
           if (pend < 0) return;
           const TC* src = T + (pend & (SW_RING - 1)) * (SW_CH * SW_LANES) + prow * SW_LANES + j;
           double* q = ocol + os * (size_t)(pend * SW_CH + prow);
 #pragma unroll
           for (int t = 0; t < 8; ++t) {
-            if (xin && prow + t < prows) {
-              const double v = out_value<TC>(src[t * SW_LANES], out_exp);
-              // mode 2: a reduction performed at L2 (no return value), so
-              // neither the old value's load nor an FP64 add (1/64 rate,
-              // issued per warp) lands on this warp; each entry receives
-              // exactly one add per solve, so the result is deterministic
-              if constexpr (MODE == 2) atomicAdd(q, v);
-              else *q = v;
-            }
+            if (xin && prow + t < prows) *q = out_value<TC>(src[t * SW_LANES], out_exp);
             q += os;
           }
           prow += 8;
@@ -463,8 +455,6 @@ static cudaError_t launch_mode(int tin, int tc, int mode, bool trans, const CUte
                          : launch_types<P, 0, false>(tin, tc, tmout, a, grid, s);
     case 1: return trans ? launch_types<P, 1, true>(tin, tc, tmout, a, grid, s)
                          : launch_types<P, 1, false>(tin, tc, tmout, a, grid, s);
-    case 2: return trans ? launch_types<P, 2, true>(tin, tc, tmout, a, grid, s)
-                         : launch_types<P, 2, false>(tin, tc, tmout, a, grid, s);
     case 3: return launch_types<P, 3, false>(tin, tc, tmout, a, grid, s);
   }
   return cudaErrorInvalidValue;

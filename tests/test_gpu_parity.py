@@ -108,6 +108,50 @@ def test_mixed_solve_refines_to_tolerance(ads_mod, oracle_mod, E, p):
     assert rel_l2(u, o.solve(F)) < 1e-9
 
 
+def true_rel_residual(ads_mod, E, p, F, u):
+    """||F - M u|| / ||F|| with the FP64 mass operator."""
+    g64, _ = make(ads_mod, E, p)
+    return np.linalg.norm(F - g64.apply_mass(u)) / np.linalg.norm(F)
+
+
+@pytest.mark.parametrize("E,p", [((30, 33, 40), 2), ((17, 24, 9), 3), ((64, 20, 70), 2)])
+def test_mixed_certified_bound_covers_true_residual(ads_mod, E, p):
+    """The refinement stops on the certified bound of the FP32 updated residual
+    r - M x1; the FP64 residual of the result must lie below that bound."""
+    g, _ = make(ads_mod, E, p, prec=1)
+    for seed, smooth in ((31, False), (37, True)):
+        F = np.random.default_rng(seed).standard_normal(g.N)
+        if smooth:
+            # coefficients are x fastest: F(x, y + Ny z)
+            X, Y, Z = np.meshgrid(*[np.linspace(0, 1, m) for m in g.ndof], indexing="ij")
+            bump = np.exp(-20 * ((X - 0.3) ** 2 + (Y - 0.6) ** 2 + (Z - 0.5) ** 2))
+            F = bump.ravel(order="F") + 1e-3 * F
+        u = g.solve(F)
+        st = g.stats()
+        assert st["converged"] and 0 < st["rel_residual"] <= 1e-10
+        assert st["refinements"] >= 1
+        true = true_rel_residual(ads_mod, E, p, F, u)
+        assert true <= st["rel_residual"]
+        if p == 2:
+            # one correction always suffices at p = 2 and the bound certifies it
+            # at once: the reported value is the bound (well above the true
+            # residual), not a fallback FP64 residual (equal to it)
+            assert st["refinements"] == 1
+            assert st["rel_residual"] > 4 * true
+
+
+def test_mixed_bound_above_tolerance_falls_back_to_fp64_residual(ads_mod):
+    """With refine_tol below what the certified bound can show (~1e-12), the
+    next round's FP64 residual decides; the step still converges."""
+    E, p, tol = (30, 33, 40), 2, 3e-13
+    g, _ = make(ads_mod, E, p, prec=1, refine_tol=tol)
+    F = np.random.default_rng(41).standard_normal(g.N)
+    u = g.solve(F)
+    st = g.stats()
+    assert st["converged"] and st["rel_residual"] <= tol
+    assert true_rel_residual(ads_mod, E, p, F, u) <= 2 * tol
+
+
 @pytest.mark.parametrize("s", [(5, 4, 3), (34, 33, 40), (70, 9, 33)])
 def test_reorders_match_reference_permutations(ads_mod, oracle_mod, s):
     E = tuple(v - 1 for v in s)
