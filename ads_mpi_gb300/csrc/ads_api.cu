@@ -87,6 +87,7 @@ struct ads_handle {
   double* d_fqp = nullptr;
   double* d_kqp = nullptr;
   double* d_l2part = nullptr;
+  double* d_stage = nullptr;        // packed copy of one coefficient array (host transfers)
   unsigned char* d_slab = nullptr;  // spill-slab flags per DOF index (x, y, z)
   int* d_xslab = nullptr;           // x indices of the x slabs
   int nxslab = 0;
@@ -557,7 +558,7 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_band32[d]);
   }
   cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_g32); cudaFree(h->d_x32); cudaFree(h->d_wA); cudaFree(h->d_wB);
-  cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_l2part); cudaFree(h->d_slab); cudaFree(h->d_xslab);
+  cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_l2part); cudaFree(h->d_stage); cudaFree(h->d_slab); cudaFree(h->d_xslab);
   cudaFree(h->d_part); cudaFree(h->d_scal); cudaFree(h->d_flags); cudaFree(h->d_hist);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -698,16 +699,37 @@ int create_impl(ads_handle* h) {
 }
 
 // host <-> device copies between the packed user layouts and the padded ones
-int copy_l0_in(ads_handle* h, double* d, const double* host, cudaMemcpyKind kind) {
-  const Geometry& g = h->g;
-  ADS_CUDA(h, cudaMemcpy2DAsync(d, g.PX * 8, host, (size_t)g.N[0] * 8, (size_t)g.N[0] * 8,
-                                (size_t)g.N[1] * g.N[2], kind, h->stream));
+// Host copies go through a packed device buffer with one contiguous copy each
+// (a pitched 2-D copy moves the 2 KB rows one by one over the host link) and
+// an on-device repack; a caller's device array is repacked directly.
+int ensure_stage(ads_handle* h) {
+  if (h->d_stage) return ADS_OK;
+  const size_t n = (size_t)h->g.N[0] * h->g.N[1] * h->g.N[2];
+  ADS_CUDA(h, cudaMalloc((void**)&h->d_stage, sizeof(double) * n));
   return ADS_OK;
 }
-int copy_l0_out(ads_handle* h, double* host, const double* d, cudaMemcpyKind kind) {
-  const Geometry& g = h->g;
-  ADS_CUDA(h, cudaMemcpy2DAsync(host, (size_t)g.N[0] * 8, d, g.PX * 8, (size_t)g.N[0] * 8,
-                                (size_t)g.N[1] * g.N[2], kind, h->stream));
+int copy_l0_in(ads_handle* h, double* d, const double* src, cudaMemcpyKind kind) {
+  const size_t bytes = sizeof(double) * (size_t)h->g.N[0] * h->g.N[1] * h->g.N[2];
+  if (kind == cudaMemcpyDeviceToDevice) {
+    RUN(h, "repack", 1, launch_repack(src, d, h->g, true, h->stream));
+    return ADS_OK;
+  }
+  int st = ensure_stage(h);
+  if (st) return st;
+  ADS_CUDA(h, cudaMemcpyAsync(h->d_stage, src, bytes, kind, h->stream));
+  RUN(h, "repack", 1, launch_repack(h->d_stage, d, h->g, true, h->stream));
+  return ADS_OK;
+}
+int copy_l0_out(ads_handle* h, double* dst, const double* d, cudaMemcpyKind kind) {
+  const size_t bytes = sizeof(double) * (size_t)h->g.N[0] * h->g.N[1] * h->g.N[2];
+  if (kind == cudaMemcpyDeviceToDevice) {
+    RUN(h, "repack", 1, launch_repack(d, dst, h->g, false, h->stream));
+    return ADS_OK;
+  }
+  int st = ensure_stage(h);
+  if (st) return st;
+  RUN(h, "repack", 1, launch_repack(d, h->d_stage, h->g, false, h->stream));
+  ADS_CUDA(h, cudaMemcpyAsync(dst, h->d_stage, bytes, kind, h->stream));
   return ADS_OK;
 }
 

@@ -216,6 +216,8 @@ cudaError_t launch_step_reset(double* scal, int* flags, cudaStream_t s);
 cudaError_t launch_uscale(const double* u, long long n, double* part, int nparts, double* scal, cudaStream_t s);
 cudaError_t launch_record(const double* scal, int* flags, double* hist, int cap, cudaStream_t s);
 
+// packed coefficients (dense Nx) -> padded L0 (to_padded) or back
+cudaError_t launch_repack(const double* src, double* dst, const Geometry& g, bool to_padded, cudaStream_t s);
 // layout conversions between the per-point (kx,ky,kz,ex,ey,ez) layout and the
 // quadrature grid layout qx + QX*(qy + QY*qz)
 cudaError_t launch_qp_to_grid(const double* src, double* dst, const Geometry& g, cudaStream_t s);

@@ -600,6 +600,20 @@ cudaError_t launch_record(const double* scal, int* flags, double* hist, int cap,
 // ---------------------------------------------------------------------------
 // layout conversions
 // ---------------------------------------------------------------------------
+// packed coefficients (x fastest, dense Nx) <-> the padded L0 layout (pitch
+// PX), one CTA per (y, z) row, coalesced along x; padding is never written
+__global__ void k_repack(const double* __restrict__ src, double* __restrict__ dst, int Nx, long long PX,
+                         int to_padded) {
+  const long long row = blockIdx.x;
+  const double* s = src + row * (to_padded ? (long long)Nx : PX);
+  double* d = dst + row * (to_padded ? PX : (long long)Nx);
+  for (int x = threadIdx.x; x < Nx; x += blockDim.x) d[x] = s[x];
+}
+cudaError_t launch_repack(const double* src, double* dst, const Geometry& g, bool to_padded, cudaStream_t s) {
+  const long long rows = (long long)g.N[1] * g.N[2];
+  k_repack<<<(unsigned)rows, 128, 0, s>>>(src, dst, g.N[0], g.PX, to_padded ? 1 : 0);
+  return cudaGetLastError();
+}
 __global__ void k_qp_convert(const double* src, double* dst, Geometry g, int to_grid) {
   const int Q = g.Q;
   const long long Ex = g.E[0], Ey = g.E[1], Ez = g.E[2];

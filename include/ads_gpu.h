@@ -84,7 +84,9 @@ typedef struct ads_handle ads_handle;
 /* per-step statistics of the last ads_step / ads_steps call */
 typedef struct ads_stats {
   double l2norm;        /* the step's l2norm (problems/heat/main.F90:53) */
-  double rel_residual;  /* final ||F - M u|| / ||F|| (mixed), 0 for FP64 */
+  double rel_residual;  /* mixed: an upper bound of the final ||F - M u|| / ||F|| (the
+                           certified bound of the FP32 updated residual, or the FP64
+                           residual where that decided); 0 for FP64 */
   int refinements;      /* corrections applied in the last solve (mixed) */
   int converged;        /* 1 if the refinement reached refine_tol (mixed), 1 for FP64 */
 } ads_stats;
