@@ -45,12 +45,13 @@ NCU_TRAFFIC = {
     ("assemble_f32", "heat256p2"): 164.389888e6 + 163.244544e6,
     ("assemble_f64", "heat256p2"): 167.988992e6 + 164.684544e6,
     ("residual_f64", "heat256p2"): 291.368960e6 + 57.232128e6,
+    ("resid_update", "heat256p2"): 280.506368e6 + 92.415488e6,
     ("fixup", "heat256p2"): 272.985600e6 + 90.721024e6,
-    ("sweep_x_f32", "heat256p2"): 71.079680e6 + 25.775360e6,
-    ("sweep_y_f32", "heat256p2"): 71.082240e6 + 25.671680e6,
-    ("sweep_x_f32_corr", "heat256p2"): 71.079680e6 + 25.775360e6,
-    ("sweep_y_f32_corr", "heat256p2"): 71.082240e6 + 25.671680e6,
-    ("sweep_z_f32", "heat256p2"): 71.573760e6 + 80.585472e6,
+    ("sweep_x_f32", "heat256p2"): 71.094016e6 + 25.629184e6,
+    ("sweep_y_f32", "heat256p2"): 71.095808e6 + 25.124864e6,
+    ("sweep_x_f32_corr", "heat256p2"): 71.097344e6 + 25.651200e6,
+    ("sweep_y_f32_corr", "heat256p2"): 71.095040e6 + 25.052672e6,
+    ("sweep_z_f32", "heat256p2"): 71.513088e6 + 80.461568e6,
 }
 
 
