@@ -19,6 +19,7 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 FORM_PROJECT = 0
 FORM_HEAT = 1
+FORM_OIL = 2
 REORDER_FOR_Y = 0
 REORDER_FOR_Z = 1
 REORDER_FOR_X = 2
@@ -55,6 +56,8 @@ ABI = [
     ("ads_qp_points", [ctypes.c_void_p, ctypes.c_int, _dp], ctypes.c_int),
     ("ads_axis_tables", [ctypes.c_void_p, ctypes.c_int, _dp, _ip, _dp, _dp, _dp], ctypes.c_int),
     ("ads_set_form", [ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_double], ctypes.c_int),
+    ("ads_set_oil", [ctypes.c_void_p, _dp, ctypes.c_double], ctypes.c_int),
+    ("ads_get_drained", [ctypes.c_void_p, _dp], ctypes.c_int),
     ("ads_set_coeffs", [ctypes.c_void_p, _dp], ctypes.c_int),
     ("ads_get_coeffs", [ctypes.c_void_p, _dp], ctypes.c_int),
     ("ads_step", [ctypes.c_void_p, _dp], ctypes.c_int),
@@ -237,6 +240,21 @@ class ADS:
             if a is not None and a.size != self.nqp:
                 raise ValueError(f"per-point array must have {self.nqp} entries")
         self._check(self._L.ads_set_form(self.h, form, _ptr(f), _ptr(k), float(kappa), float(dt)))
+
+    def set_oil(self, drain_qp, mu=10.0):
+        """The oil problem's draining weight w at the points (draining(u, X) =
+        w(X) u, problems/oil/input_data.F90:265-283) and mi (exp(mi u),
+        :297-303); with set_form(FORM_OIL, f_qp=pumping, kappa_qp=Kq, dt=Dt)."""
+        w = _c64(drain_qp)
+        if w.size != self.nqp:
+            raise ValueError(f"per-point array must have {self.nqp} entries")
+        self._check(self._L.ads_set_oil(self.h, _ptr(w), float(mu)))
+
+    def drained(self):
+        """The oil problem's drained total since set_oil (ComputeResults)."""
+        v = ctypes.c_double(0.0)
+        self._check(self._L.ads_get_drained(self.h, ctypes.byref(v)))
+        return v.value
 
     def set_coeffs(self, u):
         u = _c64(u)

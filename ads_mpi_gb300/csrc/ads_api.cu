@@ -86,6 +86,7 @@ struct ads_handle {
   double* d_shadow = nullptr;
   double* d_fqp = nullptr;
   double* d_kqp = nullptr;
+  double* d_dqp = nullptr;  // oil: draining weight per point (qp grid layout)
   double* d_l2part = nullptr;
   double* d_stage = nullptr;        // packed copy of one coefficient array (host transfers)
   unsigned char* d_slab = nullptr;  // spill-slab flags per DOF index (x, y, z)
@@ -115,6 +116,8 @@ struct ads_handle {
   int form = ADS_FORM_PROJECT;
   double kappa = 1.0, dt = 0.0;
   bool has_f = false, has_k = false;
+  bool has_oil = false;  // oil: ads_set_oil was called
+  double mu = 0.0;
 
   ads_stats last{};
 
@@ -291,6 +294,8 @@ AssembleArgs assemble_args(const ads_handle* h, const double* u, double* F, bool
   a.shadow_stride = (long long)h->n0;
   a.fqp = (with_f && h->has_f) ? h->d_fqp : nullptr;
   a.kqp = h->has_k ? h->d_kqp : nullptr;
+  a.dqp = h->has_oil ? h->d_dqp : nullptr;
+  a.mu = h->mu;
   a.l2part = h->d_l2part;
   a.err = h->d_flags + FL_ERR;
   return a;
@@ -335,7 +340,7 @@ int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool 
     t32[d].nn = h->d_nn32[d]; t32[d].jw = h->d_jw32[d]; t32[d].dd = h->d_dd32[d];
   }
   // the FP32 heat assembly works on coefficients scaled by a power of two
-  if (fp32 && h->form == ADS_FORM_HEAT)
+  if (fp32 && (h->form == ADS_FORM_HEAT || h->form == ADS_FORM_OIL))
     RUN(h, "uscale", 2, launch_uscale(u, (long long)h->n0, h->d_part, h->norm_parts, h->d_scal, h->stream));
   a.uscale = h->d_scal + SC_USCALE;
   const void* tx = fp32 ? (const void*)&t32[0] : (const void*)&t64[0];
@@ -453,7 +458,7 @@ int enqueue_solve(ads_handle* h) {
 int enqueue_step(ads_handle* h) {
   RUN(h, "step_reset", 1, launch_step_reset(h->d_scal, h->d_flags, h->stream));
   int st;
-  if (h->opts.precision == ADS_PREC_MIXED && h->form == ADS_FORM_HEAT) {
+  if (h->opts.precision == ADS_PREC_MIXED && (h->form == ADS_FORM_HEAT || h->form == ADS_FORM_OIL)) {
     if ((st = enqueue_assemble(h, h->d_u, h->d_F, true, true, true))) return st;
     if ((st = enqueue_solve_mixed(h, h->d_delta, true, true))) return st;
     RUN(h, "update", 1, launch_add(h->d_u, h->d_delta, (long long)h->n0, h->stream));
@@ -558,7 +563,7 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_band32[d]);
   }
   cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_g32); cudaFree(h->d_x32); cudaFree(h->d_wA); cudaFree(h->d_wB);
-  cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_l2part); cudaFree(h->d_stage); cudaFree(h->d_slab); cudaFree(h->d_xslab);
+  cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_dqp); cudaFree(h->d_l2part); cudaFree(h->d_stage); cudaFree(h->d_slab); cudaFree(h->d_xslab);
   cudaFree(h->d_part); cudaFree(h->d_scal); cudaFree(h->d_flags); cudaFree(h->d_hist);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -679,7 +684,7 @@ int create_impl(ads_handle* h) {
   }
   h->norm_parts = 4 * nsm;
   h->npart = std::max(3 * h->res_grid, 2 * h->norm_parts);
-  if ((st = zalloc(&h->d_l2part, 2 * (size_t)h->asm_grid))) return st;
+  if ((st = zalloc(&h->d_l2part, 3 * (size_t)h->asm_grid))) return st;
   if ((st = zalloc(&h->d_part, (size_t)h->npart))) return st;
   if ((st = zalloc(&h->d_scal, SC_COUNT))) return st;
   ADS_CUDA(h, cudaMalloc(&h->d_flags, sizeof(int) * FL_COUNT));
@@ -829,7 +834,9 @@ int ads_axis_tables(const ads_handle* h, int axis, double* U, int* O, double* J,
 
 int ads_set_form(ads_handle* h, int form, const double* f_qp, const double* kappa_qp, double kappa, double dt) {
   if (!h) return ADS_ERR_ARG;
-  if (form != ADS_FORM_PROJECT && form != ADS_FORM_HEAT) return fail(h, ADS_ERR_ARG, "unknown form");
+  if (form != ADS_FORM_PROJECT && form != ADS_FORM_HEAT && form != ADS_FORM_OIL) return fail(h, ADS_ERR_ARG, "unknown form");
+  if (form == ADS_FORM_OIL && (!f_qp || !kappa_qp))
+    return fail(h, ADS_ERR_ARG, "the oil form needs pumping (f_qp) and Kq (kappa_qp) at the points");
   if (!std::isfinite(kappa) || !std::isfinite(dt)) return fail(h, ADS_ERR_NONFINITE, "non-finite kappa or dt");
   ADS_CUDA(h, cudaSetDevice(h->dev));
   const size_t bytes = sizeof(double) * (size_t)h->nqp;
@@ -852,11 +859,41 @@ int ads_set_form(ads_handle* h, int form, const double* f_qp, const double* kapp
   if (st) return st;
   h->form = form;
   h->has_f = f_qp != nullptr;
-  h->has_k = (form == ADS_FORM_HEAT) && kappa_qp != nullptr;
+  h->has_k = (form == ADS_FORM_HEAT || form == ADS_FORM_OIL) && kappa_qp != nullptr;
   h->kappa = kappa;
   h->dt = dt;
   h->has_form = true;
   invalidate_graph(h);
+  return ADS_OK;
+}
+
+int ads_set_oil(ads_handle* h, const double* drain_qp, double mu) {
+  if (!h || !drain_qp) return ADS_ERR_ARG;
+  if (!std::isfinite(mu)) return fail(h, ADS_ERR_NONFINITE, "non-finite mu");
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  const size_t bytes = sizeof(double) * (size_t)h->nqp;
+  if (!h->d_dqp) ADS_CUDA(h, cudaMalloc((void**)&h->d_dqp, bytes));
+  double* stage = nullptr;
+  ADS_CUDA(h, cudaMalloc((void**)&stage, bytes));
+  int st = ADS_OK;
+  cudaError_t e = cudaMemcpyAsync(stage, drain_qp, bytes, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = launch_qp_to_grid(stage, h->d_dqp, h->g, h->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->d_scal + SC_DRAINED_TOTAL, 0, sizeof(double), h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) st = cuda_fail(h, e, "ads_set_oil");
+  cudaFree(stage);
+  if (st) return st;
+  h->mu = mu;
+  h->has_oil = true;
+  invalidate_graph(h);
+  return ADS_OK;
+}
+
+int ads_get_drained(const ads_handle* h, double* drained) {
+  if (!h || !drained) return ADS_ERR_ARG;
+  ads_handle* hm = const_cast<ads_handle*>(h);
+  ADS_CUDA(hm, cudaSetDevice(h->dev));
+  ADS_CUDA(hm, cudaMemcpy(drained, h->d_scal + SC_DRAINED_TOTAL, sizeof(double), cudaMemcpyDeviceToHost));
   return ADS_OK;
 }
 
@@ -891,6 +928,7 @@ int ads_get_coeffs_device(ads_handle* h, double* d_u) {
 int ads_steps(ads_handle* h, int k, double* l2norms) {
   if (!h || k < 0) return ADS_ERR_ARG;
   if (!h->has_form) return fail(h, ADS_ERR_STATE, "ads_set_form must be called before stepping");
+  if (h->form == ADS_FORM_OIL && !h->has_oil) return fail(h, ADS_ERR_STATE, "ads_set_oil must be called before stepping the oil form");
   if (k == 0) return ADS_OK;
   ADS_CUDA(h, cudaSetDevice(h->dev));
   int st = ensure_hist(h, std::max(k, 64));
@@ -925,6 +963,7 @@ int ads_get_stats(const ads_handle* h, ads_stats* s) {
 int ads_assemble(ads_handle* h, double* F_out, double* l2norm) {
   if (!h || !F_out) return ADS_ERR_ARG;
   if (!h->has_form) return fail(h, ADS_ERR_STATE, "ads_set_form must be called before assembling");
+  if (h->form == ADS_FORM_OIL && !h->has_oil) return fail(h, ADS_ERR_STATE, "ads_set_oil must be called before assembling the oil form");
   ADS_CUDA(h, cudaSetDevice(h->dev));
   int st = enqueue_assemble(h, h->d_u, h->d_F, h->opts.precision == ADS_PREC_MIXED, false, true);
   if (st) return st;

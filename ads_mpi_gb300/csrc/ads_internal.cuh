@@ -83,7 +83,10 @@ struct AssembleArgs {
   long long shadow_stride;
   const double* fqp;   // qp-grid layout (qx + QX*(qy + QY*qz)), may be null
   const double* kqp;   // same layout, may be null
-  double* l2part;      // per CTA: l2 partial at [cta], max |written value| at [grid + cta]
+  const double* dqp;   // oil form: draining weight w (draining(u, X) = w u), same layout
+  double mu;           // oil form: exponent of exp(mu u)
+  double* l2part;      // per CTA: l2 partial at [cta], max |written value| at [grid + cta],
+                       // drained partial (oil form; else 0) at [2 grid + cta]
   const double* uscale;  // FP32 heat form: 2^-e with max |u| < 2^e (coefficients are scaled by it)
   int* err;
 };
@@ -94,7 +97,7 @@ struct FixupArgs {
   double* F;
   const double* shadow;
   long long shadow_stride;
-  const double* l2part;  // [nl2] l2 partials, then [nl2] max |value| partials
+  const double* l2part;  // [nl2] l2 partials, [nl2] max |value| partials, [nl2] drained partials
   int nl2;
   double* scal;          // device scalars (SC_*)
   float* g32;            // if set: every entry of the final F also as float(F * SC_IN_SCALE)
@@ -166,6 +169,9 @@ struct UpdateArgs {
 // actually launched (resident CTAs, at most the work items) is returned
 cudaError_t launch_assemble(bool fp32, bool incr, const AssembleArgs& a, const void* tabs_x,
                             const void* tabs_y, const void* tabs_z, int grid, int* used_grid, cudaStream_t s);
+// the oil form (k_assemble_oil.cu): pump (fqp), Kq (kqp) and w (dqp) all required
+cudaError_t launch_assemble_oil(bool fp32, bool incr, const AssembleArgs& a, const void* tabs_x,
+                                const void* tabs_y, const void* tabs_z, int grid, int* used_grid, cudaStream_t s);
 cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s);
 
 // kind: 0 = x sweep (L0 -> L1), 1 = y sweep (L1 -> L2), 2 = z sweep (L2 -> L0)
@@ -187,6 +193,8 @@ enum ScalarSlot {
   SC_OUT_SCALE,     // first solve: output scale 2^e
   SC_DOT,           // result of launch_dot
   SC_USCALE,        // 2^-e with max |u| < 2^e, for the FP32 assembly
+  SC_DRAINED,       // oil form: drained statistic of the last assembly
+  SC_DRAINED_TOTAL, // oil form: drained summed over the steps since ads_set_oil
   SC_COUNT = 16
 };
 enum FlagSlot {
@@ -214,7 +222,8 @@ cudaError_t launch_norm_f(const double* F, const Geometry& g, double* part, int 
 cudaError_t launch_step_reset(double* scal, int* flags, cudaStream_t s);
 // scal[SC_USCALE] = 2^-e for max |u| over n entries (power-of-two scale of the FP32 assembly)
 cudaError_t launch_uscale(const double* u, long long n, double* part, int nparts, double* scal, cudaStream_t s);
-cudaError_t launch_record(const double* scal, int* flags, double* hist, int cap, cudaStream_t s);
+// hist row of the step; adds the oil drained statistic to its running total
+cudaError_t launch_record(double* scal, int* flags, double* hist, int cap, cudaStream_t s);
 
 // packed coefficients (dense Nx) -> padded L0 (to_padded) or back
 cudaError_t launch_repack(const double* src, double* dst, const Geometry& g, bool to_padded, cudaStream_t s);

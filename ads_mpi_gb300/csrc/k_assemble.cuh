@@ -1,0 +1,625 @@
+// k_assemble.cuh — the Gauss-quadrature assembly kernel (K1) template and its
+// launcher, shared by the translation units that instantiate its forms
+// (k_assemble.cu: projection and heat; k_assemble_oil.cu: the oil problem).
+#pragma once
+#include "ads_internal.cuh"
+
+#include <algorithm>
+
+namespace ads {
+
+template <typename T>
+struct Tabs3 {
+  AxisTab<T> x, y, z;
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void cp_async8(void* dst, const void* src, int src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <int P, typename T>
+struct AsmLayout {
+  static constexpr int Q = P + 1;
+  static constexpr int TX = as_tx(P), TY = AS_TY;
+  static constexpr int CX = TX + P;  // == 32: the x footprint is one warp wide
+  static constexpr int CY = TY + P;
+  static constexpr int NCOL = CX * CY;
+  static constexpr int QY = TY * Q;
+  static constexpr int RC = P + 2;  // coefficient ring (P+1 planes in use + 1 in flight)
+  static constexpr int RF = P + 1;  // accumulator ring
+  static constexpr int NT = Q * (P + 1) * 2;  // table entries per element
+  static constexpr bool F32 = sizeof(T) == 4;
+  static constexpr int NZF = F32 ? 4 : 2;  // z fields: value, d/dz (+ y and x differences in FP32)
+  static constexpr int NYF = F32 ? 4 : 3;  // y fields
+  static_assert(CX == 32, "footprint must be one warp wide");
+  // offsets in bytes
+  static constexpr size_t o_cring = 0;                                          // double [RC][NCOL]
+  static constexpr size_t o_tring = o_cring + sizeof(double) * RC * NCOL;       // float hi, lo [RC][NCOL] (FP32 only)
+  static constexpr size_t o_fring = o_tring + (F32 ? 2 * sizeof(float) * RC * NCOL : 0);
+  static constexpr size_t fring_bytes = F32 ? 2 * sizeof(float) * RF * NCOL : sizeof(double) * RF * NCOL;
+  static constexpr size_t o_za = o_fring + fring_bytes;                         // T [NZF][Q][NCOL]
+  static constexpr size_t o_y = o_za + sizeof(T) * NZF * Q * NCOL;              // T [NYF][QY][CX]
+  static constexpr size_t o_h = o_y + sizeof(T) * NYF * QY * CX;                // T [3][QY][CX]
+  static constexpr size_t o_ny = o_h + sizeof(T) * 3 * QY * CX;
+  static constexpr size_t o_jwy = o_ny + sizeof(T) * TY * NT;
+  static constexpr size_t o_dy = o_jwy + sizeof(T) * TY * Q;                    // T [TY][Q][P]
+  static constexpr size_t o_nz = o_dy + sizeof(T) * TY * Q * P;
+  static constexpr size_t o_dz = o_nz + sizeof(T) * NT;                         // T [Q][P]
+  static constexpr size_t o_jwz = o_dz + sizeof(T) * Q * P;
+  static constexpr size_t o_red = (o_jwz + sizeof(T) * Q + 15) / 16 * 16;
+  static constexpr size_t bytes = o_red + 3 * sizeof(double) * (AS_THREADS / 32);
+};
+
+// One coefficient plane z of the brick's footprint (CY rows of 32 DOFs along
+// x, coalesced) into shared memory with 8-byte cp.async copies; entries
+// outside the mesh are zero-filled.  (The brick's x origin is a multiple of
+// 32 - p, odd for odd p, so 16-byte copies would not stay aligned.)
+template <int P>
+__device__ __forceinline__ void issue_plane(double* ring_plane, const double* __restrict__ u,
+                                            const Geometry& g, int x0, int y0, int z) {
+  constexpr int CX = 32, CY = AS_TY + P;
+  const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
+  for (int it = threadIdx.x; it < CX * CY; it += AS_THREADS) {
+    const int cy = it / CX, cx = it % CX;
+    const int x = x0 + cx, y = y0 + cy;
+    const bool ok = (z < Nz) && (y < Ny) && (x < Nx);
+    const double* src = ok ? u + (size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * z) : u;
+    cp_async8(ring_plane + it, src, ok ? 8 : 0);
+  }
+}
+
+// a per-point input (FP64 in memory) as T; the FP32 conversion is integer work
+template <typename T>
+__device__ __forceinline__ T qp_load(const double* p, long long i) {
+  if constexpr (sizeof(T) == 4) return d2f_scaled(p[i], 0);
+  else return p[i];
+}
+
+// (hi, lo) += v without rounding loss (two-sum)
+__device__ __forceinline__ void two_sum_add(float& hi, float& lo, float v) {
+  const float s = hi + v;
+  const float bp = s - hi;
+  const float err = (hi - (s - bp)) + (v - bp);
+  hi = s;
+  lo += err;
+}
+
+template <int P, typename T, int FORM, bool HAS_F, bool HAS_K, bool INCR>
+__global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (P <= 2 || sizeof(T) == 4 ? 2 : 1))
+    k_assemble(const AssembleArgs a, const Tabs3<T> tb) {
+  using L = AsmLayout<P, T>;
+  constexpr int Q = L::Q, TX = L::TX, TY = L::TY, CX = L::CX, CY = L::CY;
+  constexpr int NCOL = L::NCOL, QY = L::QY, RC = L::RC, RF = L::RF;
+  // the oil problem is the heat form with kappa = Kq exp(mu u) and the source
+  // pump - max(0, w u) (problems/oil/RHS_eq.F90:69-92)
+  constexpr bool OIL = (FORM == ADS_FORM_OIL);
+  constexpr bool HEAT = (FORM == ADS_FORM_HEAT) || OIL;
+  constexpr bool F32 = L::F32;
+  constexpr bool G0_ZERO = (FORM == ADS_FORM_HEAT) && INCR && !HAS_F;  // increment form without source: no v-term
+  // FP32 heat form: coefficients scaled by a power of two and split into
+  // float (hi, lo); the gradient is interpolated from coefficient differences
+  // (hi_a - hi_b) + (lo_a - lo_b), which carry no cancellation, with the
+  // difference weights D_b (dN_b = D_b - D_{b+1})
+  constexpr bool DIFF = F32 && HEAT;
+
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* cring = reinterpret_cast<double*>(smem + L::o_cring);
+  float* thi = reinterpret_cast<float*>(smem + L::o_tring);
+  float* tlo = thi + RC * NCOL;
+  double* fr64 = reinterpret_cast<double*>(smem + L::o_fring);
+  float* frhi = reinterpret_cast<float*>(smem + L::o_fring);
+  float* frlo = frhi + RF * NCOL;
+  T* ZA = reinterpret_cast<T*>(smem + L::o_za);
+  T* ZB = ZA + Q * NCOL;
+  T* ZAY = ZB + Q * NCOL;  // DIFF only
+  T* ZAX = ZAY + Q * NCOL;
+  T* Y0 = reinterpret_cast<T*>(smem + L::o_y);
+  T* Y1 = Y0 + QY * CX;
+  T* Y2 = Y1 + QY * CX;
+  T* Y3 = Y2 + QY * CX;    // DIFF only
+  T* DYs = reinterpret_cast<T*>(smem + L::o_dy);
+  T* DZs = reinterpret_cast<T*>(smem + L::o_dz);
+  T* H0 = reinterpret_cast<T*>(smem + L::o_h);
+  T* H1 = H0 + QY * CX;
+  T* H2 = H1 + QY * CX;
+  T* NYs = reinterpret_cast<T*>(smem + L::o_ny);
+  T* JWYs = reinterpret_cast<T*>(smem + L::o_jwy);
+  T* NZs = reinterpret_cast<T*>(smem + L::o_nz);
+  T* JWZs = reinterpret_cast<T*>(smem + L::o_jwz);
+  double* red = reinterpret_cast<double*>(smem + L::o_red);
+
+  const Geometry& g = a.g;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int Ex = g.E[0], Ey = g.E[1], Ez = g.E[2];
+  const int Nx = g.N[0], Ny = g.N[1];
+  const long long QXt = (long long)Ex * Q, QYt = (long long)Ey * Q;
+  const T dt = (T)a.dt;
+  const T kappa = (T)a.kappa;
+  const T ndtk = -(T)a.dt * (T)a.kappa;
+  const int nitems = a.nix * a.niy * a.niz;
+  // this thread's (element row, footprint column) for the y/z stages
+  const int my_ey = tid / CX, my_cx = tid % CX;
+  // power-of-two scale of the coefficients (FP32 heat form)
+  const int uexp = DIFF ? pow2_exp(*a.uscale) : 0;  // coefficients are multiplied by 2^uexp
+  const T uinv = DIFF ? (T)ldexpf(1.f, -uexp) : T(1);  // back to u (a power of two)
+  const T mu = (T)a.mu;
+
+  double l2_thread = 0.0;
+  double dr_thread = 0.0;  // oil: sum of J W max(0, w u), the drained statistic / dt
+  // max |value| written by this thread, as the bit pattern of a non-negative
+  // double (integer order = numeric order); feeds the FP32 solve's scale
+  unsigned long long amax_bits = 0ull;
+
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const int ix = item % a.nix;
+    const int iy = (item / a.nix) % a.niy;
+    const int iz = item / (a.nix * a.niy);
+    const int x0 = ix * TX, y0 = iy * TY;
+    const int ez0 = iz * a.zc;
+    const int ez1 = min(ez0 + a.zc, Ez);
+    const bool lastx = (ix == a.nix - 1), lasty = (iy == a.niy - 1), lastz = (iz == a.niz - 1);
+
+    __syncthreads();  // previous item fully done with shared memory
+
+    // per-lane x tables (element x0 + lane; lanes >= TX have no element)
+    T nx[Q][P + 1][2];
+    T jwx[Q];
+    T dx[DIFF ? Q : 1][DIFF ? P : 1];
+    const bool lane_elem = (lane < TX) && (x0 + lane < Ex);
+    {
+      const int ex = x0 + lane;
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        jwx[k] = lane_elem ? tb.x.jw[(size_t)ex * Q + k] : T(0);
+#pragma unroll
+        for (int b = 0; b <= P; ++b) {
+          nx[k][b][0] = lane_elem ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 0] : T(0);
+          nx[k][b][1] = lane_elem ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 1] : T(0);
+        }
+        if constexpr (DIFF) {
+#pragma unroll
+          for (int b = 0; b < P; ++b) dx[k][b] = lane_elem ? tb.x.dd[((size_t)ex * Q + k) * P + b] : T(0);
+        }
+      }
+    }
+    if (DIFF) {
+      for (int i = tid; i < TY * Q * P; i += AS_THREADS) {
+        const int ey = y0 + i / (Q * P);
+        DYs[i] = (ey < Ey) ? tb.y.dd[(size_t)ey * Q * P + (i % (Q * P))] : T(0);
+      }
+    }
+    for (int i = tid; i < TY * L::NT; i += AS_THREADS) {
+      const int ey = y0 + i / L::NT;
+      NYs[i] = (ey < Ey) ? tb.y.nn[(size_t)ey * L::NT + (i % L::NT)] : T(0);
+    }
+    for (int i = tid; i < TY * Q; i += AS_THREADS) {
+      const int ey = y0 + i / Q;
+      JWYs[i] = (ey < Ey) ? tb.y.jw[(size_t)ey * Q + (i % Q)] : T(0);
+    }
+    if (F32) {
+      for (int i = tid; i < 2 * RF * NCOL; i += AS_THREADS) frhi[i] = 0.f;
+    } else {
+      for (int i = tid; i < RF * NCOL; i += AS_THREADS) fr64[i] = 0.0;
+    }
+
+    // initial coefficient planes ez0 .. ez0+P
+    if (HEAT) {
+#pragma unroll
+      for (int b = 0; b <= P; ++b) issue_plane<P>(cring + ((ez0 + b) % RC) * NCOL, a.u, g, x0, y0, ez0 + b);
+    }
+    cp_async_commit();
+
+    // l2 partial: FP64 (FP64 mode) or a compensated (hi, lo) float pair
+    T l2_item = T(0);
+    float l2_lo = 0.f;
+    T dr_item = T(0);
+    float dr_lo = 0.f;
+
+    for (int ez = ez0; ez < ez1; ++ez) {
+      T l2_layer = T(0);
+      T dr_layer = T(0);
+      // prefetch the plane the next layer adds
+      if (HEAT && ez + 1 < ez1) issue_plane<P>(cring + ((ez + P + 1) % RC) * NCOL, a.u, g, x0, y0, ez + P + 1);
+      cp_async_commit();
+      for (int i = tid; i < L::NT; i += AS_THREADS) NZs[i] = tb.z.nn[(size_t)ez * L::NT + i];
+      for (int i = tid; i < Q; i += AS_THREADS) JWZs[i] = tb.z.jw[(size_t)ez * Q + i];
+      if (DIFF)
+        for (int i = tid; i < Q * P; i += AS_THREADS) DZs[i] = tb.z.dd[(size_t)ez * Q * P + i];
+      cp_async_wait<1>();
+      __syncthreads();
+
+      // FP32: split each coefficient plane once, when it arrives
+      if (DIFF) {
+        const int zlo = (ez == ez0) ? ez : ez + P;
+        for (int z = zlo; z <= ez + P; ++z) {
+          const double* src = cring + (z % RC) * NCOL;
+          float* dh = thi + (z % RC) * NCOL;
+          float* dl = tlo + (z % RC) * NCOL;
+          for (int i = tid; i < NCOL; i += AS_THREADS) split_scaled(src[i], uexp, dh[i], dl[i]);
+        }
+        __syncthreads();
+      }
+
+      // ---- z interpolation, per column: ZA = sum_b Nz C, ZB = d/dz; in FP32
+      //      also the z-interpolated y and x coefficient differences ----
+      if (HEAT) {
+        for (int col = tid; col < NCOL; col += AS_THREADS) {
+          if constexpr (DIFF) {
+            const int cy = col / CX, cx = col % CX;
+            T c[P + 1], dz[P + 1], dyv[P + 1], dxv[P + 1];
+#pragma unroll
+            for (int b = 0; b <= P; ++b) {
+              const int o = ((ez + b) % RC) * NCOL + col;
+              const float h = thi[o], l = tlo[o];
+              c[b] = h;
+              dyv[b] = (cy > 0) ? (h - thi[o - CX]) + (l - tlo[o - CX]) : T(0);
+              dxv[b] = (cx > 0) ? (h - thi[o - 1]) + (l - tlo[o - 1]) : T(0);
+              if (b > 0) {
+                const int op = ((ez + b - 1) % RC) * NCOL + col;
+                dz[b] = (h - thi[op]) + (l - tlo[op]);
+              }
+            }
+#pragma unroll
+            for (int kz = 0; kz < Q; ++kz) {
+              T za = T(0), zb = T(0), zy = T(0), zx = T(0);
+#pragma unroll
+              for (int b = 0; b <= P; ++b) {
+                const T nzv = NZs[(kz * (P + 1) + b) * 2 + 0];
+                za += nzv * c[b];
+                zy += nzv * dyv[b];
+                zx += nzv * dxv[b];
+                if (b > 0) zb += DZs[kz * P + (b - 1)] * dz[b];
+              }
+              ZA[kz * NCOL + col] = za;
+              ZB[kz * NCOL + col] = zb;
+              ZAY[kz * NCOL + col] = zy;
+              ZAX[kz * NCOL + col] = zx;
+            }
+          } else {
+            T c[P + 1];
+#pragma unroll
+            for (int b = 0; b <= P; ++b) c[b] = (T)cring[((ez + b) % RC) * NCOL + col];
+#pragma unroll
+            for (int kz = 0; kz < Q; ++kz) {
+              T za = T(0), zb = T(0);
+#pragma unroll
+              for (int b = 0; b <= P; ++b) {
+                za += NZs[(kz * (P + 1) + b) * 2 + 0] * c[b];
+                zb += NZs[(kz * (P + 1) + b) * 2 + 1] * c[b];
+              }
+              ZA[kz * NCOL + col] = za;
+              ZB[kz * NCOL + col] = zb;
+            }
+          }
+        }
+        __syncthreads();
+      }
+
+      // per-thread partial sums of this layer for DOF rows my_ey+by, planes ez+bz
+      T acc[P + 1][P + 1];
+#pragma unroll
+      for (int by = 0; by <= P; ++by)
+#pragma unroll
+        for (int bz = 0; bz <= P; ++bz) acc[by][bz] = T(0);
+
+#pragma unroll 1
+      for (int kz = 0; kz < Q; ++kz) {
+        // ---- y interpolation, one (element row, column) per thread ----
+        if (HEAT) {
+          T za[P + 1], zb[P + 1], zy[P + 1], zx[P + 1];
+#pragma unroll
+          for (int b = 0; b <= P; ++b) {
+            za[b] = ZA[kz * NCOL + (my_ey + b) * CX + my_cx];
+            zb[b] = ZB[kz * NCOL + (my_ey + b) * CX + my_cx];
+            if constexpr (DIFF) {
+              zy[b] = ZAY[kz * NCOL + (my_ey + b) * CX + my_cx];
+              zx[b] = ZAX[kz * NCOL + (my_ey + b) * CX + my_cx];
+            }
+          }
+#pragma unroll
+          for (int ky = 0; ky < Q; ++ky) {
+            T y0v = T(0), y1v = T(0), y2v = T(0), y3v = T(0);
+#pragma unroll
+            for (int b = 0; b <= P; ++b) {
+              const T nyv = NYs[my_ey * L::NT + (ky * (P + 1) + b) * 2 + 0];
+              y0v += nyv * za[b];
+              y2v += nyv * zb[b];
+              if constexpr (DIFF) {
+                y3v += nyv * zx[b];
+                if (b > 0) y1v += DYs[(my_ey * Q + ky) * P + (b - 1)] * zy[b];
+              } else {
+                const T dny = NYs[my_ey * L::NT + (ky * (P + 1) + b) * 2 + 1];
+                y1v += dny * za[b];
+              }
+            }
+            const int qy = my_ey * Q + ky;
+            Y0[qy * CX + my_cx] = y0v;
+            Y1[qy * CX + my_cx] = y1v;
+            Y2[qy * CX + my_cx] = y2v;
+            if constexpr (DIFF) Y3[qy * CX + my_cx] = y3v;
+          }
+          __syncthreads();
+        }
+
+        // ---- x interpolation + integrand + x test contraction (warp per row) ----
+        for (int qy = warp; qy < QY; qy += AS_THREADS / 32) {
+          const int ey_l = qy / Q;
+          const bool elem_ok = lane_elem && (y0 + ey_l < Ey);
+          const T jwyz = JWYs[qy] * JWZs[kz];
+          T h0[P + 1], h1[P + 1], h2[P + 1];
+#pragma unroll
+          for (int b = 0; b <= P; ++b) { h0[b] = T(0); h1[b] = T(0); h2[b] = T(0); }
+          T yv0[P + 1], yv1[P + 1], yv2[P + 1], yv3[P + 1];
+          if (HEAT) {
+#pragma unroll
+            for (int b = 0; b <= P; ++b) {
+              yv0[b] = lane_elem ? Y0[qy * CX + lane + b] : T(0);
+              yv1[b] = lane_elem ? Y1[qy * CX + lane + b] : T(0);
+              yv2[b] = lane_elem ? Y2[qy * CX + lane + b] : T(0);
+              if constexpr (DIFF) yv3[b] = (lane_elem && b > 0) ? Y3[qy * CX + lane + b] : T(0);
+            }
+          }
+          const long long qyg = (long long)y0 * Q + qy;
+          const long long qzg = (long long)ez * Q + kz;
+#pragma unroll
+          for (int kx = 0; kx < Q; ++kx) {
+            const T s = jwx[kx] * jwyz;
+            const long long qidx = ((long long)(x0 + lane) * Q + kx) + QXt * (qyg + QYt * qzg);
+            if (HEAT) {
+              T uu = T(0), dux = T(0), duy = T(0), duz = T(0);
+#pragma unroll
+              for (int b = 0; b <= P; ++b) {
+                uu += nx[kx][b][0] * yv0[b];
+                if constexpr (DIFF) {
+                  if (b > 0) dux += dx[kx][b - 1] * yv3[b];
+                } else {
+                  dux += nx[kx][b][1] * yv0[b];
+                }
+                duy += nx[kx][b][0] * yv1[b];
+                duz += nx[kx][b][0] * yv2[b];
+              }
+              T fv = T(0);
+              if (HAS_F) {
+                // in FP32 the source carries the coefficients' scale 2^uexp
+                if constexpr (DIFF) fv = elem_ok ? d2f_scaled(a.fqp[qidx], uexp) : T(0);
+                else fv = elem_ok ? a.fqp[qidx] : T(0);
+              }
+              T c;
+              if (HAS_K) c = -dt * (elem_ok ? qp_load<T>(a.kqp, qidx) : T(0)) * s;
+              else c = ndtk * s;
+              if constexpr (OIL) {
+                // kqval exp(mi u) and vdrain = max(0, w u): u itself is uu 2^-uexp
+                // in FP32 (uinv), and the drain, like fv, keeps the scale
+                if constexpr (F32) c *= expf(mu * (uu * uinv));
+                else c *= exp(mu * uu);
+                const T w = elem_ok ? qp_load<T>(a.dqp, qidx) : T(0);
+                const T vdr = w * uu > T(0) ? w * uu : T(0);
+                fv -= vdr;
+                dr_layer += s * vdr;
+              }
+              const T g1 = c * dux, g2 = c * duy, g3 = c * duz;
+              l2_layer += s * uu * uu;
+              if (G0_ZERO) {
+#pragma unroll
+                for (int b = 0; b <= P; ++b) {
+                  h0[b] += nx[kx][b][1] * g1;
+                  h1[b] += nx[kx][b][0] * g2;
+                  h2[b] += nx[kx][b][0] * g3;
+                }
+              } else {
+                // INCR: the mass term J W v u is left out (its exact-quadrature
+                // value M u is added back analytically)
+                const T g0 = INCR ? s * dt * fv : (HAS_F ? s * (uu + dt * fv) : s * uu);
+#pragma unroll
+                for (int b = 0; b <= P; ++b) {
+                  h0[b] += nx[kx][b][0] * g0 + nx[kx][b][1] * g1;
+                  h1[b] += nx[kx][b][0] * g2;
+                  h2[b] += nx[kx][b][0] * g3;
+                }
+              }
+            } else {
+              const T fv = (HAS_F && elem_ok) ? qp_load<T>(a.fqp, qidx) : (HAS_F ? T(0) : T(1));
+              const T g0 = s * fv;
+              l2_layer += s * fv * fv;
+#pragma unroll
+              for (int b = 0; b <= P; ++b) h0[b] += nx[kx][b][0] * g0;
+            }
+          }
+          // column cx = lane receives local function b of element lane - b
+          T v0 = h0[0], v1 = h1[0], v2 = h2[0];
+#pragma unroll
+          for (int b = 1; b <= P; ++b) {
+            const T s0 = __shfl_up_sync(0xffffffffu, h0[b], b);
+            const T s1 = HEAT ? __shfl_up_sync(0xffffffffu, h1[b], b) : T(0);
+            const T s2 = HEAT ? __shfl_up_sync(0xffffffffu, h2[b], b) : T(0);
+            if (lane >= b) { v0 += s0; v1 += s1; v2 += s2; }
+          }
+          H0[qy * CX + lane] = v0;
+          if (HEAT) { H1[qy * CX + lane] = v1; H2[qy * CX + lane] = v2; }
+        }
+        __syncthreads();
+
+        // ---- y test contraction of this thread's element row, then z ----
+        {
+          T i0[P + 1], i1[P + 1];
+#pragma unroll
+          for (int by = 0; by <= P; ++by) { i0[by] = T(0); i1[by] = T(0); }
+#pragma unroll
+          for (int ky = 0; ky < Q; ++ky) {
+            const int qy = my_ey * Q + ky;
+            const T hv0 = H0[qy * CX + my_cx];
+            const T hv1 = HEAT ? H1[qy * CX + my_cx] : T(0);
+            const T hv2 = HEAT ? H2[qy * CX + my_cx] : T(0);
+#pragma unroll
+            for (int by = 0; by <= P; ++by) {
+              const T nyv = NYs[my_ey * L::NT + (ky * (P + 1) + by) * 2 + 0];
+              if (HEAT) {
+                const T dny = NYs[my_ey * L::NT + (ky * (P + 1) + by) * 2 + 1];
+                i0[by] += nyv * hv0 + dny * hv1;
+                i1[by] += nyv * hv2;
+              } else {
+                i0[by] += nyv * hv0;
+              }
+            }
+          }
+#pragma unroll
+          for (int bz = 0; bz <= P; ++bz) {
+            const T nz0 = NZs[(kz * (P + 1) + bz) * 2 + 0];
+            const T nz1 = NZs[(kz * (P + 1) + bz) * 2 + 1];
+#pragma unroll
+            for (int by = 0; by <= P; ++by) {
+              if (HEAT) acc[by][bz] += nz0 * i0[by] + nz1 * i1[by];
+              else acc[by][bz] += nz0 * i0[by];
+            }
+          }
+        }
+        if (!HEAT) __syncthreads();
+      }  // kz
+
+      if constexpr (F32) {
+        two_sum_add(l2_item, l2_lo, l2_layer);
+        if constexpr (OIL) two_sum_add(dr_item, dr_lo, dr_layer);
+      } else {
+        l2_item += l2_layer;
+        if constexpr (OIL) dr_item += dr_layer;
+      }
+
+      // accumulate this layer's element partials into the DOF planes, one
+      // element-row offset at a time so no two threads touch the same entry
+#pragma unroll
+      for (int by = 0; by <= P; ++by) {
+        const int row = my_ey + by;
+#pragma unroll
+        for (int bz = 0; bz <= P; ++bz) {
+          const int o = ((ez + bz) % RF) * NCOL + row * CX + my_cx;
+          if (F32) two_sum_add(frhi[o], frlo[o], (float)acc[by][bz]);
+          else fr64[o] += (double)acc[by][bz];
+        }
+        __syncthreads();
+      }
+
+      // DOF plane ez is complete: write it out and clear its ring slot
+      {
+        const int cz = ez;
+        const bool ownz = (cz < ez1) || lastz;
+        const int slot = (cz % RF) * NCOL;
+        for (int it = tid; it < NCOL; it += AS_THREADS) {
+          const int cy = it / CX, cx = it % CX;
+          const int x = x0 + cx, y = y0 + cy;
+          double v;
+          if (F32) {
+            v = f2d_scaled(frhi[slot + it], -uexp) + f2d_scaled(frlo[slot + it], -uexp);
+            frhi[slot + it] = 0.f;
+            frlo[slot + it] = 0.f;
+          } else {
+            v = fr64[slot + it];
+            fr64[slot + it] = 0.0;
+          }
+          if (x < Nx && y < Ny) {
+            const bool ownx = (cx < TX) || lastx, owny = (cy < TY) || lasty;
+            const int cls = (ownx ? 0 : 1) | (owny ? 0 : 2) | (ownz ? 0 : 4);
+            double* dst = (cls == 0) ? a.F : a.shadow + (size_t)(cls - 1) * a.shadow_stride;
+            dst[(size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * cz)] = v;
+            const unsigned long long vb = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+            amax_bits = vb > amax_bits ? vb : amax_bits;
+          }
+        }
+      }
+      __syncthreads();
+    }  // ez
+
+    // remaining planes ez1 .. ez1+P-1
+    for (int cz = ez1; cz < ez1 + P; ++cz) {
+      const bool ownz = lastz;
+      const int slot = (cz % RF) * NCOL;
+      for (int it = tid; it < NCOL; it += AS_THREADS) {
+        const int cy = it / CX, cx = it % CX;
+        const int x = x0 + cx, y = y0 + cy;
+        if (x < Nx && y < Ny && cz < g.N[2]) {
+          const double v = F32 ? f2d_scaled(frhi[slot + it], -uexp) + f2d_scaled(frlo[slot + it], -uexp)
+                               : fr64[slot + it];
+          const bool ownx = (cx < TX) || lastx, owny = (cy < TY) || lasty;
+          const int cls = (ownx ? 0 : 1) | (owny ? 0 : 2) | (ownz ? 0 : 4);
+          double* dst = (cls == 0) ? a.F : a.shadow + (size_t)(cls - 1) * a.shadow_stride;
+          dst[(size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * cz)] = v;
+          const unsigned long long vb = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+          amax_bits = vb > amax_bits ? vb : amax_bits;
+        }
+      }
+    }
+    l2_thread += (double)l2_item + (double)l2_lo;
+    if constexpr (OIL) dr_thread += (double)dr_item + (double)dr_lo;
+    cp_async_wait<0>();
+  }  // item
+
+  // deterministic block reduction of the l2 and drained partials and of max |value|
+  double v = l2_thread, dv = dr_thread;
+  unsigned long long mb = amax_bits;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v += __shfl_down_sync(0xffffffffu, v, o);
+    if constexpr (OIL) dv += __shfl_down_sync(0xffffffffu, dv, o);
+    const unsigned long long ob = __shfl_down_sync(0xffffffffu, mb, o);
+    mb = ob > mb ? ob : mb;
+  }
+  __syncthreads();
+  unsigned long long* redm = reinterpret_cast<unsigned long long*>(red + AS_THREADS / 32);
+  double* redd = red + 2 * (AS_THREADS / 32);
+  if (lane == 0) { red[warp] = v; redm[warp] = mb; redd[warp] = dv; }
+  __syncthreads();
+  if (tid == 0) {
+    double t = 0.0, d = 0.0;
+    unsigned long long m = 0ull;
+    for (int w = 0; w < AS_THREADS / 32; ++w) {
+      t += red[w];
+      d += redd[w];
+      m = redm[w] > m ? redm[w] : m;
+    }
+    // the FP32 heat form integrated (2^uexp u)^2, and the drain 2^uexp w u
+    a.l2part[blockIdx.x] = DIFF ? t * ldexp(1.0, -2 * uexp) : t;
+    a.l2part[gridDim.x + blockIdx.x] = __longlong_as_double((long long)m);
+    a.l2part[2 * gridDim.x + blockIdx.x] = (DIFF ? d * ldexp(1.0, -uexp) : d) * a.dt;
+  }
+}
+
+
+template <int P, typename T, int FORM, bool HF, bool HK, bool INCR>
+static cudaError_t launch_one(const AssembleArgs& a, const void* tx, const void* ty, const void* tz,
+                              int grid, int* used_grid, cudaStream_t s) {
+  using L = AsmLayout<P, T>;
+  Tabs3<T> tb;
+  tb.x = *static_cast<const AxisTab<T>*>(tx);
+  tb.y = *static_cast<const AxisTab<T>*>(ty);
+  tb.z = *static_cast<const AxisTab<T>*>(tz);
+  auto kern = k_assemble<P, T, FORM, HF, HK, INCR>;
+  const size_t bytes = L::bytes;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return e;
+  // persistent: the resident CTA count (registers and shared memory), at most `grid`
+  int per_sm = 0, dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, AS_THREADS, bytes);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  const int items = a.nix * a.niy * a.niz;
+  int g = std::min(std::min(grid, items), nsm * per_sm);
+  if (g < 1) g = 1;
+  *used_grid = g;
+  kern<<<g, AS_THREADS, bytes, s>>>(a, tb);
+  return cudaGetLastError();
+}
+
+
+}  // namespace ads

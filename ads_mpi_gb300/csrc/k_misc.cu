@@ -581,7 +581,7 @@ cudaError_t launch_step_reset(double* scal, int* flags, cudaStream_t s) {
 }
 
 // hist rows of 4 doubles: l2norm, relative residual, corrections, converged
-__global__ void k_record(const double* scal, int* flags, double* hist, int cap) {
+__global__ void k_record(double* scal, int* flags, double* hist, int cap) {
   if (threadIdx.x != 0) return;
   const int c = flags[FL_HIST];
   if (c < cap) {
@@ -591,8 +591,9 @@ __global__ void k_record(const double* scal, int* flags, double* hist, int cap) 
     hist[4 * c + 3] = (double)flags[FL_CONV];
   }
   flags[FL_HIST] = c + 1;
+  scal[SC_DRAINED_TOTAL] += scal[SC_DRAINED];  // oil form; 0 for the others
 }
-cudaError_t launch_record(const double* scal, int* flags, double* hist, int cap, cudaStream_t s) {
+cudaError_t launch_record(double* scal, int* flags, double* hist, int cap, cudaStream_t s) {
   k_record<<<1, 32, 0, s>>>(scal, flags, hist, cap);
   return cudaGetLastError();
 }

@@ -150,3 +150,88 @@ def gaussian_bumps_separable(Xx, Xy, Xz, seed=0, n=16, width=0.05, device=None):
         yz = gz[:, None, :, None] * gy[None, :, None, :]
         out += yz[:, :, None, :, :, None] * gx[None, None, :, None, None, :]
     return out
+
+
+# ---------------------------------------------------------------------------
+# The oil problem's pointwise data (problems/oil/input_data.F90).  The
+# reference draws its curves with Fortran random_number and reads the pump and
+# drain positions from the command line; here both come from seeded numpy
+# generators.  The functions restate falloff/lerp/bump3d (src/math.F90:44-88,
+# 173-181), dist_from_segment/dist_from_curves (input_data.F90:166-237),
+# pumping/draining (:241-283), kq (:286-294) and initial_state (:307-318).
+# ---------------------------------------------------------------------------
+OIL_RADIUS = 0.15
+OIL_KQMIN, OIL_KQMAX = 1.0, 1000.0
+
+
+def _falloff(r, R, t):
+    h = (t - r) / (R - r)
+    v = ((h - 1.0) * (h + 1.0)) ** 2
+    return np.where(t < r, 1.0, np.where(t > R, 0.0, v))
+
+
+def _lerp(t, x, y):
+    return (1.0 - t) * x + t * y
+
+
+def oil_curves(seed=0, cN=30, cL=16, step=0.05):
+    """The cN random-walk curves of cL points each (InitInputData,
+    input_data.F90:137-163): a random start and direction, then cL - 1 steps
+    whose direction is nudged by a random acceleration.  Shape (cN, cL, 3)."""
+    rng = np.random.default_rng(seed)
+    c = np.zeros((cN, cL, 3))
+    for i in range(cN):
+        c[i, 0] = rng.random(3)
+        dx = rng.random(3)
+        for j in range(1, cL):
+            rng.random(3)  # the reference draws t here and does not use it
+            ddx = rng.random(3)
+            ddx = 2.0 * (ddx - 0.5) - 0.4 * dx * np.sum(dx ** 2)
+            dx = dx + 0.4 * ddx
+            c[i, j] = c[i, j - 1] + step * dx
+    return c
+
+
+def oil_wells(seed=0, npumps=2, ndrains=2):
+    """Pump and drain positions (InitPumps reads them from the command line)."""
+    rng = np.random.default_rng(seed + 1)
+    return rng.uniform(0.2, 0.8, (npumps, 3)), rng.uniform(0.2, 0.8, (ndrains, 3))
+
+
+def _dist2_from_curves(P, curves, chunk=4096):
+    """Squared distance of each point of P (M, 3) to the nearest curve segment,
+    starting from 1e3 as the reference does."""
+    a = curves[:, :-1].reshape(-1, 3)
+    b = curves[:, 1:].reshape(-1, 3)
+    d = b - a
+    len2 = np.sum(d * d, axis=1)
+    out = np.empty(P.shape[0])
+    for s in range(0, P.shape[0], chunk):
+        p = P[s:s + chunk, None, :]
+        c = p - a[None]
+        proj = np.sum(c * d[None], axis=2) / len2[None]
+        near = np.where((proj < 0.0)[..., None], a[None],
+                        np.where((proj > 1.0)[..., None], b[None], a[None] + proj[..., None] * d[None]))
+        out[s:s + chunk] = np.minimum(1e3, np.min(np.sum((p - near) ** 2, axis=2), axis=1))
+    return out
+
+
+def oil_fields(x, y, z, seed=0, npumps=2, ndrains=2):
+    """Kq, pumping, the draining weight w (draining(u, X) = w u) and the
+    initial state at the points (x, y, z); arrays of the points' shape."""
+    shape = np.broadcast(x, y, z).shape
+    P = np.stack([np.broadcast_to(v, shape).ravel() for v in (x, y, z)], axis=1)
+    curves = oil_curves(seed)
+    pumps, drains = oil_wells(seed, npumps, ndrains)
+    dist = np.sqrt(_dist2_from_curves(P, curves))
+    kq = _lerp(_falloff(0.0, 0.06, dist), OIL_KQMIN, OIL_KQMAX)
+    pump = np.zeros(P.shape[0])
+    for i in range(npumps):
+        pump += _falloff(0.0, OIL_RADIUS, np.linalg.norm(pumps[i][None] - P, axis=1))
+    drain = np.zeros(P.shape[0])
+    for i in range(ndrains):
+        drain += _falloff(0.0, OIL_RADIUS, np.linalg.norm(drains[i][None] - P, axis=1))
+    bump = _falloff(0.2 / 2.0, 0.6 / 2.0, np.linalg.norm(P - 0.5, axis=1))
+    init = 0.1 * _lerp(_falloff(0.0, 0.1, dist), 0.0, 1.0) * bump
+    return {k: np.ascontiguousarray(v.reshape(shape)) for k, v in
+            (("kq", kq), ("pump", pump), ("drain", drain), ("init", init))}

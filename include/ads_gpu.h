@@ -20,6 +20,8 @@
  *   ads_solve           the Kronecker solve of Sub_Step             src/ADS.F90:518-779
  *   ads_reorder         ReorderRHSForY / ForZ / ForX                src/reorderRHS.F90:7-93
  *   ads_apply_mass      (Mx (x) My (x) Mz) u with MKBBT's mass band  src/projection_engine.F90:63-132
+ *   ads_set_oil         the oil problem's pointwise data and mi      problems/oil/input_data.F90:6-20,265-303
+ *   ads_get_drained     the `drained` statistic (ComputeResults)     problems/oil/input_data.F90:83-99
  *   ads_heat_adjoint    new: hand-written adjoint of the explicit heat step
  *
  * Layouts.  Coefficient vectors are x-fastest, u[x + Nx*(y + Ny*z)], which is
@@ -66,6 +68,8 @@ extern "C" {
 /* integrand forms (replace the RHS_fun callback) */
 #define ADS_FORM_PROJECT 0  /* J W v f: L2Projection, heat at t = 0 */
 #define ADS_FORM_HEAT 1     /* J W (v u + dt (-kappa grad u . grad v + v f)): heat at t > 0 */
+#define ADS_FORM_OIL 2      /* J W (v u + dt (-Kq exp(mu u) grad u . grad v + v (pump - max(0, w u)))):
+                               the oil problem at t > 0, problems/oil/RHS_eq.F90:69-92 */
 
 /* 3-D permutations of ReorderRHSFor{Y,Z,X} */
 #define ADS_REORDER_FOR_Y 0 /* F(x, y+z*Ny) -> F2(y, x+z*Nx) */
@@ -109,10 +113,22 @@ int ads_axis_tables(const ads_handle* h, int axis, double* U, int* O, double* J,
                     double* NN);
 
 /* Select the integrand.  f_qp: projection target (PROJECT) or source term
- * (HEAT, may be NULL = 0).  kappa_qp: per-point conductivity (HEAT, may be
- * NULL, then kappa is used).  Arrays are copied; the caller keeps ownership. */
+ * (HEAT, may be NULL = 0) or pumping(X) (OIL, required).  kappa_qp:
+ * per-point conductivity (HEAT, may be NULL, then kappa is used) or Kq(X)
+ * (OIL, required: the Kqvals cache of problems/oil/input_data.F90:333-395).
+ * Arrays are copied; the caller keeps ownership. */
 int ads_set_form(ads_handle* h, int form, const double* f_qp, const double* kappa_qp,
                  double kappa, double dt);
+/* The rest of the oil problem's pointwise data (problems/oil/input_data.F90):
+ * drain_qp = the draining weight w(X) with draining(u, X) = w(X) u (:265-283),
+ * mu = the exponent of bq = exp(mu u) (:297-303; mi = 10 there).  Needed
+ * before stepping with ADS_FORM_OIL; resets the drained total. */
+int ads_set_oil(ads_handle* h, const double* drain_qp, double mu);
+/* The oil problem's `drained` statistic (problems/oil/RHS_eq.F90:87, printed
+ * by ComputeResults, problems/oil/input_data.F90:83-99): the sum over the
+ * steps since ads_set_oil of J W v dt max(0, w u) over points and test
+ * functions. */
+int ads_get_drained(const ads_handle* h, double* drained);
 
 /* Coefficient state (host buffers, x-fastest). */
 int ads_set_coeffs(ads_handle* h, const double* u);

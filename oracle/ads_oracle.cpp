@@ -383,6 +383,7 @@ struct OrcADS {
   // band factors cached per axis for the current matrix mix
   int last_info = 0;
   int pivoted[3] = {0, 0, 0};
+  double drained = 0.0;  // oil problem: sum of J W v Dt vdrain of the last assembly
 };
 
 // Index of Un(ex,ey,ez,kx,ky,kz) in the Fortran column-major layout (0-based).
@@ -507,7 +508,7 @@ static void orc_form_un(OrcADS& A) {
 }
 
 // Problem integrands (the RHS_fun_int callback, src/Interfaces.F90:52-81).
-enum { ORC_FORM_PROJECT = 0, ORC_FORM_HEAT = 1 };
+enum { ORC_FORM_PROJECT = 0, ORC_FORM_HEAT = 1, ORC_FORM_OIL = 2 };
 
 struct OrcFormCtx {
   int form;
@@ -516,6 +517,8 @@ struct OrcFormCtx {
   double kappa_const;
   double dt;
   int heat_initial;      // project the heat problem's own initial_state(X)
+  const double* drain;   // oil: draining weight per point, draining(u, X) = drain * u
+  double mu;             // oil: exponent of the saturation factor exp(mu u)
 };
 
 struct OrcPoint {
@@ -528,12 +531,14 @@ struct OrcPoint {
   size_t qp;  // linear (kx,ky,kz,ex,ey,ez) index
 };
 
-typedef void (*orc_rhs_fun)(const OrcFormCtx*, const OrcPoint*, double* l2norm, double* ret);
+// extra: a per-call statistic the problem accumulates (the oil problem's
+// `drained` module variable); 0 for the other problems
+typedef void (*orc_rhs_fun)(const OrcFormCtx*, const OrcPoint*, double* l2norm, double* ret, double* extra);
 
 // L2Projection / heat t=0 integrand:
 // problems/L2Projection/RHS_eq.F90:66-70 and problems/heat/RHS_eq.F90:82-85.
 __attribute__((noinline)) static void orc_rhs_project(const OrcFormCtx* c, const OrcPoint* P,
-                                                      double* l2norm, double* ret) {
+                                                      double* l2norm, double* ret, double* extra) {
   const OrcADS& A = *P->A;
   const double v = A.ax[0].nn(0, P->a[0], P->k[0], P->e[0]) *
                    A.ax[1].nn(0, P->a[1], P->k[1], P->e[1]) *
@@ -544,11 +549,12 @@ __attribute__((noinline)) static void orc_rhs_project(const OrcFormCtx* c, const
   else fval = 1.0;
   *ret = P->J * P->W * v * fval;
   *l2norm = P->J * P->W * v * fval * fval;
+  *extra = 0.0;
 }
 
 // Heat t>0 integrand: problems/heat/RHS_eq.F90:69-81 (kqval = kappa, fval = f).
 __attribute__((noinline)) static void orc_rhs_heat(const OrcFormCtx* c, const OrcPoint* P,
-                                                   double* l2norm, double* ret) {
+                                                   double* l2norm, double* ret, double* extra) {
   const OrcADS& A = *P->A;
   const OrcAxis &X = A.ax[0], &Y = A.ax[1], &Z = A.ax[2];
   const int *a = P->a, *k = P->k, *e = P->e;
@@ -560,6 +566,33 @@ __attribute__((noinline)) static void orc_rhs_heat(const OrcFormCtx* c, const Or
   const double fval = c->fqp ? c->fqp[P->qp] : 0.0;
   const double rhs = c->dt * (-kqval * (P->du[0] * dvx + P->du[1] * dvy + P->du[2] * dvz) + v * fval);
   *ret = P->J * P->W * (v * P->un + rhs);
+  *l2norm = P->J * P->W * v * P->un * P->un;
+  *extra = 0.0;
+}
+
+// Oil problem t>0 integrand: problems/oil/RHS_eq.F90:69-92.  The pointwise
+// inputs are sampled by the host at the quadrature points: kqval = Kqvals
+// (input_data.F90:333-336 through CacheKqValues), vpump = pumping(X)
+// (:241-259), and the draining weight w(X) with draining(u, X) = w(X) u
+// (:265-283); bq = exp(mi u) (:297-303).  extra receives the `drained`
+// increment J W v Dt vdrain.
+__attribute__((noinline)) static void orc_rhs_oil(const OrcFormCtx* c, const OrcPoint* P,
+                                                  double* l2norm, double* ret, double* extra) {
+  const OrcADS& A = *P->A;
+  const OrcAxis &X = A.ax[0], &Y = A.ax[1], &Z = A.ax[2];
+  const int *a = P->a, *k = P->k, *e = P->e;
+  const double v = X.nn(0, a[0], k[0], e[0]) * Y.nn(0, a[1], k[1], e[1]) * Z.nn(0, a[2], k[2], e[2]);
+  const double dvx = X.nn(1, a[0], k[0], e[0]) * Y.nn(0, a[1], k[1], e[1]) * Z.nn(0, a[2], k[2], e[2]);
+  const double dvy = X.nn(0, a[0], k[0], e[0]) * Y.nn(1, a[1], k[1], e[1]) * Z.nn(0, a[2], k[2], e[2]);
+  const double dvz = X.nn(0, a[0], k[0], e[0]) * Y.nn(0, a[1], k[1], e[1]) * Z.nn(1, a[2], k[2], e[2]);
+  const double kqval = c->kappa ? c->kappa[P->qp] : c->kappa_const;
+  const double vpump = c->fqp ? c->fqp[P->qp] : 0.0;
+  const double vdrain = std::max(0.0, (c->drain ? c->drain[P->qp] : 0.0) * P->un);
+  const double fval = vpump - vdrain;
+  const double rhs =
+      c->dt * (-kqval * std::exp(c->mu * P->un) * (P->du[0] * dvx + P->du[1] * dvy + P->du[2] * dvz) + v * fval);
+  *ret = P->J * P->W * (v * P->un + rhs);
+  *extra = P->J * P->W * v * c->dt * vdrain;
   *l2norm = P->J * P->W * v * P->un * P->un;
 }
 
@@ -573,14 +606,14 @@ static double orc_form_3d_rhs(OrcADS& A, const OrcFormCtx* ctx, orc_rhs_fun fun)
   const int E1 = X.nelem, E2 = Y.nelem, E3 = Z.nelem;
   const size_t nqp = A.nqp;
   const size_t sx = A.s[0], sy = A.s[1];
-  double l2total = 0.0;
+  double l2total = 0.0, extotal = 0.0;
   const int c1 = X.p + 1, c2 = Y.p + 1, c3 = Z.p + 1;
   for (int colour = 0; colour < c1 * c2 * c3; ++colour) {
     const int ox = colour % c1, oy = (colour / c1) % c2, oz = colour / (c1 * c2);
     const int n1 = (E1 - ox + c1 - 1) / c1, n2 = (E2 - oy + c2 - 1) / c2, n3 = (E3 - oz + c3 - 1) / c3;
     const long total = (long)std::max(n1, 0) * std::max(n2, 0) * std::max(n3, 0);
-    double l2colour = 0.0;
-#pragma omp parallel reduction(+ : l2colour)
+    double l2colour = 0.0, excolour = 0.0;
+#pragma omp parallel reduction(+ : l2colour, excolour)
     {
     std::vector<double> elarr((size_t)c1 * c2 * c3, 0.0);
 #pragma omp for schedule(static)
@@ -593,7 +626,7 @@ static double orc_form_3d_rhs(OrcADS& A, const OrcFormCtx* ctx, orc_rhs_fun fun)
       P.A = &A;
       P.e[0] = ex; P.e[1] = ey; P.e[2] = ez;
       P.J = X.J[ex] * Y.J[ey] * Z.J[ez];
-      double l2el = 0.0;
+      double l2el = 0.0, exel = 0.0;
       for (int kx = 0; kx < X.ng; ++kx)
         for (int ky = 0; ky < Y.ng; ++ky)
           for (int kz = 0; kz < Z.ng; ++kz) {
@@ -610,10 +643,11 @@ static double orc_form_3d_rhs(OrcADS& A, const OrcFormCtx* ctx, orc_rhs_fun fun)
               for (int ay = 0; ay <= Y.p; ++ay)
                 for (int az = 0; az <= Z.p; ++az) {
                   P.a[0] = ax_; P.a[1] = ay; P.a[2] = az;
-                  double l2tmp, res;
-                  fun(ctx, &P, &l2tmp, &res);
+                  double l2tmp, res, extmp;
+                  fun(ctx, &P, &l2tmp, &res, &extmp);
                   elarr[ax_ + c1 * (ay + c2 * az)] += res;
                   l2el = l2el + l2tmp;
+                  exel = exel + extmp;
                 }
           }
       for (int ax_ = 0; ax_ <= X.p; ++ax_)
@@ -623,10 +657,13 @@ static double orc_form_3d_rhs(OrcADS& A, const OrcFormCtx* ctx, orc_rhs_fun fun)
             A.F[ix + sx * (iy + sy * iz)] += elarr[ax_ + c1 * (ay + c2 * az)];
           }
       l2colour += l2el;
+      excolour += exel;
     }
     }
     l2total += l2colour;
+    extotal += excolour;
   }
+  A.drained = extotal;
   return l2total;
 }
 
@@ -746,7 +783,7 @@ ORC_API int orc_step(OrcADS* A, int form, const double* fqp, const double* kappa
   std::fill(A->Un13.begin(), A->Un13.end(), 0.0);
   std::fill(A->Un23.begin(), A->Un23.end(), 0.0);
   orc_form_un(*A);
-  OrcFormCtx ctx{form, fqp, kappa_qp, kappa, dt, heat_initial};
+  OrcFormCtx ctx{form, fqp, kappa_qp, kappa, dt, heat_initial, nullptr, 0.0};
   orc_rhs_fun fun = (form == ORC_FORM_HEAT) ? orc_rhs_heat : orc_rhs_project;
   const double l2 = orc_form_3d_rhs(*A, &ctx, fun);
   if (l2norm) *l2norm = l2;
@@ -758,9 +795,36 @@ ORC_API int orc_step(OrcADS* A, int form, const double* fqp, const double* kappa
 ORC_API double orc_assemble(OrcADS* A, int form, const double* fqp, const double* kappa_qp,
                             double kappa, double dt, int heat_initial) {
   orc_form_un(*A);
-  OrcFormCtx ctx{form, fqp, kappa_qp, kappa, dt, heat_initial};
+  OrcFormCtx ctx{form, fqp, kappa_qp, kappa, dt, heat_initial, nullptr, 0.0};
   orc_rhs_fun fun = (form == ORC_FORM_HEAT) ? orc_rhs_heat : orc_rhs_project;
   return orc_form_3d_rhs(*A, &ctx, fun);
+}
+
+// One oil-problem step at t > 0 (problems/oil/main.F90 driving Step with the
+// oil ComputePointForRHS): pump_qp, kq_qp, drain_qp per quadrature point in
+// the (kx,ky,kz,ex,ey,ez) layout.  Writes the step's l2norm and its drained
+// increment.
+ORC_API int orc_step_oil(OrcADS* A, const double* pump_qp, const double* kq_qp, const double* drain_qp,
+                         double mu, double dt, double* l2norm, double* drained) {
+  std::fill(A->Un13.begin(), A->Un13.end(), 0.0);
+  std::fill(A->Un23.begin(), A->Un23.end(), 0.0);
+  orc_form_un(*A);
+  OrcFormCtx ctx{ORC_FORM_OIL, pump_qp, kq_qp, 1.0, dt, 0, drain_qp, mu};
+  const double l2 = orc_form_3d_rhs(*A, &ctx, orc_rhs_oil);
+  if (l2norm) *l2norm = l2;
+  if (drained) *drained = A->drained;
+  const double mix[4] = {1.0, 0.0, 0.0, 0.0};
+  return orc_kron_solve(*A, mix);
+}
+
+// Only the oil assembly, leaving F in place; returns the l2norm, writes drained.
+ORC_API double orc_assemble_oil(OrcADS* A, const double* pump_qp, const double* kq_qp, const double* drain_qp,
+                                double mu, double dt, double* drained) {
+  orc_form_un(*A);
+  OrcFormCtx ctx{ORC_FORM_OIL, pump_qp, kq_qp, 1.0, dt, 0, drain_qp, mu};
+  const double l2 = orc_form_3d_rhs(*A, &ctx, orc_rhs_oil);
+  if (drained) *drained = A->drained;
+  return l2;
 }
 
 // Only the Kronecker solve of F (mix = (1,0,0,0)); result in R and F.

@@ -16,6 +16,7 @@ _lib = None
 
 FORM_PROJECT = 0
 FORM_HEAT = 1
+FORM_OIL = 2
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -59,6 +60,10 @@ def lib():
         L.orc_assemble.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_int]
         L.orc_assemble.restype = ctypes.c_double
+        L.orc_step_oil.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, _dp, _dp]
+        L.orc_step_oil.restype = ctypes.c_int
+        L.orc_assemble_oil.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, _dp]
+        L.orc_assemble_oil.restype = ctypes.c_double
         L.orc_solve_F.argtypes = [ctypes.c_void_p, _dp]
         L.orc_solve_F.restype = ctypes.c_int
         L.orc_pivoted.argtypes = [ctypes.c_void_p, _ip]
@@ -192,6 +197,23 @@ class Oracle:
         kq = None if kappa_qp is None else np.ascontiguousarray(kappa_qp, dtype=np.float64).ravel()
         l2 = lib().orc_assemble(self.h, form, _p(fqp), _p(kq), kappa, dt, int(heat_initial))
         return self.F(), l2
+
+    def step_oil(self, pump_qp, kq_qp, drain_qp, mu, dt):
+        """One oil-problem step (problems/oil/RHS_eq.F90:69-92); returns (l2norm, drained)."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (pump_qp, kq_qp, drain_qp)]
+        l2, dr = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        info = lib().orc_step_oil(self.h, _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), mu, dt, ctypes.byref(l2),
+                                  ctypes.byref(dr))
+        if info:
+            raise RuntimeError(f"oracle step failed: info={info}")
+        return l2.value, dr.value
+
+    def assemble_oil(self, pump_qp, kq_qp, drain_qp, mu, dt):
+        """The oil assembly only; returns (F, l2norm, drained)."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (pump_qp, kq_qp, drain_qp)]
+        dr = ctypes.c_double(0.0)
+        l2 = lib().orc_assemble_oil(self.h, _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), mu, dt, ctypes.byref(dr))
+        return self.F(), l2, dr.value
 
     def solve(self, F):
         F = np.ascontiguousarray(F, dtype=np.float64).ravel().copy()
