@@ -18,7 +18,7 @@ module ads_gpu
 
    integer(c_int), parameter :: ADS_OK = 0
    integer(c_int), parameter :: ADS_PREC_FP64 = 0, ADS_PREC_MIXED = 1
-   integer(c_int), parameter :: ADS_FORM_PROJECT = 0, ADS_FORM_HEAT = 1
+   integer(c_int), parameter :: ADS_FORM_PROJECT = 0, ADS_FORM_HEAT = 1, ADS_FORM_OIL = 2
 
    type, bind(c) :: ads_opts
       integer(c_int) :: precision
@@ -64,6 +64,17 @@ module ads_gpu
          integer(c_int), value :: form
          type(c_ptr), value :: f_qp, kappa_qp
          real(c_double), value :: kappa, dt
+      end function
+      integer(c_int) function ads_set_oil(h, drain_qp, mu) bind(c, name="ads_set_oil")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         real(c_double), intent(in) :: drain_qp(*)
+         real(c_double), value :: mu
+      end function
+      integer(c_int) function ads_get_drained(h, drained) bind(c, name="ads_get_drained")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         real(c_double), intent(out) :: drained
       end function
       integer(c_int) function ads_set_coeffs(h, u) bind(c, name="ads_set_coeffs")
          import :: c_int, c_ptr, c_double
@@ -121,6 +132,25 @@ contains
       if (present(kqp)) pk = c_loc(kqp)
       mierr = ads_set_form(g % h, form, pf, pk, kappa, dt)
    end subroutine GpuSetForm
+
+   ! The oil problem's draining weight at the points (draining(u, X) = w u,
+   ! problems/oil/input_data.F90:265-283) and mi; pumping and Kqvals go to
+   ! GpuSetForm(g, ADS_FORM_OIL, pump_qp, kq_qp, 1d0, Dt, mierr).
+   subroutine GpuSetOil(g, drain_qp, mi, mierr)
+      type(ads_gpu_handle), intent(in) :: g
+      real(c_double), intent(in) :: drain_qp(:)
+      real(c_double), intent(in) :: mi
+      integer(kind=4), intent(out) :: mierr
+      mierr = ads_set_oil(g % h, drain_qp, mi)
+   end subroutine GpuSetOil
+
+   ! The drained total since GpuSetOil (what ComputeResults reduces and prints).
+   subroutine GpuDrained(g, drained, mierr)
+      type(ads_gpu_handle), intent(in) :: g
+      real(c_double), intent(out) :: drained
+      integer(kind=4), intent(out) :: mierr
+      mierr = ads_get_drained(g % h, drained)
+   end subroutine GpuDrained
 
    ! Step (src/ADS.F90:437); F receives the solution (ads_data % F after Step).
    subroutine GpuStep(iter, g, F, l2norm, mierr)

@@ -216,13 +216,50 @@ def _dist2_from_curves(P, curves, chunk=4096):
     return out
 
 
-def oil_fields(x, y, z, seed=0, npumps=2, ndrains=2):
-    """Kq, pumping, the draining weight w (draining(u, X) = w u) and the
-    initial state at the points (x, y, z); arrays of the points' shape."""
+def _oil_fields_torch(x, y, z, curves, pumps, drains, device, chunk=1 << 17):
+    """oil_fields on a torch device, the same formulas in FP64."""
+    import torch
+
+    def t(v):
+        return torch.as_tensor(np.ascontiguousarray(v), dtype=torch.float64, device=device)
+
+    def falloff(r, R, d):
+        h = (d - r) / (R - r)
+        v = ((h - 1.0) * (h + 1.0)) ** 2
+        return torch.where(d < r, torch.ones_like(d), torch.where(d > R, torch.zeros_like(d), v))
+
     shape = np.broadcast(x, y, z).shape
-    P = np.stack([np.broadcast_to(v, shape).ravel() for v in (x, y, z)], axis=1)
+    P = torch.stack([t(np.broadcast_to(v, shape)).reshape(-1) for v in (x, y, z)], dim=1)
+    a, b = t(curves[:, :-1].reshape(-1, 3)), t(curves[:, 1:].reshape(-1, 3))
+    d = b - a
+    len2 = (d * d).sum(dim=1)
+    d2 = torch.empty(P.shape[0], dtype=torch.float64, device=device)
+    for s in range(0, P.shape[0], chunk):
+        p = P[s:s + chunk, None, :]
+        proj = ((p - a[None]) * d[None]).sum(dim=2) / len2[None]
+        near = torch.where((proj < 0.0)[..., None], a[None],
+                           torch.where((proj > 1.0)[..., None], b[None], a[None] + proj[..., None] * d[None]))
+        d2[s:s + chunk] = torch.clamp(((p - near) ** 2).sum(dim=2).min(dim=1).values, max=1e3)
+    dist = torch.sqrt(d2)
+    kq = (1.0 - falloff(0.0, 0.06, dist)) * OIL_KQMIN + falloff(0.0, 0.06, dist) * OIL_KQMAX
+    pump = sum(falloff(0.0, OIL_RADIUS, torch.linalg.norm(t(w)[None] - P, dim=1)) for w in pumps)
+    drain = sum(falloff(0.0, OIL_RADIUS, torch.linalg.norm(t(w)[None] - P, dim=1)) for w in drains)
+    bump = falloff(0.2 / 2.0, 0.6 / 2.0, torch.linalg.norm(P - 0.5, dim=1))
+    init = 0.1 * falloff(0.0, 0.1, dist) * bump
+    return {k: v.reshape(shape).cpu().numpy() for k, v in
+            (("kq", kq), ("pump", pump), ("drain", drain), ("init", init))}
+
+
+def oil_fields(x, y, z, seed=0, npumps=2, ndrains=2, device=None):
+    """Kq, pumping, the draining weight w (draining(u, X) = w u) and the
+    initial state at the points (x, y, z); arrays of the points' shape.  Uses
+    torch on `device` when given (large grids), numpy otherwise."""
+    shape = np.broadcast(x, y, z).shape
     curves = oil_curves(seed)
     pumps, drains = oil_wells(seed, npumps, ndrains)
+    if device is not None:
+        return _oil_fields_torch(x, y, z, curves, pumps, drains, device)
+    P = np.stack([np.broadcast_to(v, shape).ravel() for v in (x, y, z)], axis=1)
     dist = np.sqrt(_dist2_from_curves(P, curves))
     kq = _lerp(_falloff(0.0, 0.06, dist), OIL_KQMIN, OIL_KQMAX)
     pump = np.zeros(P.shape[0])

@@ -304,7 +304,8 @@ def aux_runs(args, dev):
     g a seeded Gaussian random field, 100 steps, mixed forward + FP64
     adjoint against an all-FP64 reference gradient), and the mixed step
     against FP64 at 256^3 p = 3 plus the per-step error of the mixed path
-    over the first steps at 256^3 p = 2."""
+    over the first steps at 256^3 p = 2, and the oil problem at 128^3
+    (mixed against FP64, with its drained statistic)."""
     import numpy as np
     import torch
     import ads_mpi_gb300 as A
@@ -406,6 +407,40 @@ def aux_runs(args, dev):
                   "against an all-FP64 reference gradient",
         "kappa_max": float(kappa.max()), "dt_lambda_max_at_configured_dt": dtv * lam,
         "configured_dt": kappa_check(dtv), "stable_dt": kappa_check(dt_stable)}
+
+    # ---- oil problem (problems/oil/RHS_eq.F90:69-92), 128^3 p=2: mixed vs FP64 ----
+    # seeded curves (Kq), pumps and drains; mi = 10; dt at half the explicit
+    # limit for the largest Kq exp(mi u) (u stays below 0.1)
+    E, p, Ko, mu = 128, 2, 10, 10.0
+    n = (E + p - 1,) * 3
+    g64 = A.ADS(n, (p, p, p), precision=A.PREC_FP64, device=dev)
+    gmx = A.ADS(n, (p, p, p), precision=A.PREC_MIXED, refine_tol=1e-10, max_refine=3, device=dev)
+    x, y, z = g64.qp_coords()
+    of = inputs.oil_fields(x, y, z, seed=args.seed, device=f"cuda:{dev}")
+    del x, y, z
+    lam = 3 * 21.6 * E * E * float(of["kq"].max()) * float(np.exp(mu * 0.1))
+    dto = float(f"{0.5 / lam:.0e}")
+    row = {"dt": dto, "mu": mu, "steps": Ko}
+    res = {}
+    for name, gg in (("fp64", g64), ("mixed", gmx)):
+        gg.set_form(A.FORM_PROJECT, f_qp=of["init"])
+        gg.step()
+        gg.set_form(A.FORM_OIL, f_qp=of["pump"], kappa_qp=of["kq"], dt=dto)
+        gg.set_oil(of["drain"], mu=mu)
+        gg.steps(2)
+        secs = time_device_steps(torch, gg, Ko)
+        row[name] = gg.N * Ko / secs
+        res[name] = (gg.coeffs(), gg.drained())
+    a64 = res["fp64"][0]
+    row["mixed_rel_err_vs_fp64"] = float(np.linalg.norm(res["mixed"][0] - a64) / np.linalg.norm(a64))
+    row["drained_fp64"], row["drained_mixed"] = res["fp64"][1], res["mixed"][1]
+    row["mixed_rel_residual"] = gmx.stats()["rel_residual"]
+    out["oil_128p2"] = {"config": "oil problem 128^3 p=2: Kq from 30 seeded curves (Kq in [1, 1000]), 2 pumps, "
+                                  "2 drains, mi = 10, projection of the initial state then 2 + 10 steps",
+                        "unit": UNIT, **row, "mixed_over_fp64": row["mixed"] / row["fp64"]}
+    del of
+    gmx.cleanup()
+    g64.cleanup()
 
     # ---- 256^3 p=3: mixed vs FP64 step time ----
     # initial coefficients: the seeded bumps at the Greville abscissae (a

@@ -100,6 +100,11 @@ def test_oil_inputs_are_seeded_and_in_range():
     assert a["kq"].min() >= inputs.OIL_KQMIN and a["kq"].max() <= inputs.OIL_KQMAX
     assert a["pump"].min() >= 0.0 and a["drain"].min() >= 0.0
     assert 0.0 <= a["init"].min() and a["init"].max() <= 0.1
+    # the torch path (used for large grids) evaluates the same formulas
+    pytest.importorskip("torch")
+    c = inputs.oil_fields(pts[:, 0], pts[:, 1], pts[:, 2], seed=7, device="cpu")
+    for k in a:
+        assert np.allclose(c[k], a[k], rtol=1e-12, atol=1e-12)
     # the curves follow the reference's random walk: consecutive points 0.05 |dx| apart
     c = inputs.oil_curves(7)
     assert c.shape == (30, 16, 3)
