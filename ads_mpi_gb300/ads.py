@@ -58,6 +58,8 @@ ABI = [
     ("ads_set_form", [ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_double], ctypes.c_int),
     ("ads_set_oil", [ctypes.c_void_p, _dp, ctypes.c_double], ctypes.c_int),
     ("ads_get_drained", [ctypes.c_void_p, _dp], ctypes.c_int),
+    ("ads_save_spline_plot", [ctypes.c_void_p, ctypes.c_char_p, _dp, _ip, _dp], ctypes.c_int),
+    ("ads_write_vti", [ctypes.c_char_p, _ip, _dp], ctypes.c_int),
     ("ads_set_coeffs", [ctypes.c_void_p, _dp], ctypes.c_int),
     ("ads_get_coeffs", [ctypes.c_void_p, _dp], ctypes.c_int),
     ("ads_step", [ctypes.c_void_p, _dp], ctypes.c_int),
@@ -82,6 +84,15 @@ ABI = [
     ("ads_launch_count", [ctypes.c_void_p], ctypes.c_longlong),
     ("ads_launch_count_reset", [ctypes.c_void_p], ctypes.c_int),
 ]
+
+
+def write_vti(name, vals):
+    """VtkOutput (src/vtk.F90:15-77): vals shaped (resz, resy, resx) into name.vti."""
+    v = np.ascontiguousarray(vals, dtype=np.float64)
+    res = np.array([v.shape[2], v.shape[1], v.shape[0]], dtype=np.int32)
+    st = load().ads_write_vti(os.fsencode(name), res.ctypes.data_as(_ip), v.ctypes.data_as(_dp))
+    if st != 0:
+        raise ADSError(st, f"cannot write {name}.vti")
 
 
 def lib_path():
@@ -249,6 +260,22 @@ class ADS:
         if w.size != self.nqp:
             raise ValueError(f"per-point array must have {self.nqp} entries")
         self._check(self._L.ads_set_oil(self.h, _ptr(w), float(mu)))
+
+    def save_spline_plot(self, name=None, rng=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), res=(31, 31, 31)):
+        """SaveSplinePlot (src/plot.F90:111-140) of the current coefficients:
+        the spline at an res grid over rng, returned shaped (resz, resy, resx)
+        and, with a name, written to name.vti as VtkOutput does."""
+        r = np.ascontiguousarray(rng, dtype=np.float64)
+        rs = np.ascontiguousarray(res, dtype=np.int32)
+        vals = np.zeros(int(np.prod(res)))
+        nm = None if name is None else os.fsencode(name)
+        self._check(self._L.ads_save_spline_plot(self.h, nm, _ptr(r), rs.ctypes.data_as(_ip), _ptr(vals)))
+        return vals.reshape(res[2], res[1], res[0])
+
+    # reference name: PrintSolution (src/ADS.F90:955-989)
+    def print_solution(self, iter, directory="."):
+        """The solution sampled on 31^3 points of [0,1]^3 into <directory>/step<iter>.vti."""
+        return self.save_spline_plot(os.path.join(directory, f"step{iter}"))
 
     def drained(self):
         """The oil problem's drained total since set_oil (ComputeResults)."""

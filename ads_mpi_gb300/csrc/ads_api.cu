@@ -889,6 +889,94 @@ int ads_set_oil(ads_handle* h, const double* drain_qp, double mu) {
   return ADS_OK;
 }
 
+// One value as Fortran's F30.10 edit descriptor writes it, after adjustl and
+// trim (src/vtk.F90:57-58): fixed notation with 10 decimals, asterisks when it
+// does not fit in 30 characters, Infinity / NaN spelled out.
+static std::string f30_10(double v) {
+  if (std::isnan(v)) return "NaN";
+  if (std::isinf(v)) return v > 0 ? "Infinity" : "-Infinity";
+  char buf[512];
+  std::snprintf(buf, sizeof buf, "%.10f", v);
+  if (std::strlen(buf) > 30) return std::string(30, '*');
+  return buf;
+}
+
+int ads_write_vti(const char* name, const int res[3], const double* vals) {
+  if (!name || !res || !vals) return ADS_ERR_ARG;
+  for (int d = 0; d < 3; ++d)
+    if (res[d] < 1 || res[d] > 99999) return ADS_ERR_ARG;
+  const std::string path = std::string(name) + ".vti";
+  FILE* f = std::fopen(path.c_str(), "w");
+  if (!f) return ADS_ERR_ARG;
+  char extent[64];
+  std::snprintf(extent, sizeof extent, "0 %5d 0 %5d 0 %5d", res[0] - 1, res[1] - 1, res[2] - 1);
+  std::fprintf(f, "<?xml version=\"1.0\"?>\n");
+  std::fprintf(f, "<VTKFile type=\"ImageData\" version=\"0.1\">\n");
+  std::fprintf(f, "  <ImageData WholeExtent=\"%s\" origin=\"0 0 0\" spacing=\"1 1 1\">\n", extent);
+  std::fprintf(f, "    <Piece Extent=\"%s\">\n", extent);
+  std::fprintf(f, "      <PointData Scalars=\"Result\">\n");
+  std::fprintf(f, "        <DataArray Name=\"Result\" type=\"Float32\">\n");
+  const size_t n = (size_t)res[0] * res[1] * res[2];
+  for (size_t i = 0; i < n; ++i) std::fprintf(f, "          %s\n", f30_10(vals[i]).c_str());
+  std::fprintf(f, "        </DataArray>\n");
+  std::fprintf(f, "      </PointData>\n");
+  std::fprintf(f, "    </Piece>\n");
+  std::fprintf(f, "  </ImageData>\n");
+  std::fprintf(f, "</VTKFile>\n");
+  const bool ok = std::ferror(f) == 0;
+  std::fclose(f);
+  return ok ? ADS_OK : ADS_ERR_ARG;
+}
+
+int ads_save_spline_plot(ads_handle* h, const char* name, const double range[6], const int res[3], double* vals) {
+  if (!h || !range || !res) return ADS_ERR_ARG;
+  for (int d = 0; d < 3; ++d)
+    if (res[d] < 2 || res[d] > 4096) return fail(h, ADS_ERR_ARG, "plot resolution must be 2..4096 per axis");
+  for (int i = 0; i < 6; ++i)
+    if (!std::isfinite(range[i])) return fail(h, ADS_ERR_NONFINITE, "non-finite plot range");
+  const long long n = (long long)res[0] * res[1] * res[2];
+  if (n > (1ll << 28)) return fail(h, ADS_ERR_ARG, "plot grid too large (more than 2^28 samples)");
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  std::vector<double> tab;
+  std::vector<int> first;
+  for (int d = 0; d < 3; ++d) {
+    std::vector<double> B;
+    std::vector<int> F;
+    sample_basis(h->ax[d], range[2 * d], range[2 * d + 1], res[d], B, F);
+    tab.insert(tab.end(), B.begin(), B.end());
+    first.insert(first.end(), F.begin(), F.end());
+  }
+  std::vector<double> host;
+  double* out = vals;
+  if (!out) {
+    host.resize((size_t)n);
+    out = host.data();
+  }
+  double *d_tab = nullptr, *d_vals = nullptr;
+  int* d_first = nullptr;
+  int st = ADS_OK;
+  cudaError_t e = cudaMalloc((void**)&d_tab, sizeof(double) * tab.size());
+  if (e == cudaSuccess) e = cudaMalloc((void**)&d_first, sizeof(int) * first.size());
+  if (e == cudaSuccess) e = cudaMalloc((void**)&d_vals, sizeof(double) * (size_t)n);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) {
+    st = run_kernel(h, "eval_grid", 1, [&]() -> cudaError_t {
+      return launch_eval_grid(h->d_u, h->g, d_tab, d_first, res[0], res[1], res[2], d_vals, h->stream);
+    });
+  }
+  if (e == cudaSuccess && !st) e = cudaMemcpyAsync(out, d_vals, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess && !st) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess && !st) st = cuda_fail(h, e, "ads_save_spline_plot");
+  cudaFree(d_tab);
+  cudaFree(d_first);
+  cudaFree(d_vals);
+  if (st) return st;
+  if (name && ads_write_vti(name, res, out) != ADS_OK)
+    return fail(h, ADS_ERR_ARG, std::string("cannot write ") + name + ".vti");
+  return ADS_OK;
+}
+
 int ads_get_drained(const ads_handle* h, double* drained) {
   if (!h || !drained) return ADS_ERR_ARG;
   ads_handle* hm = const_cast<ads_handle*>(h);

@@ -225,6 +225,10 @@ cudaError_t launch_uscale(const double* u, long long n, double* part, int nparts
 // hist row of the step; adds the oil drained statistic to its running total
 cudaError_t launch_record(double* scal, int* flags, double* hist, int cap, cudaStream_t s);
 
+// the spline of the L0 coefficients u at an rx x ry x rz sample grid (x fastest);
+// tab/first: the per-axis sample tables of sample_basis, x then y then z
+cudaError_t launch_eval_grid(const double* u, const Geometry& g, const double* tab, const int* first, int rx,
+                             int ry, int rz, double* vals, cudaStream_t s);
 // packed coefficients (dense Nx) -> padded L0 (to_padded) or back
 cudaError_t launch_repack(const double* src, double* dst, const Geometry& g, bool to_padded, cudaStream_t s);
 // layout conversions between the per-point (kx,ky,kz,ex,ey,ez) layout and the

@@ -599,6 +599,52 @@ cudaError_t launch_record(double* scal, int* flags, double* hist, int cap, cudaS
 }
 
 // ---------------------------------------------------------------------------
+// SaveSplinePlot + EvalSpline (src/plot.F90:111-140, src/basis.F90:323-369):
+// the spline at a res_x x res_y x res_z grid, one thread per sample (x
+// fastest).  The host tabulates each axis's span and p+1 nonzero B-splines
+// per sample; the (p+1)^3 products are summed in the reference's order.
+// ---------------------------------------------------------------------------
+template <int P>
+__global__ void k_eval_grid(const double* __restrict__ u, Geometry g, const double* __restrict__ tab,
+                            const int* __restrict__ first, int rx, int ry, int rz, double* __restrict__ vals) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)rx * ry * rz;
+  if (idx >= n) return;
+  const int ix = (int)(idx % rx), iy = (int)((idx / rx) % ry), iz = (int)(idx / ((long long)rx * ry));
+  // tables: x samples, then y, then z
+  const double* bx = tab + (size_t)ix * (P + 1);
+  const double* by = tab + (size_t)(rx + iy) * (P + 1);
+  const double* bz = tab + (size_t)(rx + ry + iz) * (P + 1);
+  const int x0 = first[ix], y0 = first[rx + iy], z0 = first[rx + ry + iz];
+  const int Ny = g.N[1];
+  double val = 0.0;
+#pragma unroll
+  for (int a = 0; a <= P; ++a)
+#pragma unroll
+    for (int b = 0; b <= P; ++b)
+#pragma unroll
+      for (int c = 0; c <= P; ++c) {
+        const double w = bx[a] * by[b] * bz[c];
+        val = val + w * u[(size_t)(x0 + a) + (size_t)g.PX * ((size_t)(y0 + b) + (size_t)Ny * (z0 + c))];
+      }
+  vals[idx] = val;
+}
+
+cudaError_t launch_eval_grid(const double* u, const Geometry& g, const double* tab, const int* first, int rx,
+                             int ry, int rz, double* vals, cudaStream_t s) {
+  const long long n = (long long)rx * ry * rz;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  switch (g.P) {
+    case 1: k_eval_grid<1><<<blocks, 256, 0, s>>>(u, g, tab, first, rx, ry, rz, vals); break;
+    case 2: k_eval_grid<2><<<blocks, 256, 0, s>>>(u, g, tab, first, rx, ry, rz, vals); break;
+    case 3: k_eval_grid<3><<<blocks, 256, 0, s>>>(u, g, tab, first, rx, ry, rz, vals); break;
+    case 4: k_eval_grid<4><<<blocks, 256, 0, s>>>(u, g, tab, first, rx, ry, rz, vals); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // layout conversions
 // ---------------------------------------------------------------------------
 // packed coefficients (x fastest, dense Nx) <-> the padded L0 layout (pitch

@@ -91,6 +91,34 @@ static void nonzero_basis(const std::vector<double>& U, int i, int deg, double x
   }
 }
 
+int find_span(const AxisHost& a, double x) {
+  const int n = a.n, p = a.p;
+  const std::vector<double>& U = a.U;
+  if (x >= U[n + 1]) return n;
+  if (x <= U[p]) return p;
+  int low = p, high = n + 1;
+  int span = (low + high) / 2;
+  while (x < U[span] || x >= U[span + 1]) {
+    if (x < U[span]) high = span;
+    else low = span;
+    span = (low + high) / 2;
+  }
+  return span;
+}
+
+void sample_basis(const AxisHost& a, double t0, double t1, int res, std::vector<double>& B,
+                  std::vector<int>& first) {
+  B.assign((size_t)res * (a.p + 1), 0.0);
+  first.assign(res, 0);
+  for (int i = 0; i < res; ++i) {
+    const double t = i / (double)(res - 1);
+    const double x = (1.0 - t) * t0 + t * t1;  // lerp, src/math.F90:44-51
+    const int span = find_span(a, x);
+    nonzero_basis(a.U, span, a.p, x, &B[(size_t)i * (a.p + 1)]);
+    first[i] = span - a.p;
+  }
+}
+
 int axis_setup(int n, int p, AxisHost& a) {
   if (p < 1 || p > 4 || n < p) return 1;
   a.n = n; a.p = p; a.q = p + 1;

@@ -21,6 +21,12 @@ struct AxisHost {
 void open_knot(int n, int p, std::vector<double>& U);
 int gauss_legendre(int q, double* x, double* w);
 int axis_setup(int n, int p, AxisHost& a);
+// FindSpan (src/basis.F90:226-259): the knot span of x, clamped to [p, n]
+int find_span(const AxisHost& a, double x);
+// The p+1 nonzero B-splines at the res sample points lerp(i/(res-1), t0, t1)
+// of SaveSplinePlot (src/plot.F90:126-133): B[i*(p+1) + r] = N_{first[i]+r}(x_i)
+void sample_basis(const AxisHost& a, double t0, double t1, int res, std::vector<double>& B,
+                  std::vector<int>& first);
 // LU factors (see ads_internal.cuh) of the mass band; returns 1 on a zero pivot
 int band_factor(const AxisHost& a, std::vector<double>& fac, std::vector<double>& tfac);
 

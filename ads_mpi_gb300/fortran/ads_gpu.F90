@@ -76,6 +76,14 @@ module ads_gpu
          type(c_ptr), value :: h
          real(c_double), intent(out) :: drained
       end function
+      integer(c_int) function ads_save_spline_plot(h, name, range, res, vals) bind(c, name="ads_save_spline_plot")
+         import :: c_int, c_ptr, c_double, c_char
+         type(c_ptr), value :: h
+         character(kind=c_char), intent(in) :: name(*)
+         real(c_double), intent(in) :: range(6)
+         integer(c_int), intent(in) :: res(3)
+         type(c_ptr), value :: vals
+      end function
       integer(c_int) function ads_set_coeffs(h, u) bind(c, name="ads_set_coeffs")
          import :: c_int, c_ptr, c_double
          type(c_ptr), value :: h
@@ -151,6 +159,20 @@ contains
       integer(kind=4), intent(out) :: mierr
       mierr = ads_get_drained(g % h, drained)
    end subroutine GpuDrained
+
+   ! PrintSolution (src/ADS.F90:955-989): the solution on 31^3 points of
+   ! [0,1]^3 written to step<iter>.vti by the library's VtkOutput.
+   subroutine GpuPrintSolution(iter, g, mierr)
+      integer(kind=4), intent(in) :: iter
+      type(ads_gpu_handle), intent(in) :: g
+      integer(kind=4), intent(out) :: mierr
+      character(len=20) :: filename
+      real(c_double) :: range(6) = (/ 0d0, 1d0, 0d0, 1d0, 0d0, 1d0 /)
+      integer(c_int) :: res(3) = (/ 31, 31, 31 /)
+      write(filename, '(I10)') iter
+      filename = 'step' // adjustl(filename)
+      mierr = ads_save_spline_plot(g % h, trim(filename) // c_null_char, range, res, c_null_ptr)
+   end subroutine GpuPrintSolution
 
    ! Step (src/ADS.F90:437); F receives the solution (ads_data % F after Step).
    subroutine GpuStep(iter, g, F, l2norm, mierr)

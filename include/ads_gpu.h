@@ -22,6 +22,8 @@
  *   ads_apply_mass      (Mx (x) My (x) Mz) u with MKBBT's mass band  src/projection_engine.F90:63-132
  *   ads_set_oil         the oil problem's pointwise data and mi      problems/oil/input_data.F90:6-20,265-303
  *   ads_get_drained     the `drained` statistic (ComputeResults)     problems/oil/input_data.F90:83-99
+ *   ads_save_spline_plot  SaveSplinePlot + VtkOutput of PrintSolution  src/ADS.F90:955-989
+ *   ads_write_vti       VtkOutput                                    src/vtk.F90:15-77
  *   ads_heat_adjoint    new: hand-written adjoint of the explicit heat step
  *
  * Layouts.  Coefficient vectors are x-fastest, u[x + Nx*(y + Ny*z)], which is
@@ -124,6 +126,19 @@ int ads_set_form(ads_handle* h, int form, const double* f_qp, const double* kapp
  * mu = the exponent of bq = exp(mu u) (:297-303; mi = 10 there).  Needed
  * before stepping with ADS_FORM_OIL; resets the drained total. */
 int ads_set_oil(ads_handle* h, const double* drain_qp, double mu);
+/* SaveSplinePlot + EvalSpline (src/plot.F90:111-140, src/basis.F90:323-369)
+ * on the current coefficients: vals[ix + res0*(iy + res1*iz)] = the spline at
+ * x = lerp(ix/(res0-1), range[0], range[1]), y from range[2..3], z from
+ * range[4..5] (res 2..4096 per axis).  With name non-NULL the samples are
+ * also written to name.vti as VtkOutput does (src/vtk.F90:15-77).  vals may
+ * be NULL.  PrintSolution (src/ADS.F90:955-989) is name "step<iter>", range
+ * [0,1]^3, res 31^3. */
+int ads_save_spline_plot(ads_handle* h, const char* name, const double range[6], const int res[3],
+                         double* vals);
+/* VtkOutput (src/vtk.F90:15-77) alone: an ASCII VTK ImageData file name.vti
+ * with the res0 x res1 x res2 samples (x fastest) in F30.10 notation.  No
+ * handle or GPU needed. */
+int ads_write_vti(const char* name, const int res[3], const double* vals);
 /* The oil problem's `drained` statistic (problems/oil/RHS_eq.F90:87, printed
  * by ComputeResults, problems/oil/input_data.F90:83-99): the sum over the
  * steps since ads_set_oil of J W v dt max(0, w u) over points and test

@@ -840,6 +840,58 @@ ORC_API void orc_pivoted(const OrcADS* A, int* piv) {
   for (int d = 0; d < 3; ++d) piv[d] = A->pivoted[d];
 }
 
+// FindSpan (src/basis.F90:226-259): the knot span of uu, clamped to [p, n],
+// by the reference's binary search.
+ORC_API int orc_find_span(int n, int p, double uu, const double* U) {
+  if (uu >= U[n + 1]) return n;
+  if (uu <= U[p]) return p;
+  int low = p, high = n + 1;
+  int span = (low + high) / 2;
+  while (uu < U[span] || uu >= U[span + 1]) {
+    if (uu < U[span]) high = span;
+    else low = span;
+    span = (low + high) / 2;
+  }
+  return span;
+}
+
+// SaveSplinePlot's sampling (src/plot.F90:111-140) with EvalSpline
+// (src/basis.F90:323-369, d = 0) on the coefficients R: vals(ix, iy, iz) at
+// x = lerp((ix-1)/(resx-1), startx, endx) etc., x fastest.  range =
+// (startx, endx, starty, endy, startz, endz).  The plotted array is the one
+// GatherFullSolution (src/my_mpi.F90:422-514) collects, at one rank R itself.
+ORC_API void orc_eval_spline_grid(const OrcADS* A, const double range[6], const int res[3], double* vals) {
+  const OrcAxis &X = A->ax[0], &Y = A->ax[1], &Z = A->ax[2];
+  const int sx = A->s[0], sy = A->s[1];
+  auto lerp = [](double t, double a, double b) { return (1.0 - t) * a + t * b; };
+#pragma omp parallel for schedule(static)
+  for (int ix = 1; ix <= res[0]; ++ix) {
+    std::vector<double> bx(X.p + 1), by(Y.p + 1), bz(Z.p + 1);
+    const double x = lerp((ix - 1) / (double)(res[0] - 1), range[0], range[1]);
+    const int xspan = orc_find_span(X.n, X.p, x, X.U.data());
+    orc_ders_basis_funs(xspan, x, X.p, 0, X.U.data(), bx.data());
+    for (int iy = 1; iy <= res[1]; ++iy) {
+      const double y = lerp((iy - 1) / (double)(res[1] - 1), range[2], range[3]);
+      const int yspan = orc_find_span(Y.n, Y.p, y, Y.U.data());
+      orc_ders_basis_funs(yspan, y, Y.p, 0, Y.U.data(), by.data());
+      for (int iz = 1; iz <= res[2]; ++iz) {
+        const double z = lerp((iz - 1) / (double)(res[2] - 1), range[4], range[5]);
+        const int zspan = orc_find_span(Z.n, Z.p, z, Z.U.data());
+        orc_ders_basis_funs(zspan, z, Z.p, 0, Z.U.data(), bz.data());
+        const int x0 = xspan - X.p, y0 = yspan - Y.p, z0 = zspan - Z.p;
+        double val = 0.0;
+        for (int a = 0; a <= X.p; ++a)
+          for (int b = 0; b <= Y.p; ++b)
+            for (int c = 0; c <= Z.p; ++c) {
+              const double w = bx[a] * by[b] * bz[c];
+              val = val + w * A->R[(x0 + a) + (size_t)sx * ((y0 + b) + (size_t)sy * (z0 + c))];
+            }
+        vals[(ix - 1) + (size_t)res[0] * ((iy - 1) + (size_t)res[1] * (iz - 1))] = val;
+      }
+    }
+  }
+}
+
 // Heat-problem quadrature-point field of initial_state (problems/heat/input_data.F90:57-70)
 // in the (kx,ky,kz,ex,ey,ez) layout.
 ORC_API void orc_heat_initial_qp(const OrcADS* A, double* fqp) {

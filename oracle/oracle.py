@@ -64,6 +64,9 @@ def lib():
         L.orc_step_oil.restype = ctypes.c_int
         L.orc_assemble_oil.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, _dp]
         L.orc_assemble_oil.restype = ctypes.c_double
+        L.orc_find_span.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp]
+        L.orc_find_span.restype = ctypes.c_int
+        L.orc_eval_spline_grid.argtypes = [ctypes.c_void_p, _dp, _ip, _dp]
         L.orc_solve_F.argtypes = [ctypes.c_void_p, _dp]
         L.orc_solve_F.restype = ctypes.c_int
         L.orc_pivoted.argtypes = [ctypes.c_void_p, _ip]
@@ -214,6 +217,14 @@ class Oracle:
         dr = ctypes.c_double(0.0)
         l2 = lib().orc_assemble_oil(self.h, _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), mu, dt, ctypes.byref(dr))
         return self.F(), l2, dr.value
+
+    def eval_spline_grid(self, rng=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), res=(31, 31, 31)):
+        """SaveSplinePlot's samples of the current coefficients (x fastest), shaped (resz, resy, resx)."""
+        r = np.ascontiguousarray(rng, dtype=np.float64)
+        rs = np.ascontiguousarray(res, dtype=np.int32)
+        vals = np.zeros(int(np.prod(res)))
+        lib().orc_eval_spline_grid(self.h, _p(r), _p(rs, _ip), _p(vals))
+        return vals.reshape(res[2], res[1], res[0])
 
     def solve(self, F):
         F = np.ascontiguousarray(F, dtype=np.float64).ravel().copy()
