@@ -81,6 +81,7 @@ struct ads_handle {
   double* d_delta = nullptr;  // mixed: increment of the heat step
   float* d_g32 = nullptr;     // mixed: the FP32 solve's scaled input (G, then each residual), L0
   float* d_x32 = nullptr;     // mixed: the FP32 correction x1, L0
+  float* d_wC = nullptr;      // mixed: the y sweep's FP32 output, L0
   double* d_wA = nullptr;  // L1 (double-sized; float view uses the same memory)
   double* d_wB = nullptr;  // L2
   double* d_shadow = nullptr;
@@ -108,8 +109,7 @@ struct ads_handle {
   // TMA store maps of the sweeps' transposed outputs
   CUtensorMap tm_u_out64{}, tm_r_out64{};
   CUtensorMap tm_wA_out64{}, tm_wB_out64{};
-  CUtensorMap tm_wA_out32{}, tm_wB_out32{};
-  CUtensorMap tm_x32_out{};
+  CUtensorMap tm_wA_out32{}, tm_wC_out32{};
 
   // form
   bool has_form = false;
@@ -370,24 +370,40 @@ int enqueue_solve64(ads_handle* h, const double* in, const CUtensorMap* tm_out, 
 
 // FP32 Kronecker solve of an L0 input (tin 0: double, scaled by *in_scale on
 // load; tin 1: float, already scaled): final_mode 1 writes out = s x (FP64),
-// final_mode 0 writes x itself (FP32) into d_x32
+// final_mode 0 writes x itself (FP32) into d_x32.  x sweep L0 -> L1 (wA) and
+// y sweep L1 -> L0 (wC) in the skewed form of k_sweep (their lines are
+// contiguous along the solve direction), the y sweep with its lanes along x
+// so that its TMA-stored chunks land in L0; z sweep L0 -> L0 in the column
+// form of k_csweep (lines x contiguous: 16-byte row copies, each solution
+// row stored straight out).
 int enqueue_solve32(ads_handle* h, const void* in, int tin, const double* in_scale, const double* out_scale,
                     int final_mode, const int* skip, const char* tag, double* out) {
+  const Geometry& g = h->g;
+  const long long Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
+  std::string nx = std::string("sweep_x_f32") + tag, ny = std::string("sweep_y_f32") + tag,
+              nz = std::string("sweep_z_f32") + tag;
   SweepArgs ax = sweep_args(h, 0, h->d_fac32[0], in);
   ax.in_scale_dev = in_scale;
   ax.skip_flag = skip;
-  std::string nx = std::string("sweep_x_f32") + tag, ny = std::string("sweep_y_f32") + tag,
-              nz = std::string("sweep_z_f32") + tag;
   RUN(h, nx.c_str(), 1, launch_sweep(h->P, tin, 1, 0, false, &h->tm_wA_out32, ax, sweep_grid(h, 0), h->stream));
   SweepArgs ay = sweep_args(h, 1, h->d_fac32[1], h->d_wA);
+  // lines x (stride PY in L1: y + PY (x + Nx z)), tiles over z
+  ay.lanes_total = (int)Nx; ay.lane_dim = 1; ay.out_line_dim = 1; ay.third_extent = (int)Nz;
+  ay.out_third_extent = ay.third_extent;
+  ay.in_ls = g.PY; ay.in_t3s = g.PY * Nx;
+  ay.tiles_lane = (ay.lanes_total + SW_LANES - 1) / SW_LANES;
   ay.skip_flag = skip;
-  RUN(h, ny.c_str(), 1, launch_sweep(h->P, 1, 1, 0, false, &h->tm_wB_out32, ay, sweep_grid(h, 1), h->stream));
-  SweepArgs az = sweep_args(h, 2, h->d_fac32[2], h->d_wB);
-  az.out_scale_dev = out_scale;
-  az.skip_flag = skip;
-  az.out = out;
-  const CUtensorMap* zmap = final_mode == 0 ? &h->tm_x32_out : &h->tm_wB_out32;  // the latter unused
-  RUN(h, nz.c_str(), 1, launch_sweep(h->P, 1, 1, final_mode, false, zmap, az, sweep_grid(h, 2), h->stream));
+  RUN(h, ny.c_str(), 1, launch_sweep(h->P, 1, 1, 0, false, &h->tm_wC_out32, ay, ay.tiles_lane * (int)Nz, h->stream));
+  CSweepArgs cz{};
+  cz.L = (int)Nz; cz.nl = (int)Nx; cz.n3 = (int)Ny;
+  cz.in = h->d_wC;
+  cz.in_ls = 1; cz.in_ps = g.PX * Ny; cz.in_ts = g.PX;
+  cz.out = final_mode == 1 ? static_cast<void*>(out) : static_cast<void*>(h->d_x32);
+  cz.out_ps = g.PX * Ny; cz.out_ts = g.PX;
+  cz.fac = h->d_fac32[2];
+  cz.out_scale_dev = out_scale;
+  cz.skip_flag = skip;
+  RUN(h, nz.c_str(), 1, launch_csweep(h->P, final_mode, cz, h->stream));
   return ADS_OK;
 }
 
@@ -562,7 +578,7 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_fac64[d]); cudaFree(h->d_tfac64[d]); cudaFree(h->d_fac32[d]); cudaFree(h->d_band[d]);
     cudaFree(h->d_band32[d]);
   }
-  cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_g32); cudaFree(h->d_x32); cudaFree(h->d_wA); cudaFree(h->d_wB);
+  cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_g32); cudaFree(h->d_x32); cudaFree(h->d_wC); cudaFree(h->d_wA); cudaFree(h->d_wB);
   cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_dqp); cudaFree(h->d_l2part); cudaFree(h->d_stage); cudaFree(h->d_slab); cudaFree(h->d_xslab);
   cudaFree(h->d_part); cudaFree(h->d_scal); cudaFree(h->d_flags); cudaFree(h->d_hist);
   if (h->ev0) cudaEventDestroy(h->ev0);
@@ -635,6 +651,9 @@ int create_impl(ads_handle* h) {
     double* x32 = nullptr;
     if ((st = zalloc(&x32, (h->n0 + 1) / 2))) return st;
     h->d_x32 = reinterpret_cast<float*>(x32);
+    double* wc = nullptr;
+    if ((st = zalloc(&wc, (h->n0 + 1) / 2))) return st;
+    h->d_wC = reinterpret_cast<float*>(wc);
   }
   if ((st = zalloc(&h->d_wA, h->n1))) return st;
   if ((st = zalloc(&h->d_wB, h->n2))) return st;
@@ -697,8 +716,8 @@ int create_impl(ads_handle* h) {
   ok &= make_l1_out(h, &h->tm_wA_out64, h->d_wA, false);
   ok &= make_l2_out(h, &h->tm_wB_out64, h->d_wB, false);
   ok &= make_l1_out(h, &h->tm_wA_out32, h->d_wA, true);
-  ok &= make_l2_out(h, &h->tm_wB_out32, h->d_wB, true);
-  if (h->d_x32) ok &= make_l0_out(h, &h->tm_x32_out, h->d_x32, true);
+  // the FP32 y sweep's output: L0 chunks of 32 x by SW_CH y
+  if (h->d_wC) ok &= encode(&h->tm_wC_out32, h->d_wC, true, h->g.N[0], h->g.N[1], h->g.N[2], h->g.PX, SW_LANES, SW_CH, 1);
   if (!ok) return fail(h, ADS_ERR_CUDA, "cuTensorMapEncodeTiled rejected a layout");
   return ADS_OK;
 }

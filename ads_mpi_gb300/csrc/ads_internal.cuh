@@ -129,6 +129,22 @@ struct SweepArgs {
   int* err;
 };
 
+// Column-form FP32 sweep (k_csweep.cu): lines l in [0, nl) in tiles of 32,
+// positions i in [0, L), third index t in [0, n3).  Element (l, i, t) of the
+// input is in[l*in_ls + i*in_ps + t*in_ts] (in_ls == 1: lines contiguous), of the
+// output out[l + i*out_ps + t*out_ts]: float (mode 0) or, in mode 1, the FP64
+// state 2^e x with 2^e = *out_scale_dev.
+struct CSweepArgs {
+  int L, nl, n3;
+  const float* in;
+  long long in_ls, in_ps, in_ts;
+  void* out;
+  long long out_ps, out_ts;
+  const float* fac;              // factor rows (2P+2) x L, as for k_sweep
+  const double* out_scale_dev;
+  const int* skip_flag;
+};
+
 struct ResidualArgs {
   Geometry g;
   int zc, nix, niy, niz;
@@ -358,5 +374,6 @@ __device__ __forceinline__ int pow2_exp(double s) {
   return (int)(((unsigned long long)__double_as_longlong(s) >> 52) & 0x7ffull) - 1023;
 }
 size_t sweep_smem_bytes(int tin, int tc, int P, int L);
+cudaError_t launch_csweep(int P, int mode, const CSweepArgs& a, cudaStream_t s);
 
 }  // namespace ads

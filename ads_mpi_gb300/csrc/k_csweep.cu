@@ -1,0 +1,271 @@
+// k_csweep.cu — the FP32 z sweep of the mixed step in column form.
+//
+// Replaces SolveOneDirection (src/ADS.F90:294-379) along z and the reorder
+// back to the x-fastest layout (src/reorderRHS.F90:7-93) for the FP32
+// solves.  The input (the y sweep's output) has the lines contiguous: 32
+// consecutive x at one y form a 128-byte row at every z.  One warp solves 32
+// lines with the lanes ACROSS the lines: at every step all 32 lanes are at
+// the same position, so
+//   * the tile is staged position-major by 16-byte copies, S[pos][line] with
+//     a row stride of 36 floats: a row of 32 lanes hits 32 different banks;
+//   * the LU factors of a position are the same for every lane: one
+//     broadcast vector load per step from a per-CTA table;
+//   * there is no wavefront skew, so no ramp steps;
+//   * each solution row (32 consecutive x) is stored straight to global
+//     memory, coalesced, during the backward pass: FP32, or the FP64 state
+//     2^e x.
+// (The x and y sweeps read inputs whose positions are contiguous; staging
+// those position-major takes 4-byte transposing copies, measured slower than
+// k_sweep's skewed form, so they stay there.)  A CTA holds as many warps
+// (tiles) as shared memory allows next to one copy of the factor tables;
+// warps loop over tiles on their own.  No wait spins: cp.async groups
+// complete in hardware.
+#include "ads_internal.cuh"
+
+#include <algorithm>
+#include <type_traits>
+
+namespace ads {
+
+constexpr int CS_BLK = 16;        // steps per software-pipelined block
+constexpr int CS_GROUPS = 4;      // position groups of the staged input
+constexpr int CS_MAX_WARPS = 8;
+
+__device__ __forceinline__ unsigned cs_smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void cs_cp16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(cs_smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cs_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cs_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// factor table of one position: forward f[1..P] in VF float4, backward
+// (bs, g[1..P]) in VB float4
+template <int P>
+struct CsTab {
+  static constexpr int VF = (P + 3) / 4;
+  static constexpr int VB = (P + 1 + 3) / 4;
+  __host__ __device__ static size_t bytes(int L) { return sizeof(float4) * (size_t)(VF + VB) * L; }
+};
+
+constexpr int CS_SROW = 36;  // floats per staged row: 16-byte aligned, 32 lanes on 32 banks
+size_t csweep_warp_bytes(int L) { return sizeof(float) * (size_t)L * CS_SROW; }
+
+template <int P, int MODE>
+__global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  if (a.skip_flag != nullptr && *a.skip_flag != 0) return;
+  using Tab = CsTab<P>;
+  constexpr int VF = Tab::VF, VB = Tab::VB;
+  const int L = a.L;
+  const int j = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int srow = CS_SROW;
+  float4* FT = reinterpret_cast<float4*>(smem);      // [L][VF]
+  float4* BT = FT + (size_t)VF * L;                  // [L][VB]
+  float* S = reinterpret_cast<float*>(smem + Tab::bytes(L)) + (size_t)warp * L * srow;
+
+  // factor rows (global [row][L]): row 0 fs (1 here), 1..P f, P+1 bs, P+2.. g
+  for (int i = threadIdx.x; i < L; i += blockDim.x) {
+    float fw[4 * VF], bw[4 * VB];
+#pragma unroll
+    for (int m = 0; m < 4 * VF; ++m) fw[m] = (m < P) ? a.fac[(size_t)(1 + m) * L + i] : 0.f;
+#pragma unroll
+    for (int m = 0; m < 4 * VB; ++m) bw[m] = (m <= P) ? a.fac[(size_t)(P + 1 + m) * L + i] : 0.f;
+#pragma unroll
+    for (int v = 0; v < VF; ++v) FT[(size_t)i * VF + v] = make_float4(fw[4 * v], fw[4 * v + 1], fw[4 * v + 2], fw[4 * v + 3]);
+#pragma unroll
+    for (int v = 0; v < VB; ++v) BT[(size_t)i * VB + v] = make_float4(bw[4 * v], bw[4 * v + 1], bw[4 * v + 2], bw[4 * v + 3]);
+  }
+  __syncthreads();
+
+  const double osd = (MODE == 1) ? *a.out_scale_dev : 1.0;
+  const int out_exp = pow2_exp(osd);
+  const int tiles_l = (a.nl + 31) / 32;
+  const int ntiles = tiles_l * a.n3;
+  const int GP = ((L + CS_GROUPS - 1) / CS_GROUPS + CS_BLK - 1) / CS_BLK * CS_BLK;  // positions per group
+
+  for (int tile = blockIdx.x * nwarps + warp; tile < ntiles; tile += gridDim.x * nwarps) {
+    const int tl = tile % tiles_l, t3 = tile / tiles_l;
+    const int l0 = tl * 32;
+    const int nlv = min(32, a.nl - l0);
+    const float* src = a.in + (size_t)t3 * a.in_ts + (size_t)l0 * a.in_ls;
+
+    __syncwarp();  // the previous tile is done with S
+    // ---- stage: group g holds positions [g*GP, (g+1)*GP) of every line ----
+#pragma unroll 1
+    for (int g = 0; g < CS_GROUPS; ++g) {
+      const int p0 = g * GP, p1 = min(L, p0 + GP);
+      // 16-byte copies of the line-contiguous rows (lines up to a multiple
+      // of 4: within the row's padded pitch)
+      const int nc = (nlv + 3) / 4;
+      for (int idx = j; idx < (p1 - p0) * nc; idx += 32) {
+        const int i = p0 + idx / nc, c = idx % nc;
+        cs_cp16(S + (size_t)i * srow + 4 * c, src + (size_t)i * a.in_ps + 4 * c);
+      }
+      cs_commit();
+    }
+
+    float* Sj = S + j;
+    // ---- forward: y_i = b_i - sum_m f[m]_i y_{i-m}, in place ----
+    {
+      float prev[P];
+#pragma unroll
+      for (int m = 0; m < P; ++m) prev[m] = 0.f;
+      int i = 0;
+#pragma unroll 1
+      for (int g = 0; g < CS_GROUPS; ++g) {
+        switch (g) {
+          case 0: cs_wait<CS_GROUPS - 1>(); break;
+          case 1: cs_wait<CS_GROUPS - 2>(); break;
+          case 2: cs_wait<CS_GROUPS - 3>(); break;
+          default: cs_wait<0>(); break;
+        }
+        __syncwarp();
+        const int ie = min(L, (g + 1) * GP);
+#pragma unroll 1
+        for (; i + CS_BLK <= ie; i += CS_BLK) {
+          float bv[CS_BLK];
+          float4 fv[CS_BLK][VF];
+#pragma unroll
+          for (int t = 0; t < CS_BLK; ++t) {
+            bv[t] = Sj[(size_t)(i + t) * srow];
+#pragma unroll
+            for (int v = 0; v < VF; ++v) fv[t][v] = FT[(size_t)(i + t) * VF + v];
+          }
+#pragma unroll
+          for (int t = 0; t < CS_BLK; ++t) {
+            const float* f = reinterpret_cast<const float*>(fv[t]);
+            float y = bv[t];
+#pragma unroll
+            for (int m = P; m >= 1; --m) y -= f[m - 1] * prev[m - 1];
+#pragma unroll
+            for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
+            prev[0] = y;
+            bv[t] = y;
+          }
+#pragma unroll
+          for (int t = 0; t < CS_BLK; ++t) Sj[(size_t)(i + t) * srow] = bv[t];
+        }
+#pragma unroll 1
+        for (; i < ie; ++i) {
+          float4 fv[VF];
+#pragma unroll
+          for (int v = 0; v < VF; ++v) fv[v] = FT[(size_t)i * VF + v];
+          const float* f = reinterpret_cast<const float*>(fv);
+          float y = Sj[(size_t)i * srow];
+#pragma unroll
+          for (int m = P; m >= 1; --m) y -= f[m - 1] * prev[m - 1];
+#pragma unroll
+          for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
+          prev[0] = y;
+          Sj[(size_t)i * srow] = y;
+        }
+      }
+    }
+
+    // ---- backward: x_i = bs_i y_i - sum_m g[m]_i x_{i+m}; row i goes out ----
+    {
+      const bool act = j < nlv;
+      using TO = typename std::conditional<MODE == 1, double, float>::type;
+      TO* op = static_cast<TO*>(a.out) + (size_t)t3 * a.out_ts + (size_t)(l0 + j);
+      const size_t ops = (size_t)a.out_ps;
+      float nxt[P];
+#pragma unroll
+      for (int m = 0; m < P; ++m) nxt[m] = 0.f;
+      int i = L;
+      const int rem = L % CS_BLK;
+#pragma unroll 1
+      for (int r = 0; r < rem; ++r) {
+        --i;
+        float4 bw[VB];
+#pragma unroll
+        for (int v = 0; v < VB; ++v) bw[v] = BT[(size_t)i * VB + v];
+        const float* b = reinterpret_cast<const float*>(bw);
+        float x = b[0] * Sj[(size_t)i * srow];
+#pragma unroll
+        for (int m = P; m >= 1; --m) x -= b[m] * nxt[m - 1];
+#pragma unroll
+        for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
+        nxt[0] = x;
+        if (act) {
+          if constexpr (MODE == 1) op[(size_t)i * ops] = f2d_scaled(x, out_exp);
+          else op[(size_t)i * ops] = x;
+        }
+      }
+#pragma unroll 1
+      for (; i >= CS_BLK; i -= CS_BLK) {
+        const int ib = i - CS_BLK;  // block [ib, i), processed downwards
+        float yv[CS_BLK];
+        float4 bw[CS_BLK][VB];
+#pragma unroll
+        for (int t = 0; t < CS_BLK; ++t) {
+          yv[t] = Sj[(size_t)(ib + t) * srow];
+#pragma unroll
+          for (int v = 0; v < VB; ++v) bw[t][v] = BT[(size_t)(ib + t) * VB + v];
+        }
+#pragma unroll
+        for (int t = CS_BLK - 1; t >= 0; --t) {
+          const float* b = reinterpret_cast<const float*>(bw[t]);
+          float x = b[0] * yv[t];
+#pragma unroll
+          for (int m = P; m >= 1; --m) x -= b[m] * nxt[m - 1];
+#pragma unroll
+          for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
+          nxt[0] = x;
+          yv[t] = x;
+        }
+        if (act) {
+#pragma unroll
+          for (int t = CS_BLK - 1; t >= 0; --t) {
+            if constexpr (MODE == 1) op[(size_t)(ib + t) * ops] = f2d_scaled(yv[t], out_exp);
+            else op[(size_t)(ib + t) * ops] = yv[t];
+          }
+        }
+      }
+    }
+  }
+  cs_wait<0>();
+}
+
+template <int P, int MODE>
+static cudaError_t launch_cs(const CSweepArgs& a, cudaStream_t s) {
+  auto kern = k_csweep<P, MODE>;
+  int dev = 0, nsm = 0, smem_max = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t tab = CsTab<P>::bytes(a.L), per = csweep_warp_bytes(a.L);
+  if (tab + per > (size_t)smem_max) return cudaErrorInvalidValue;
+  const int nw = (int)std::min<size_t>(CS_MAX_WARPS, ((size_t)smem_max - tab) / per);
+  const size_t bytes = tab + per * nw;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return e;
+  const int tiles = (a.nl + 31) / 32 * a.n3;
+  const int grid = std::max(1, std::min(nsm, (tiles + nw - 1) / nw));
+  kern<<<grid, 32 * nw, bytes, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_csweep(int P, int mode, const CSweepArgs& a, cudaStream_t s) {
+  if (a.in == nullptr || a.out == nullptr || a.fac == nullptr || (mode == 1 && a.out_scale_dev == nullptr))
+    return cudaErrorInvalidValue;
+  // lines contiguous, rows 16-byte aligned (pitches are multiples of 8 entries)
+  if (a.in_ls != 1 || (a.in_ps % 4) != 0 || (a.in_ts % 4) != 0) return cudaErrorInvalidValue;
+  switch (P * 2 + mode) {
+    case 2: return launch_cs<1, 0>(a, s);
+    case 3: return launch_cs<1, 1>(a, s);
+    case 4: return launch_cs<2, 0>(a, s);
+    case 5: return launch_cs<2, 1>(a, s);
+    case 6: return launch_cs<3, 0>(a, s);
+    case 7: return launch_cs<3, 1>(a, s);
+    case 8: return launch_cs<4, 0>(a, s);
+    case 9: return launch_cs<4, 1>(a, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace ads
