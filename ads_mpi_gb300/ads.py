@@ -64,6 +64,7 @@ ABI = [
     ("ads_get_coeffs", [ctypes.c_void_p, _dp], ctypes.c_int),
     ("ads_step", [ctypes.c_void_p, _dp], ctypes.c_int),
     ("ads_steps", [ctypes.c_void_p, ctypes.c_int, _dp], ctypes.c_int),
+    ("ads_multistep", [ctypes.c_void_p, _dp, _dp], ctypes.c_int),
     ("ads_get_stats", [ctypes.c_void_p, ctypes.POINTER(Stats)], ctypes.c_int),
     ("ads_assemble", [ctypes.c_void_p, _dp, _dp], ctypes.c_int),
     ("ads_solve", [ctypes.c_void_p, _dp, _dp], ctypes.c_int),
@@ -311,6 +312,15 @@ class ADS:
         out = np.zeros(max(k, 1))
         self._check(self._L.ads_steps(self.h, k, _ptr(out)))
         return out[:k]
+
+    # reference name: MultiStep (src/ADS.F90:391-429); returns l2norm
+    def multistep(self, mix):
+        """Three substeps with the 1-D matrix mixes mix[s] = (M, K, B, BT)
+        weights of substep s (the reference's mix(4,3), one row per substep)."""
+        m = np.ascontiguousarray(mix, dtype=np.float64).reshape(3, 4)
+        l2 = ctypes.c_double(0.0)
+        self._check(self._L.ads_multistep(self.h, _ptr(m), ctypes.byref(l2)))
+        return l2.value
 
     def stats(self):
         s = Stats()

@@ -90,6 +90,14 @@ struct ads_handle {
   double* d_dqp = nullptr;  // oil: draining weight per point (qp grid layout)
   double* d_l2part = nullptr;
   double* d_stage = nullptr;        // packed copy of one coefficient array (host transfers)
+  // MultiStep: the start-of-step state, a work array, and per axis the
+  // pivoted LU of the last matrix mix
+  double* d_un = nullptr;
+  double* d_ms = nullptr;
+  double* d_mab[3] = {nullptr, nullptr, nullptr};
+  int* d_mpiv[3] = {nullptr, nullptr, nullptr};
+  double mab_mix[3][4] = {};
+  bool mab_valid[3] = {false, false, false};
   unsigned char* d_slab = nullptr;  // spill-slab flags per DOF index (x, y, z)
   int* d_xslab = nullptr;           // x indices of the x slabs
   int nxslab = 0;
@@ -579,7 +587,8 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_band32[d]);
   }
   cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_g32); cudaFree(h->d_x32); cudaFree(h->d_wC); cudaFree(h->d_wA); cudaFree(h->d_wB);
-  cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_dqp); cudaFree(h->d_l2part); cudaFree(h->d_stage); cudaFree(h->d_slab); cudaFree(h->d_xslab);
+  cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_dqp); cudaFree(h->d_l2part); cudaFree(h->d_stage); cudaFree(h->d_un); cudaFree(h->d_ms);
+  for (int d = 0; d < 3; ++d) { cudaFree(h->d_mab[d]); cudaFree(h->d_mpiv[d]); } cudaFree(h->d_slab); cudaFree(h->d_xslab);
   cudaFree(h->d_part); cudaFree(h->d_scal); cudaFree(h->d_flags); cudaFree(h->d_hist);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -996,11 +1005,91 @@ int ads_save_spline_plot(ads_handle* h, const char* name, const double range[6],
   return ADS_OK;
 }
 
+// the pivoted LU of mix along axis d, cached per mix
+static int multistep_factors(ads_handle* h, int d, const double mix[4]) {
+  if (h->mab_valid[d] && std::memcmp(h->mab_mix[d], mix, sizeof(double) * 4) == 0) return ADS_OK;
+  const AxisHost& a = h->ax[d];
+  std::vector<double> AB;
+  mix_band(a, mix, AB);
+  std::vector<int> ipiv(a.N);
+  if (band_lu(a.N, a.p, a.p, AB.data(), 3 * a.p + 1, ipiv.data()))
+    return fail(h, ADS_ERR_ZERO_PIVOT, "zero pivot in the 1-D matrix of the MultiStep mix");
+  if (!h->d_mab[d]) ADS_CUDA(h, cudaMalloc((void**)&h->d_mab[d], sizeof(double) * AB.size()));
+  if (!h->d_mpiv[d]) ADS_CUDA(h, cudaMalloc((void**)&h->d_mpiv[d], sizeof(int) * ipiv.size()));
+  // in stream order: the previous substep's solves on this stream may still
+  // read the old factors (a pageable source is staged before the call returns)
+  ADS_CUDA(h, cudaMemcpyAsync(h->d_mab[d], AB.data(), sizeof(double) * AB.size(), cudaMemcpyHostToDevice, h->stream));
+  ADS_CUDA(h, cudaMemcpyAsync(h->d_mpiv[d], ipiv.data(), sizeof(int) * ipiv.size(), cudaMemcpyHostToDevice, h->stream));
+  std::memcpy(h->mab_mix[d], mix, sizeof(double) * 4);
+  h->mab_valid[d] = true;
+  return ADS_OK;
+}
+
+int ads_multistep(ads_handle* h, const double mix[12], double* l2norm) {
+  if (!h || !mix) return ADS_ERR_ARG;
+  if (!h->has_form) return fail(h, ADS_ERR_STATE, "ads_set_form must be called before stepping");
+  if (h->form == ADS_FORM_OIL)
+    return fail(h, ADS_ERR_UNSUPPORTED, "MultiStep supports the projection and heat forms (the oil integrand "
+                                        "would need its value and gradient from different coefficient sets)");
+  for (int i = 0; i < 12; ++i)
+    if (!std::isfinite(mix[i])) return fail(h, ADS_ERR_NONFINITE, "non-finite MultiStep mix");
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  const Geometry& g = h->g;
+  const long long Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
+  const size_t bytes = sizeof(double) * h->n0;
+  for (double** p : {&h->d_un, &h->d_ms}) {
+    if (!*p) {
+      ADS_CUDA(h, cudaMalloc((void**)p, bytes));
+      ADS_CUDA(h, cudaMemset(*p, 0, bytes));
+    }
+  }
+  int st;
+  ADS_CUDA(h, cudaMemcpyAsync(h->d_un, h->d_u, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  double l2 = 0.0;
+  for (int sub = 0; sub < 3; ++sub) {
+    const double* mx = mix + 4 * sub;
+    for (int d = 0; d < 3; ++d)
+      if ((st = multistep_factors(h, d, mx))) return st;
+    // FormUn(sub) + Form3DRHS: the integrand sees u from the start of the
+    // step (Un) and grad u of the current coefficients (dUn); the heat form
+    // is linear in both, so F = F(current) + M (u^n - current)
+    if ((st = enqueue_assemble(h, h->d_u, h->d_F, false, false, true))) return st;
+    if (sub == 0) {
+      // the l2norm integrates Un, the same in every substep
+      ADS_CUDA(h, cudaMemcpyAsync(&l2, h->d_scal + SC_L2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    } else if (h->form == ADS_FORM_HEAT) {
+      ADS_CUDA(h, cudaMemcpyAsync(h->d_ms, h->d_un, bytes, cudaMemcpyDeviceToDevice, h->stream));
+      RUN(h, "axpby", 1, launch_axpby(h->d_ms, h->d_u, -1.0, 1.0, (long long)h->n0, h->stream));
+      ResidualArgs ra = residual_args(h, h->d_ms, nullptr, h->d_r);  // d_r = M (u^n - current)
+      RUN(h, "mass_apply", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
+      RUN(h, "add", 1, launch_add(h->d_F, h->d_r, (long long)h->n0, h->stream));
+    }
+    // Sub_Step's three solves with the mix, in place on F (L0)
+    RUN(h, "band_solve_x", 1, launch_band_solve(h->d_F, Ny, Nz, g.PX, g.PX * Ny, 1, (int)Nx, h->P, h->P,
+                                                h->d_mab[0], h->d_mpiv[0], h->stream));
+    RUN(h, "band_solve_y", 1, launch_band_solve(h->d_F, Nx, Nz, 1, g.PX * Ny, g.PX, (int)Ny, h->P, h->P,
+                                                h->d_mab[1], h->d_mpiv[1], h->stream));
+    RUN(h, "band_solve_z", 1, launch_band_solve(h->d_F, Nx, Ny, 1, g.PX, g.PX * Ny, (int)Nz, h->P, h->P,
+                                                h->d_mab[2], h->d_mpiv[2], h->stream));
+    ADS_CUDA(h, cudaMemcpyAsync(h->d_u, h->d_F, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  ADS_CUDA(h, cudaStreamSynchronize(h->stream));
+  if ((st = check_flags(h))) return st;
+  if (!std::isfinite(l2)) return fail(h, ADS_ERR_NONFINITE, "non-finite l2norm");
+  h->last.l2norm = l2;
+  h->last.rel_residual = 0.0;
+  h->last.refinements = 0;
+  h->last.converged = 1;
+  if (l2norm) *l2norm = l2;
+  return ADS_OK;
+}
+
 int ads_get_drained(const ads_handle* h, double* drained) {
   if (!h || !drained) return ADS_ERR_ARG;
   ads_handle* hm = const_cast<ads_handle*>(h);
   ADS_CUDA(hm, cudaSetDevice(h->dev));
-  ADS_CUDA(hm, cudaMemcpy(drained, h->d_scal + SC_DRAINED_TOTAL, sizeof(double), cudaMemcpyDeviceToHost));
+  ADS_CUDA(hm, cudaMemcpyAsync(drained, h->d_scal + SC_DRAINED_TOTAL, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  ADS_CUDA(hm, cudaStreamSynchronize(h->stream));
   return ADS_OK;
 }
 

@@ -245,6 +245,10 @@ cudaError_t launch_record(double* scal, int* flags, double* hist, int cap, cudaS
 // tab/first: the per-axis sample tables of sample_basis, x then y then z
 cudaError_t launch_eval_grid(const double* u, const Geometry& g, const double* tab, const int* first, int rx,
                              int ry, int rz, double* vals, cudaStream_t s);
+// MultiStep: the pivoted band solve (band_lu factors) along one direction of an
+// FP64 L0 array, lines (l1, l2) at b + l1*s1 + l2*s2, positions ps apart
+cudaError_t launch_band_solve(double* b, long long n1, long long n2, long long s1, long long s2, long long ps, int n,
+                              int kl, int ku, const double* AB, const int* ipiv, cudaStream_t s);
 // packed coefficients (dense Nx) -> padded L0 (to_padded) or back
 cudaError_t launch_repack(const double* src, double* dst, const Geometry& g, bool to_padded, cudaStream_t s);
 // layout conversions between the per-point (kx,ky,kz,ex,ey,ez) layout and the

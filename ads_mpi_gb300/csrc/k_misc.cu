@@ -645,6 +645,49 @@ cudaError_t launch_eval_grid(const double* u, const Geometry& g, const double* t
 }
 
 // ---------------------------------------------------------------------------
+// One direction of MultiStep's Kronecker solve with a general 1-D matrix mix
+// (src/ADS.F90:391-429 through Sub_Step): the banded LU with row interchanges
+// of band_lu applied to every line of an FP64 L0 array in place, as DGBTRS
+// does: interchanges and L by columns, then U (kl+ku superdiagonals) by
+// columns from the bottom.  One thread per line; line (l1, l2) starts at
+// b + l1*s1 + l2*s2 with positions ps apart (l1 runs fastest: for the y and z
+// directions consecutive threads touch consecutive x).
+// ---------------------------------------------------------------------------
+__global__ void k_band_solve(double* b, long long n1, long long n2, long long s1, long long s2, long long ps,
+                             int n, int kl, int ku, const double* __restrict__ AB, const int* __restrict__ ipiv) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n1 * n2) return;
+  double* x = b + (t % n1) * s1 + (t / n1) * s2;
+  const int kv = kl + ku, ldab = 2 * kl + ku + 1;
+  for (int j = 0; j < n - 1; ++j) {
+    const int lm = min(kl, n - 1 - j), l = ipiv[j];
+    double bj = x[(size_t)j * ps];
+    if (l != j) {
+      const double bl = x[(size_t)l * ps];
+      x[(size_t)l * ps] = bj;
+      x[(size_t)j * ps] = bl;
+      bj = bl;
+    }
+    if (bj != 0.0)
+      for (int i = 1; i <= lm; ++i) x[(size_t)(j + i) * ps] -= AB[(size_t)(kv + i) + (size_t)ldab * j] * bj;
+  }
+  for (int j = n - 1; j >= 0; --j) {
+    double bj = x[(size_t)j * ps];
+    if (bj != 0.0) {
+      bj /= AB[(size_t)kv + (size_t)ldab * j];
+      x[(size_t)j * ps] = bj;
+      for (int i = j - 1; i >= max(0, j - kv); --i) x[(size_t)i * ps] -= bj * AB[(size_t)(kv + i - j) + (size_t)ldab * j];
+    }
+  }
+}
+cudaError_t launch_band_solve(double* b, long long n1, long long n2, long long s1, long long s2, long long ps, int n,
+                              int kl, int ku, const double* AB, const int* ipiv, cudaStream_t s) {
+  const long long lines = n1 * n2;
+  k_band_solve<<<(unsigned)((lines + 127) / 128), 128, 0, s>>>(b, n1, n2, s1, s2, ps, n, kl, ku, AB, ipiv);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // layout conversions
 // ---------------------------------------------------------------------------
 // packed coefficients (x fastest, dense Nx) <-> the padded L0 layout (pitch

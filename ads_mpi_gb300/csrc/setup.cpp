@@ -13,6 +13,7 @@
 // the reference uses the equivalent Piegl-Tiller algorithm A2.3.
 #include <cmath>
 #include <cstring>
+#include <algorithm>
 #include <vector>
 
 #include "setup.h"
@@ -181,6 +182,52 @@ int axis_setup(int n, int p, AxisHost& a) {
           const double vd = a.NN[(((size_t)e * q + k) * (p + 1) + d) * 2];
           a.band[(size_t)(ib - ia + p) * N + ia] += vc * vd * a.J[e] * a.W[k];
         }
+  return 0;
+}
+
+void mix_band(const AxisHost& a, const double mix[4], std::vector<double>& AB) {
+  const int p = a.p, n1 = a.N, ldab = 3 * p + 1;
+  AB.assign((size_t)ldab * n1, 0.0);
+  // contributions summed in MKBBT's order: element, point, row function, column function
+  for (int e = 0; e < a.E; ++e)
+    for (int k = 0; k < a.q; ++k)
+      for (int c = 0; c <= p; ++c)
+        for (int d = 0; d <= p; ++d) {
+          auto nn = [&](int der, int f) { return a.NN[(((size_t)e * a.q + k) * (p + 1) + f) * 2 + der]; };
+          const double M = nn(0, c) * nn(0, d) * a.J[e] * a.W[k];
+          const double K = nn(1, c) * nn(1, d) * a.J[e] * a.W[k];
+          const double B = nn(1, c) * nn(0, d) * a.J[e] * a.W[k];
+          const double BT = nn(0, c) * nn(1, d) * a.J[e] * a.W[k];
+          const int ia = a.O[e] + c, ib = a.O[e] + d;
+          AB[(size_t)(2 * p + ia - ib) + (size_t)ldab * ib] += mix[0] * M + mix[1] * K + mix[2] * B + mix[3] * BT;
+        }
+}
+
+int band_lu(int n, int kl, int ku, double* AB, int ldab, int* ipiv) {
+  const int kv = ku + kl;
+  auto at = [&](int i, int j) -> double& { return AB[(size_t)(kv + i - j) + (size_t)ldab * j]; };
+  int ju = 0;  // last column touched by the row interchanges so far
+  for (int j = 0; j < n; ++j) {
+    const int km = std::min(kl, n - 1 - j);
+    int jp = 0;
+    double amax = std::fabs(at(j, j));
+    for (int i = 1; i <= km; ++i)
+      if (std::fabs(at(j + i, j)) > amax) { amax = std::fabs(at(j + i, j)); jp = i; }
+    ipiv[j] = j + jp;
+    if (at(j + jp, j) == 0.0) return j + 1;
+    ju = std::max(ju, std::min(j + ku + jp, n - 1));
+    if (jp != 0)
+      for (int c = j; c <= ju; ++c) std::swap(at(j + jp, c), at(j, c));
+    if (km > 0) {
+      const double r = 1.0 / at(j, j);
+      for (int i = 1; i <= km; ++i) at(j + i, j) *= r;
+      for (int c = j + 1; c <= ju; ++c) {
+        const double u = at(j, c);
+        if (u != 0.0)
+          for (int i = 1; i <= km; ++i) at(j + i, c) += at(j + i, j) * -u;
+      }
+    }
+  }
   return 0;
 }
 

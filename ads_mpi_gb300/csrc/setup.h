@@ -27,6 +27,15 @@ int find_span(const AxisHost& a, double x);
 // of SaveSplinePlot (src/plot.F90:126-133): B[i*(p+1) + r] = N_{first[i]+r}(x_i)
 void sample_basis(const AxisHost& a, double t0, double t1, int res, std::vector<double>& B,
                   std::vector<int>& first);
+// MKBBT (src/projection_engine.F90:63-132): mix[0] M + mix[1] K + mix[2] B +
+// mix[3] BT with B(a, b) = int N_a' N_b, in LAPACK band storage: kl = ku = p,
+// ldab = 3p+1, A(i, j) at AB[(2p + i - j) + ldab j] (rows 0..p-1 hold the fill-in
+// of the pivoting and start at zero)
+void mix_band(const AxisHost& a, const double mix[4], std::vector<double>& AB);
+// banded LU with partial pivoting in place (the DGBTF2 algorithm): L below the
+// diagonal, U with kl+ku superdiagonals, ipiv 0-based row interchanges;
+// returns 0, or j+1 for a zero pivot in column j
+int band_lu(int n, int kl, int ku, double* AB, int ldab, int* ipiv);
 // LU factors (see ads_internal.cuh) of the mass band; returns 1 on a zero pivot
 int band_factor(const AxisHost& a, std::vector<double>& fac, std::vector<double>& tfac);
 

@@ -12,6 +12,7 @@
  *                        problems/L2Projection/RHS_eq.F90:66-70)
  *   ads_step            Step(iter, RHS_fun, ads, ads_data, l2norm, mierr)  src/ADS.F90:437-461
  *   ads_steps           the time loop of problems/heat/main.F90:49-60 (Step + MPI_Reduce)
+ *   ads_multistep       MultiStep(iter, mix, RHS_fun, ...)          src/ADS.F90:391-429
  *   ads_get_coeffs      ads_data%F after Step / R(:,2,2,2)          src/ADS.F90:777-779
  *   ads_set_coeffs      R(:,2,2,2) before FormUn                    src/projection_engine.F90:412
  *   ads_qp_points       ads%Xx/Xy/Xz (BasisData X output)           src/basis.F90:74-112
@@ -153,6 +154,15 @@ int ads_get_coeffs(ads_handle* h, double* u);
  * Kronecker solve, store the solution as the new coefficients.  l2norm may be
  * NULL. */
 int ads_step(ads_handle* h, double* l2norm);
+/* MultiStep(iter, mix, RHS_fun, ...) (src/ADS.F90:391-429): three substeps,
+ * substep s assembling with the form (u from the start of the step, grad u
+ * from the current coefficients, as FormUn(s) provides them) and solving
+ * (A_s (x) A_s (x) A_s) u = F with A_s = mix[4s] M + mix[4s+1] K +
+ * mix[4s+2] B + mix[4s+3] BT (MKBBT, src/projection_engine.F90:63-132), by
+ * a banded LU with partial pivoting.  mix is the reference's mix(4,3) in
+ * column order.  FP64 on both precisions; PROJECT and HEAT forms.  l2norm
+ * (may be NULL) is the step's, which integrates the start-of-step state. */
+int ads_multistep(ads_handle* h, const double mix[12], double* l2norm);
 /* k Steps; l2norms (k entries) may be NULL.  Runs without host round trips. */
 int ads_steps(ads_handle* h, int k, double* l2norms);
 int ads_get_stats(const ads_handle* h, ads_stats* st);

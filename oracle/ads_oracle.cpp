@@ -464,12 +464,15 @@ ORC_API void orc_get_F(const OrcADS* A, double* F) {
 // projection_engine.F90
 // ---------------------------------------------------------------------------
 
-// FormUn (src/projection_engine.F90:306-441) for one rank and subun = 1:
-// u and grad u of the spline with coefficients R at every quadrature point,
-// stored in Un / dUn with the reference's layout.
-static void orc_form_un(OrcADS& A) {
+// FormUn (src/projection_engine.F90:306-441) for one rank: u and grad u of
+// the spline with coefficients R at every quadrature point, stored in
+// Un / Un13 / Un23 (by subun) and dUn with the reference's layout.
+// subun = 1, 2, 3 fills Un, Un13 or Un23 with the values; dUn always
+// (src/projection_engine.F90:330-340,424-433)
+static void orc_form_un(OrcADS& A, int subun = 1) {
   const OrcAxis &X = A.ax[0], &Y = A.ax[1], &Z = A.ax[2];
-  std::fill(A.Un.begin(), A.Un.end(), 0.0);
+  std::vector<double>& V = (subun == 1) ? A.Un : (subun == 2 ? A.Un13 : A.Un23);
+  std::fill(V.begin(), V.end(), 0.0);
   std::fill(A.dUn.begin(), A.dUn.end(), 0.0);
   const int E1 = X.nelem, E2 = Y.nelem, E3 = Z.nelem;
   const long total = (long)E1 * E2 * E3;
@@ -502,7 +505,7 @@ static void orc_form_un(OrcADS& A) {
           A.dUn[q] = dux;
           A.dUn[q + nqp] = duy;
           A.dUn[q + 2 * nqp] = duz;
-          A.Un[q] = Uval;
+          V[q] = Uval;
         }
   }
 }
@@ -825,6 +828,31 @@ ORC_API double orc_assemble_oil(OrcADS* A, const double* pump_qp, const double* 
   const double l2 = orc_form_3d_rhs(*A, &ctx, orc_rhs_oil);
   if (drained) *drained = A->drained;
   return l2;
+}
+
+// MultiStep (src/ADS.F90:391-429): three substeps; substep s runs FormUn(s)
+// (Un, Un13 or Un23 and dUn from the current R), Form3DRHS with the form's
+// integrand, and the Kronecker solve with the 1-D mix mix[4s..4s+3].  l2norm
+// is the last substep's, as in the reference.
+ORC_API int orc_multistep(OrcADS* A, int form, const double* fqp, const double* kappa_qp, double kappa,
+                          double dt, const double* mix, double* l2norm) {
+  OrcFormCtx ctx{form, fqp, kappa_qp, kappa, dt, 0, nullptr, 0.0};
+  orc_rhs_fun fun = (form == ORC_FORM_HEAT) ? orc_rhs_heat : orc_rhs_project;
+  double l2 = 0.0;
+  for (int s = 1; s <= 3; ++s) {
+    orc_form_un(*A, s);
+    if (s == 1) {
+      std::fill(A->Un13.begin(), A->Un13.end(), 0.0);
+      std::fill(A->Un23.begin(), A->Un23.end(), 0.0);
+    } else if (s == 2) {
+      std::fill(A->Un23.begin(), A->Un23.end(), 0.0);
+    }
+    l2 = orc_form_3d_rhs(*A, &ctx, fun);
+    const int info = orc_kron_solve(*A, mix + 4 * (s - 1));
+    if (info) return info;
+  }
+  if (l2norm) *l2norm = l2;
+  return 0;
 }
 
 // Only the Kronecker solve of F (mix = (1,0,0,0)); result in R and F.

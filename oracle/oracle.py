@@ -67,6 +67,9 @@ def lib():
         L.orc_find_span.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp]
         L.orc_find_span.restype = ctypes.c_int
         L.orc_eval_spline_grid.argtypes = [ctypes.c_void_p, _dp, _ip, _dp]
+        L.orc_multistep.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_double,
+                                    _dp, _dp]
+        L.orc_multistep.restype = ctypes.c_int
         L.orc_solve_F.argtypes = [ctypes.c_void_p, _dp]
         L.orc_solve_F.restype = ctypes.c_int
         L.orc_pivoted.argtypes = [ctypes.c_void_p, _ip]
@@ -225,6 +228,18 @@ class Oracle:
         vals = np.zeros(int(np.prod(res)))
         lib().orc_eval_spline_grid(self.h, _p(r), _p(rs, _ip), _p(vals))
         return vals.reshape(res[2], res[1], res[0])
+
+    def multistep(self, form, mix, fqp=None, kappa_qp=None, kappa=1.0, dt=0.0):
+        """MultiStep (src/ADS.F90:391-429) with mix(4,3) given as a (3, 4) array of
+        substep rows (M, K, B, BT weights); returns the l2norm."""
+        m = np.ascontiguousarray(mix, dtype=np.float64).ravel()
+        fqp = None if fqp is None else np.ascontiguousarray(fqp, dtype=np.float64).ravel()
+        kq = None if kappa_qp is None else np.ascontiguousarray(kappa_qp, dtype=np.float64).ravel()
+        l2 = ctypes.c_double(0.0)
+        info = lib().orc_multistep(self.h, form, _p(fqp), _p(kq), kappa, dt, _p(m), ctypes.byref(l2))
+        if info:
+            raise RuntimeError(f"oracle MultiStep failed: info={info}")
+        return l2.value
 
     def solve(self, F):
         F = np.ascontiguousarray(F, dtype=np.float64).ravel().copy()
