@@ -84,6 +84,12 @@ module ads_gpu
          integer(c_int), intent(in) :: res(3)
          type(c_ptr), value :: vals
       end function
+      integer(c_int) function ads_multistep(h, mix, l2norm) bind(c, name="ads_multistep")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         real(c_double), intent(in) :: mix(4, 3)
+         real(c_double), intent(out) :: l2norm
+      end function
       integer(c_int) function ads_set_coeffs(h, u) bind(c, name="ads_set_coeffs")
          import :: c_int, c_ptr, c_double
          type(c_ptr), value :: h
@@ -185,6 +191,19 @@ contains
       if (mierr /= ADS_OK) return
       mierr = ads_get_coeffs(g % h, F)
    end subroutine GpuStep
+
+   ! MultiStep (src/ADS.F90:391): mix(4,3) as the reference's; F receives the solution.
+   subroutine GpuMultiStep(iter, mix, g, F, l2norm, mierr)
+      integer(kind=4), intent(in) :: iter
+      real(c_double), intent(in) :: mix(4, 3)
+      type(ads_gpu_handle), intent(in) :: g
+      real(c_double), intent(out) :: F(:)
+      real(c_double), intent(out) :: l2norm
+      integer(kind=4), intent(out) :: mierr
+      mierr = ads_multistep(g % h, mix, l2norm)
+      if (mierr /= ADS_OK) return
+      mierr = ads_get_coeffs(g % h, F)
+   end subroutine GpuMultiStep
 
    ! Cleanup (src/ADS.F90:802).
    subroutine GpuCleanup(g, mierr)
