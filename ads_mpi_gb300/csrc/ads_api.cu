@@ -270,14 +270,9 @@ SweepArgs sweep_args(const ads_handle* h, int axis, const void* fac, const void*
     a.lanes_total = N[0]; a.lane_dim = 1; a.out_line_dim = 2; a.third_extent = N[1];
     a.in_ls = g.PZ; a.in_t3s = g.PZ * (long long)N[0];
   }
-  a.out_third_extent = a.third_extent;
   a.tiles_lane = (a.lanes_total + SW_LANES - 1) / SW_LANES;
   a.fac = fac;
   a.in_scale = 1.0;
-  a.out_scale = 1.0;
-  a.out = h->d_u;
-  a.out_pitch = h->g.PX;
-  a.out_slice = h->g.PX * (long long)N[1];
   a.err = h->d_flags + FL_ERR;
   return a;
 }
@@ -397,7 +392,6 @@ int enqueue_solve32(ads_handle* h, const void* in, int tin, const double* in_sca
   SweepArgs ay = sweep_args(h, 1, h->d_fac32[1], h->d_wA);
   // lines x (stride PY in L1: y + PY (x + Nx z)), tiles over z
   ay.lanes_total = (int)Nx; ay.lane_dim = 1; ay.out_line_dim = 1; ay.third_extent = (int)Nz;
-  ay.out_third_extent = ay.third_extent;
   ay.in_ls = g.PY; ay.in_t3s = g.PY * Nx;
   ay.tiles_lane = (ay.lanes_total + SW_LANES - 1) / SW_LANES;
   ay.skip_flag = skip;

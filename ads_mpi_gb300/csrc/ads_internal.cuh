@@ -117,15 +117,9 @@ struct SweepArgs {
   const void* fac;  // factor rows (TC), (2P+2) x L
   double in_scale;  // multiply the input by this before the solve
   const double* in_scale_dev;   // if set, in_scale = *in_scale_dev (refinement)
-  double out_scale;
-  const double* out_scale_dev;  // if set, out_scale = *out_scale_dev
   const int* skip_flag;         // if set and *skip_flag != 0, the kernel returns at once
-  double* out;      // FINAL modes: L0 base
-  long long out_pitch;   // PX
-  long long out_slice;   // PX * Ny
   int out_line_dim;      // TMA store: 1 -> coords (lanes, line, third); 2 -> (lanes, third, line)
   int third_extent;      // extent of the tile's fixed (third) dimension
-  int out_third_extent;  // same, for the final modes (y extent of L0)
   int* err;
 };
 
@@ -191,8 +185,8 @@ cudaError_t launch_assemble_oil(bool fp32, bool incr, const AssembleArgs& a, con
 cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s);
 
 // kind: 0 = x sweep (L0 -> L1), 1 = y sweep (L1 -> L2), 2 = z sweep (L2 -> L0)
-// mode: 0 = TMA store to the next layout (for the z sweep: FP32 or FP64 L0 through
-//       tmout), 1 = final store to FP64 L0 (u = s*x), 3 = identity transpose (no solve)
+// mode: 0 = TMA store to the next layout through tmout, 3 = identity transpose
+//       (no solve); trans (the adjoint's transposed solve) in FP64 only
 // tin: 0 = double input, 1 = float input; tc: 0 = double compute, 1 = float compute
 // The input is read through a.in (set with sweep_input in the host code).
 cudaError_t launch_sweep(int P, int tin, int tc, int mode, bool trans, const CUtensorMap* tmout,

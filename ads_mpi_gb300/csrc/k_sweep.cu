@@ -24,8 +24,7 @@
 //   z sweep: L2 (z fastest) -> L0 (x fastest)   = solve + ReorderRHSForX
 //
 // Mode 3 skips the solve and is the plain staged transpose used by
-// ads_reorder.  Mode 1 finishes the z sweep with coalesced plain stores into
-// the FP64 state (u = s*x).
+// ads_reorder.
 // No wait in this kernel spins: cp.async and bulk-group waits complete in
 // hardware.
 #include "ads_internal.cuh"
@@ -101,12 +100,6 @@ __device__ __forceinline__ TC load_y(const TIn* p) {
   if constexpr (sizeof(TIn) == 8 && sizeof(TC) == 4) return reinterpret_cast<const float*>(p)[0];
   else return (TC)*p;
 }
-// solution value -> FP64 state, times 2^sexp
-template <typename TC>
-__device__ __forceinline__ double out_value(TC x, int sexp) {
-  if constexpr (sizeof(TC) == 4) return f2d_scaled(x, sexp);
-  else return x * ldexp(1.0, sexp);
-}
 
 // One warp per CTA, persistent over tiles of 32 lines.  The recurrences run in
 // blocks of SW_BLK steps once every lane is inside its line: all loads of a
@@ -138,8 +131,6 @@ __global__ void __launch_bounds__(SW_LANES)
   const double isd = (a.in_scale_dev != nullptr) ? *a.in_scale_dev : a.in_scale;
   const int in_exp = pow2_exp(isd);
   const TC in_scale = (TC)isd;
-  const double osd = (a.out_scale_dev != nullptr) ? *a.out_scale_dev : a.out_scale;
-  const int out_exp = pow2_exp(osd);
 
   constexpr int V = 16 / (int)sizeof(TIn);          // elements per 16-byte copy
   const int nv = LS / V;                             // copies per line
@@ -267,9 +258,7 @@ __global__ void __launch_bounds__(SW_LANES)
     //      transposed into the output ring (row i mod 128).  Chunk c is
     //      complete right after step L-1-c*CH+31 (lane 31 passes its lowest
     //      position); the loop runs in segments that end at those steps. ----
-    if (MODE == 0 || MODE == 3) {
-      if (j == 0) bulk_wait_read<0>();  // the previous tile's stores are done reading the ring
-    }
+    if (j == 0) bulk_wait_read<0>();  // the previous tile's stores are done reading the ring
     __syncwarp();
     {
       constexpr int RMASK = SW_RING * SW_CH - 1;
@@ -291,33 +280,6 @@ __global__ void __launch_bounds__(SW_LANES)
           nxt[0] = x;
         }
         T[((i & RMASK) << 5) + j] = x;
-      };
-      // Mode 1 (final z sweep): lanes are x, positions are z, t3 is y; a
-      // completed chunk's rows (32 x each, coalesced) go out a few at a time
-      // during the following blocks of steps, so the conversions and stores
-      // fill issue slots the dependent recurrence leaves idle.  Each lane
-      // writes and reads only its own column of the ring slot.
-      const int xo = lane_base + j;
-      const bool xin = xo < a.lanes_total;
-      double* const ocol = a.out + (size_t)xo + (size_t)a.out_pitch * (size_t)t3;
-      int pend = -1, prow = 0, prows = 0;  // chunk being written out, next row, its row count
-      const size_t os = (size_t)a.out_slice;
-      auto emit8 = [&]() {  // the next 8 rows of the pending chunk
-        if constexpr (MODE == 1) {
-          if (pend < 0) return;
-          const TC* src = T + (pend & (SW_RING - 1)) * (SW_CH * SW_LANES) + prow * SW_LANES + j;
-          double* q = ocol + os * (size_t)(pend * SW_CH + prow);
-#pragma unroll
-          for (int t = 0; t < 8; ++t) {
-            if (xin && prow + t < prows) *q = out_value<TC>(src[t * SW_LANES], out_exp);
-            q += os;
-          }
-          prow += 8;
-          if (prow >= prows) pend = -1;
-        }
-      };
-      auto emit_rows = [&](int n) {
-        for (int k = 0; k < n; k += 8) emit8();
       };
       int s = 0;
       for (int c = nchunk - 1; c >= 0; --c) {
@@ -356,7 +318,6 @@ __global__ void __launch_bounds__(SW_LANES)
             }
 #pragma unroll
             for (int t = 0; t < SW_BLK; ++t) T[(((i0 - t) & RMASK) << 5) + j] = yv[t];
-            emit_rows(SW_BLK);
             s += SW_BLK;
           } else if (s + SW_BLK <= sb) {
             // ramp block: lanes outside their line read a clamped position,
@@ -382,7 +343,6 @@ __global__ void __launch_bounds__(SW_LANES)
               }
               if (act) T[((ic & RMASK) << 5) + j] = x;
             }
-            emit_rows(SW_BLK);
             s += SW_BLK;
           } else {
             const int i = L - 1 - (s - j);
@@ -391,32 +351,21 @@ __global__ void __launch_bounds__(SW_LANES)
           }
         }
         TC* slot = T + (c & (SW_RING - 1)) * (SW_CH * SW_LANES);
-        if (MODE == 0 || MODE == 3) {
-          fence_proxy_async();
-          __syncwarp();
-          if (j == 0) {
-            if (a.out_line_dim == 1) tma_store_3d(&tmout, lane_base, c * SW_CH, t3, slot);
-            else tma_store_3d(&tmout, lane_base, t3, c * SW_CH, slot);
-            bulk_commit();
-            // lane 0 enters chunk c-2 two steps after this event; its slot was
-            // last stored from for chunk c+2, two commits ago
-            bulk_wait_read<SW_RING - 2>();
-          }
-          __syncwarp();
-        } else {
-          // finish the previous chunk's rows, then queue this one
-          emit_rows(SW_CH);
-          pend = c;
-          prow = 0;
-          prows = min(SW_CH, L - c * SW_CH);
+        fence_proxy_async();
+        __syncwarp();
+        if (j == 0) {
+          if (a.out_line_dim == 1) tma_store_3d(&tmout, lane_base, c * SW_CH, t3, slot);
+          else tma_store_3d(&tmout, lane_base, t3, c * SW_CH, slot);
+          bulk_commit();
+          // lane 0 enters chunk c-2 two steps after this event; its slot was
+          // last stored from for chunk c+2, two commits ago
+          bulk_wait_read<SW_RING - 2>();
         }
+        __syncwarp();
       }
-      emit_rows(SW_CH);
     }
   }
-  if (MODE == 0 || MODE == 3) {
-    if (j == 0) bulk_wait_all();
-  }
+  if (j == 0) bulk_wait_all();
   __syncwarp();
 }
 
@@ -451,10 +400,11 @@ template <int P>
 static cudaError_t launch_mode(int tin, int tc, int mode, bool trans, const CUtensorMap* tmout,
                                const SweepArgs& a, int grid, cudaStream_t s) {
   switch (mode) {
-    case 0: return trans ? launch_types<P, 0, true>(tin, tc, tmout, a, grid, s)
-                         : launch_types<P, 0, false>(tin, tc, tmout, a, grid, s);
-    case 1: return trans ? launch_types<P, 1, true>(tin, tc, tmout, a, grid, s)
-                         : launch_types<P, 1, false>(tin, tc, tmout, a, grid, s);
+    case 0:
+      if (!trans) return launch_types<P, 0, false>(tin, tc, tmout, a, grid, s);
+      // the transposed solve (adjoint) is FP64 only
+      if (tin == 0 && tc == 0) return launch_t<double, double, P, 0, true>(tmout, a, grid, s);
+      return cudaErrorInvalidValue;
     case 3: return launch_types<P, 3, false>(tin, tc, tmout, a, grid, s);
   }
   return cudaErrorInvalidValue;
