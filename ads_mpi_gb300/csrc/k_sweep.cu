@@ -65,20 +65,63 @@ constexpr int SW_RING = 4;       // transposed output chunks per warp (power of 
 constexpr int SW_GROUPS = 4;     // position groups of the staged input
 constexpr int SW_BLK = 32;       // steps per software-pipelined block
 
+// The factors of one position packed for one vector load per step: forward
+// (f1..fP) in KF entries, backward (bs, g1..gP) in KB entries (powers of two),
+// plus the forward scales fs as a row of their own (transposed solve only).
+__host__ __device__ constexpr int sw_kf(int P) { return P <= 1 ? 1 : (P <= 2 ? 2 : 4); }
+__host__ __device__ constexpr int sw_kb(int P) { return P + 1 <= 2 ? 2 : (P + 1 <= 4 ? 4 : 8); }
+
 // Shared memory of one CTA (one warp): staged lines S[32][LS] (TIn), the
-// output ring T[SW_RING * 32 positions][32 lines] (TC), the factor rows
-// ((2P+2) x L, TC).  LS = L rounded up to a multiple of 4: even (so the skewed
-// accesses are conflict-free) and a whole number of 16-byte copies.
+// output ring T[SW_RING * 32 positions][32 lines] (TC), the packed factors
+// (KF + KB + 1 entries per position, TC).  LS = L rounded up to a multiple of
+// 4: even (so the skewed accesses are conflict-free) and a whole number of
+// 16-byte copies.
 template <typename TIn, typename TC>
 struct SweepSmem {
   __host__ __device__ static int ls(int L) { return (L + 3) / 4 * 4; }
   __host__ __device__ static size_t s_bytes(int L) { return sizeof(TIn) * (size_t)SW_LANES * ls(L); }
   __host__ __device__ static size_t t_bytes() { return sizeof(TC) * (size_t)SW_LANES * SW_CH * SW_RING; }
-  __host__ __device__ static size_t f_bytes(int P, int L) {
-    return (sizeof(TC) * (size_t)(2 * P + 2) * L + 15) / 16 * 16;
+  // forward vectors, then backward vectors (16-byte aligned), then fs
+  __host__ __device__ static size_t fw_bytes(int P, int L) {
+    return (sizeof(TC) * (size_t)sw_kf(P) * L + 15) / 16 * 16;
   }
-  __host__ __device__ static size_t total(int P, int L) { return 128 + s_bytes(L) + t_bytes() + f_bytes(P, L); }
+  __host__ __device__ static size_t bw_bytes(int P, int L) {
+    return (sizeof(TC) * (size_t)sw_kb(P) * L + 15) / 16 * 16;
+  }
+  __host__ __device__ static size_t f_bytes(int P, int L, bool trans) {
+    return fw_bytes(P, L) + bw_bytes(P, L) + (trans ? (sizeof(TC) * (size_t)L + 15) / 16 * 16 : 0);
+  }
+  __host__ __device__ static size_t total(int P, int L, bool trans) {
+    return 128 + s_bytes(L) + t_bytes() + f_bytes(P, L, trans);
+  }
 };
+
+// K consecutive entries as one or more 8/16-byte loads (p aligned to their size)
+template <typename TC, int K>
+__device__ __forceinline__ void sw_ldk(const TC* p, TC (&v)[K]) {
+  constexpr int B = (int)sizeof(TC) * K;
+  if constexpr (B == 4) {
+    v[0] = p[0];
+  } else if constexpr (B == 8) {
+    if constexpr (sizeof(TC) == 4) {
+      const float2 t = *reinterpret_cast<const float2*>(p);
+      v[0] = t.x; v[1] = t.y;
+    } else {
+      v[0] = p[0];
+    }
+  } else {
+#pragma unroll
+    for (int h = 0; h < B / 16; ++h) {
+      if constexpr (sizeof(TC) == 4) {
+        const float4 t = reinterpret_cast<const float4*>(p)[h];
+        v[4 * h] = t.x; v[4 * h + 1] = t.y; v[4 * h + 2] = t.z; v[4 * h + 3] = t.w;
+      } else {
+        const double2 t = reinterpret_cast<const double2*>(p)[h];
+        v[2 * h] = t.x; v[2 * h + 1] = t.y;
+      }
+    }
+  }
+}
 
 // An input of the compute type is used as it is (launch_sweep rejects an
 // input scale for it); an FP64 input of an FP32 solve is scaled by 2^sexp.
@@ -120,11 +163,21 @@ __global__ void __launch_bounds__(SW_LANES)
   unsigned char* p0 = smem_dyn + pad;
   TIn* S = reinterpret_cast<TIn*>(p0);
   TC* T = reinterpret_cast<TC*>(p0 + SM::s_bytes(L));
-  TC* Fs = reinterpret_cast<TC*>(p0 + SM::s_bytes(L) + SM::t_bytes());
+  constexpr int KF = sw_kf(P), KB = sw_kb(P);
+  TC* FW = reinterpret_cast<TC*>(p0 + SM::s_bytes(L) + SM::t_bytes());  // [L][KF]: f1..fP
+  TC* BW = reinterpret_cast<TC*>(reinterpret_cast<unsigned char*>(FW) + SM::fw_bytes(P, L));  // [L][KB]: bs, g
+  TC* FS = reinterpret_cast<TC*>(reinterpret_cast<unsigned char*>(BW) + SM::bw_bytes(P, L));  // [L]: fs (TRANS)
 
   if (MODE != 3) {
+    // factor rows (global [row][L]): 0 fs, 1..P f, P+1 bs, P+2..2P+1 g
     const TC* fac = static_cast<const TC*>(a.fac);
-    for (int idx = j; idx < (2 * P + 2) * L; idx += SW_LANES) Fs[idx] = fac[idx];
+    for (int i = j; i < L; i += SW_LANES) {
+#pragma unroll
+      for (int m = 0; m < KF; ++m) FW[(size_t)i * KF + m] = (m < P) ? fac[(size_t)(1 + m) * L + i] : TC(0);
+#pragma unroll
+      for (int m = 0; m < KB; ++m) BW[(size_t)i * KB + m] = (m <= P) ? fac[(size_t)(P + 1 + m) * L + i] : TC(0);
+      if (TRANS) FS[i] = fac[i];
+    }
   }
   __syncwarp();
 
@@ -176,9 +229,11 @@ __global__ void __launch_bounds__(SW_LANES)
       auto fstep = [&](int i) {
         TIn* yp = Sj + i;
         const TC b = load_in<TC>(*yp, in_exp, in_scale);
-        TC y = TRANS ? Fs[i] * b : b;
+        TC f[KF];
+        sw_ldk<TC, KF>(FW + (size_t)i * KF, f);
+        TC y = TRANS ? FS[i] * b : b;
 #pragma unroll
-        for (int m = P; m >= 1; --m) y -= Fs[m * L + i] * prev[m - 1];
+        for (int m = P; m >= 1; --m) y -= f[m - 1] * prev[m - 1];
 #pragma unroll
         for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
         prev[0] = y;
@@ -201,20 +256,18 @@ __global__ void __launch_bounds__(SW_LANES)
           if (s >= RAMP && s + SW_BLK <= sbl) {
             const int i0 = s - j;
             TIn* yp = Sj + i0;
-            const TC* fp = Fs + i0;
-            TC bv[SW_BLK], fv[SW_BLK][P + 1];
+            TC bv[SW_BLK], fv[SW_BLK][KF], fsv[SW_BLK];
 #pragma unroll
             for (int t = 0; t < SW_BLK; ++t) {
               bv[t] = load_in<TC>(yp[t], in_exp, in_scale);
-              fv[t][0] = TRANS ? fp[t] : TC(1);
-#pragma unroll
-              for (int m = 1; m <= P; ++m) fv[t][m] = fp[m * L + t];
+              sw_ldk<TC, KF>(FW + (size_t)(i0 + t) * KF, fv[t]);
+              fsv[t] = TRANS ? FS[i0 + t] : TC(1);
             }
 #pragma unroll
             for (int t = 0; t < SW_BLK; ++t) {
-              TC y = TRANS ? fv[t][0] * bv[t] : bv[t];
+              TC y = TRANS ? fsv[t] * bv[t] : bv[t];
 #pragma unroll
-              for (int m = P; m >= 1; --m) y -= fv[t][m] * prev[m - 1];
+              for (int m = P; m >= 1; --m) y -= fv[t][m - 1] * prev[m - 1];
 #pragma unroll
               for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
               prev[0] = y;
@@ -232,9 +285,11 @@ __global__ void __launch_bounds__(SW_LANES)
               const bool act = (i >= 0) && (i < L);
               const int ic = min(max(i, 0), L - 1);
               const TC b = load_in<TC>(Sj[ic], in_exp, in_scale);
-              TC y = TRANS ? Fs[ic] * b : b;
+              TC f[KF];
+              sw_ldk<TC, KF>(FW + (size_t)ic * KF, f);
+              TC y = TRANS ? FS[ic] * b : b;
 #pragma unroll
-              for (int m = P; m >= 1; --m) y -= Fs[m * L + ic] * prev[m - 1];
+              for (int m = P; m >= 1; --m) y -= f[m - 1] * prev[m - 1];
               y = act ? y : TC(0);
 #pragma unroll
               for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
@@ -265,16 +320,17 @@ __global__ void __launch_bounds__(SW_LANES)
       TC nxt[P];
 #pragma unroll
       for (int m = 0; m < P; ++m) nxt[m] = TC(0);
-      const TC* BS = Fs + (P + 1) * L;
       auto bstep = [&](int i) {
         TC x;
         if (MODE == 3) {
           x = load_in<TC>(Sj[i], 0, TC(1));
         } else {
           const TC y = load_y<TC>(Sj + i);
-          x = TRANS ? y : BS[i] * y;
+          TC gb[KB];
+          sw_ldk<TC, KB>(BW + (size_t)i * KB, gb);
+          x = TRANS ? y : gb[0] * y;
 #pragma unroll
-          for (int m = P; m >= 1; --m) x -= BS[m * L + i] * nxt[m - 1];
+          for (int m = P; m >= 1; --m) x -= gb[m] * nxt[m - 1];
 #pragma unroll
           for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
           nxt[0] = x;
@@ -290,7 +346,6 @@ __global__ void __launch_bounds__(SW_LANES)
           if (s >= RAMP && s + SW_BLK <= sbl) {
             const int i0 = L - 1 - (s - j);
             const TIn* yp = Sj + i0;
-            const TC* gp = BS + i0;
             TC yv[SW_BLK];
 #pragma unroll
             for (int t = 0; t < SW_BLK; ++t) {
@@ -298,13 +353,9 @@ __global__ void __launch_bounds__(SW_LANES)
               else yv[t] = load_y<TC>(yp - t);
             }
             if (MODE != 3) {
-              TC gv[SW_BLK][P + 1];
+              TC gv[SW_BLK][KB];
 #pragma unroll
-              for (int t = 0; t < SW_BLK; ++t) {
-                gv[t][0] = TRANS ? TC(1) : gp[-t];
-#pragma unroll
-                for (int m = 1; m <= P; ++m) gv[t][m] = gp[m * L - t];
-              }
+              for (int t = 0; t < SW_BLK; ++t) sw_ldk<TC, KB>(BW + (size_t)(i0 - t) * KB, gv[t]);
 #pragma unroll
               for (int t = 0; t < SW_BLK; ++t) {
                 TC x = TRANS ? yv[t] : gv[t][0] * yv[t];
@@ -333,9 +384,11 @@ __global__ void __launch_bounds__(SW_LANES)
                 x = load_in<TC>(Sj[ic], 0, TC(1));
               } else {
                 const TC y = load_y<TC>(Sj + ic);
-                x = TRANS ? y : BS[ic] * y;
+                TC gb[KB];
+                sw_ldk<TC, KB>(BW + (size_t)ic * KB, gb);
+                x = TRANS ? y : gb[0] * y;
 #pragma unroll
-                for (int m = P; m >= 1; --m) x -= BS[m * L + ic] * nxt[m - 1];
+                for (int m = P; m >= 1; --m) x -= gb[m] * nxt[m - 1];
                 x = act ? x : TC(0);
 #pragma unroll
                 for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
@@ -372,7 +425,7 @@ __global__ void __launch_bounds__(SW_LANES)
 template <typename TIn, typename TC, int P, int MODE, bool TRANS>
 static cudaError_t launch_t(const CUtensorMap* tmout, const SweepArgs& a, int grid, cudaStream_t s) {
   auto kern = k_sweep<TIn, TC, P, MODE, TRANS>;
-  const size_t bytes = SweepSmem<TIn, TC>::total(P, a.L);
+  const size_t bytes = SweepSmem<TIn, TC>::total(P, a.L, TRANS);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e != cudaSuccess) return e;
   // persistent: as many CTAs as fit at once, each looping over tiles
@@ -411,9 +464,9 @@ static cudaError_t launch_mode(int tin, int tc, int mode, bool trans, const CUte
 }
 
 size_t sweep_smem_bytes(int tin, int tc, int P, int L) {
-  if (tin == 0 && tc == 0) return SweepSmem<double, double>::total(P, L);
-  if (tin == 0 && tc == 1) return SweepSmem<double, float>::total(P, L);
-  return SweepSmem<float, float>::total(P, L);
+  if (tin == 0 && tc == 0) return SweepSmem<double, double>::total(P, L, true);
+  if (tin == 0 && tc == 1) return SweepSmem<double, float>::total(P, L, false);
+  return SweepSmem<float, float>::total(P, L, false);
 }
 
 cudaError_t launch_sweep(int P, int tin, int tc, int mode, bool trans, const CUtensorMap* tmout,
