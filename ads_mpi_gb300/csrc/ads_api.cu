@@ -111,6 +111,7 @@ struct ads_handle {
   // launch geometry
   int asm_grid = 0, asm_zc = 0, asm_nix = 0, asm_niy = 0, asm_niz = 0;
   int res_grid = 0, res_zc = 0, res_nix = 0, res_niy = 0, res_niz = 0;
+  int upd_grid = 0, upd_niy = 0;  // k_resid_update: the x and z tiling of res_*, its own rows
   int norm_parts = 0;
 
   // tensor maps
@@ -438,7 +439,7 @@ int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready, bool f32_in
   UpdateArgs ua{};
   ua.g = h->g;
   ua.zc = h->res_zc;
-  ua.nix = h->res_nix; ua.niy = h->res_niy; ua.niz = h->res_niz;
+  ua.nix = h->res_nix; ua.niy = h->upd_niy; ua.niz = h->res_niz;
   ua.x1 = h->d_x32;
   ua.r1 = h->d_g32;
   ua.delta = x;
@@ -451,8 +452,8 @@ int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready, bool f32_in
     if ((st = residual(k == 0))) return st;
     RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, true, k == 0, h->d_scal, h->d_flags, h->stream));
     if ((st = enqueue_solve32(h, h->d_g32, 1, nullptr, nullptr, 0, conv, "_corr", nullptr))) return st;
-    RUN(h, "resid_update", 1, launch_resid_update(h->P, ua, h->res_grid, h->stream));
-    RUN(h, "certify", 1, launch_certify(h->d_part, h->res_grid, h->P, ndof, h->opts.refine_tol, h->d_scal,
+    RUN(h, "resid_update", 1, launch_resid_update(h->P, ua, h->upd_grid, h->stream));
+    RUN(h, "certify", 1, launch_certify(h->d_part, h->upd_grid, h->P, ndof, h->opts.refine_tol, h->d_scal,
                                         h->d_flags, h->stream));
   }
   if ((st = residual(h->opts.max_refine == 0))) return st;
@@ -686,6 +687,8 @@ int create_impl(ads_handle* h) {
     h->res_zc = std::min(g.N[2], 32);
     h->res_niz = (g.N[2] + h->res_zc - 1) / h->res_zc;
     h->res_grid = h->res_nix * h->res_niy * h->res_niz;
+    h->upd_niy = (g.N[1] + resid_update_rows() - 1) / resid_update_rows();
+    h->upd_grid = h->res_nix * h->upd_niy * h->res_niz;
   }
   {
     // spill-slab membership of each DOF index (the assembly's bricks spill the
@@ -705,7 +708,7 @@ int create_impl(ads_handle* h) {
     if (!xs.empty()) ADS_CUDA(h, cudaMemcpy(h->d_xslab, xs.data(), sizeof(int) * xs.size(), cudaMemcpyHostToDevice));
   }
   h->norm_parts = 4 * nsm;
-  h->npart = std::max(3 * h->res_grid, 2 * h->norm_parts);
+  h->npart = std::max(3 * std::max(h->res_grid, h->upd_grid), 2 * h->norm_parts);
   if ((st = zalloc(&h->d_l2part, 3 * (size_t)h->asm_grid))) return st;
   if ((st = zalloc(&h->d_part, (size_t)h->npart))) return st;
   if ((st = zalloc(&h->d_scal, SC_COUNT))) return st;

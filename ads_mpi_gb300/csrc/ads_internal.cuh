@@ -222,6 +222,8 @@ cudaError_t launch_residual(int P, const ResidualArgs& a, int grid, cudaStream_t
 cudaError_t launch_decide(const double* part, int n, double tol, bool count_iter, bool use_ff, double* scal,
                           int* flags, cudaStream_t s);
 cudaError_t launch_resid_update(int P, const UpdateArgs& a, int grid, cudaStream_t s);
+// DOF rows (y) of one k_resid_update tile; its x width is RS_TX, its z chunk UpdateArgs::zc
+int resid_update_rows();
 // from the k_resid_update partials: SC_RELRES = an upper bound of ||F - M x|| / ||F||
 // after the correction, FL_CONV if it is <= tol.  Skipped when FL_CONV is set.
 cudaError_t launch_certify(const double* part, int n, int P, long long ndof, double tol, double* scal, int* flags,

@@ -242,30 +242,35 @@ __device__ __forceinline__ void ru_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// The kernel is bandwidth-light per plane, so its planes are staged ahead:
-// a ring of RU_RING halo planes of x1 (and each thread's r1 entry of the
-// matching output plane) is filled by cp.async RU_PD(P) planes ahead of the
-// one being reduced.  Halo entries outside the grid stay zero (set once).
+// The planes are staged ahead: a ring of RU_RING halo planes of x1 (and each
+// thread's r1 entries of the matching output plane) is filled by cp.async
+// RU_PD planes ahead of the one being reduced.  Halo entries outside the grid
+// stay zero (set once).  A CTA owns 32 x RU_TY DOF columns, each thread two
+// rows (ty and ty + 8), so the per-plane work of the staging, the barriers
+// and the loop is shared by two outputs.
 constexpr int RU_RING = 8;
-__host__ __device__ constexpr int ru_pd(int P) { return (7 - P) < 4 ? (7 - P) : 4; }
+constexpr int RU_PD = 3;
+constexpr int RU_RPT = 2;                          // DOF rows per thread
+constexpr int RU_TY = RU_RPT * (RS_THREADS / RS_TX);  // 16 rows per CTA
 
 template <int P>
-__global__ void __launch_bounds__(RS_THREADS) k_resid_update(const UpdateArgs a) {
+__global__ void __launch_bounds__(RS_THREADS, (P <= 2 ? 3 : 2)) k_resid_update(const UpdateArgs a) {
   constexpr int W = 2 * P + 1;
-  constexpr int HX = RS_TX + 2 * P, HY = RS_TY + 2 * P;
-  constexpr int PD = ru_pd(P);
+  constexpr int HX = RS_TX + 2 * P, HY = RU_TY + 2 * P;
+  constexpr int PD = RU_PD;
   // a slot is refilled PD planes ahead; it must not be one that is read while
   // the refill is in flight: the plane being reduced (zin) or the output
   // plane's centre (zin - P)
   static_assert(PD >= 1 && PD + P <= RU_RING - 1, "prefetch distance");
   // r1 of an output plane is in flight for PD rounds and read by its own thread
-  constexpr int R1R = (PD + 1 <= 4) ? 4 : 8;
-  constexpr int NYI = (RS_TY * HX + RS_THREADS - 1) / RS_THREADS;  // y-pass items per thread
+  constexpr int R1R = 4;
+  static_assert(PD + 1 <= R1R, "r1 ring");
+  constexpr int NYI = (RU_TY * HX + RS_THREADS - 1) / RS_THREADS;  // y-pass items per thread
   constexpr int NH = (HY * HX + RS_THREADS - 1) / RS_THREADS;      // halo entries per thread
   constexpr int ZMAX = 32 + 2 * P;                                  // input planes of a chunk (zc <= 32)
   __shared__ float xin[RU_RING][HY * HX];
-  __shared__ float r1s_[R1R][RS_THREADS];
-  __shared__ float bys[RS_TY * HX], bya[RS_TY * HX];
+  __shared__ float r1s_[R1R][RU_RPT][RS_THREADS];
+  __shared__ float bys[RU_TY * HX], bya[RU_TY * HX];
   __shared__ float cz[ZMAX * W];  // cz[(zin - z0 + P) * W + j] = Mz(zin - P + j, zin), 0 outside the grid
   __shared__ double red[3][RS_THREADS / 32];
 
@@ -275,13 +280,19 @@ __global__ void __launch_bounds__(RS_THREADS) k_resid_update(const UpdateArgs a)
   const int tid = threadIdx.x, tx = tid % RS_TX, ty = tid / RS_TX;
   const int item = blockIdx.x;
   const int ix = item % a.nix, iy = (item / a.nix) % a.niy, iz = item / (a.nix * a.niy);
-  const int x0 = ix * RS_TX, y0 = iy * RS_TY, z0 = iz * a.zc;
+  const int x0 = ix * RS_TX, y0 = iy * RU_TY, z0 = iz * a.zc;
   const int z1 = min(z0 + a.zc, Nz);
   const int out_exp = pow2_exp(*a.out_scale);
   const size_t plane = (size_t)g.PX * Ny;
-  const int xo = x0 + tx, yo = y0 + ty;
-  const bool own = xo < Nx && yo < Ny;
-  const size_t ocol = own ? (size_t)xo + (size_t)g.PX * yo : 0;
+  const int xo = x0 + tx;
+  bool own[RU_RPT];
+  size_t ocol[RU_RPT];
+#pragma unroll
+  for (int r = 0; r < RU_RPT; ++r) {
+    const int yo = y0 + ty + r * (RS_THREADS / RS_TX);
+    own[r] = xo < Nx && yo < Ny;
+    ocol[r] = own[r] ? (size_t)xo + (size_t)g.PX * yo : 0;
+  }
 
   for (int it = tid; it < RU_RING * HY * HX; it += RS_THREADS) (&xin[0][0])[it] = 0.f;
   for (int it = tid; it < (z1 - z0 + 2 * P) * W; it += RS_THREADS) {
@@ -301,7 +312,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_resid_update(const UpdateArgs a)
     const int it = tid + k * RS_THREADS;
     const int yy = it / HX, hx = it % HX;
     const int y = y0 + yy;
-    yact[k] = it < RS_TY * HX;
+    yact[k] = it < RU_TY * HX;
     yoff[k] = yact[k] ? yy * HX + hx : 0;
 #pragma unroll
     for (int m = 0; m < W; ++m) byc[k][m] = (yact[k] && y < Ny) ? a.band[1][(size_t)m * Ny + y] : 0.f;
@@ -310,8 +321,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_resid_update(const UpdateArgs a)
 #pragma unroll
   for (int m = 0; m < W; ++m) mx[m] = (xo < Nx) ? a.band[0][(size_t)m * Nx + xo] : 0.f;
 
-  // this thread's halo entries and their columns
-  size_t hcol[NH];
+  // this thread's halo entries: their source pointers in plane 0, advanced one
+  // plane per fetch
+  const float* hsrc[NH];
   bool hok[NH];
 #pragma unroll
   for (int k = 0; k < NH; ++k) {
@@ -319,7 +331,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_resid_update(const UpdateArgs a)
     const int hy = it / HX, hx = it % HX;
     const int x = x0 - P + hx, y = y0 - P + hy;
     hok[k] = it < HY * HX && x >= 0 && x < Nx && y >= 0 && y < Ny;
-    hcol[k] = hok[k] ? (size_t)x + (size_t)g.PX * y : 0;
+    hsrc[k] = a.x1 + (hok[k] ? (size_t)x + (size_t)g.PX * y : 0);
   }
   __syncthreads();
 
@@ -332,22 +344,29 @@ __global__ void __launch_bounds__(RS_THREADS) k_resid_update(const UpdateArgs a)
       const size_t po = plane * (size_t)q;
 #pragma unroll
       for (int k = 0; k < NH; ++k)
-        if (hok[k]) ru_cp4(&xin[sl][tid + k * RS_THREADS], a.x1 + hcol[k] + po);
+        if (hok[k]) ru_cp4(&xin[sl][tid + k * RS_THREADS], hsrc[k] + po);
     }
     const int qo = q - P;
-    if (own && qo >= z0 && qo < z1) ru_cp4(&r1s_[qo & (R1R - 1)][tid], a.r1 + ocol + plane * (size_t)qo);
+    if (qo >= z0 && qo < z1) {
+      const size_t po = plane * (size_t)qo;
+#pragma unroll
+      for (int r = 0; r < RU_RPT; ++r)
+        if (own[r]) ru_cp4(&r1s_[qo & (R1R - 1)][r][tid], a.r1 + ocol[r] + po);
+    }
     ru_commit();
   };
 
-  // acc[j]: partial sums of output plane zin - P + j (value and |.| channel)
-  float acs[W], act[W];
+  // acc[r][j]: partial sums of output plane zin - P + j of row r (value and |.| channel)
+  float acs[RU_RPT][W], act[RU_RPT][W];
 #pragma unroll
-  for (int j = 0; j < W; ++j) { acs[j] = 0.f; act[j] = 0.f; }
+  for (int r = 0; r < RU_RPT; ++r)
+#pragma unroll
+    for (int j = 0; j < W; ++j) { acs[r][j] = 0.f; act[r][j] = 0.f; }
   float rr = 0.f, aa = 0.f, r1q = 0.f;
 
 #pragma unroll 1
   for (int k = 0; k < PD; ++k) fetch(z0 - P + k);
-#pragma unroll 1
+#pragma unroll W
   for (int zin = z0 - P; zin < z1 + P; ++zin) {
     ru_wait<PD - 1>();  // plane zin has landed (this thread's copies)
     __syncthreads();    // ... and everyone's; the slots read last round are free
@@ -369,35 +388,48 @@ __global__ void __launch_bounds__(RS_THREADS) k_resid_update(const UpdateArgs a)
         }
       }
       __syncthreads();
-      float sv = 0.f, tv = 0.f;
-#pragma unroll
-      for (int m = 0; m < W; ++m) {
-        sv = fmaf(mx[m], bys[ty * HX + tx + m], sv);
-        tv = fmaf(mx[m], bya[ty * HX + tx + m], tv);
-      }
       const float* c = cz + (zin - z0 + P) * W;
 #pragma unroll
-      for (int j = 0; j < W; ++j) {
-        acs[j] = fmaf(c[j], sv, acs[j]);
-        act[j] = fmaf(c[j], tv, act[j]);
+      for (int r = 0; r < RU_RPT; ++r) {
+        const int row = ty + r * (RS_THREADS / RS_TX);
+        float sv = 0.f, tv = 0.f;
+#pragma unroll
+        for (int m = 0; m < W; ++m) {
+          sv = fmaf(mx[m], bys[row * HX + tx + m], sv);
+          tv = fmaf(mx[m], bya[row * HX + tx + m], tv);
+        }
+#pragma unroll
+        for (int j = 0; j < W; ++j) {
+          acs[r][j] = fmaf(c[j], sv, acs[r][j]);
+          act[r][j] = fmaf(c[j], tv, act[r][j]);
+        }
       }
     }
     const int zout = zin - P;  // complete now
-    if (zout >= z0 && zout < z1 && own) {
-      const float r1 = r1s_[zout & (R1R - 1)][tid];
-      const float x1 = xin[zout & (RU_RING - 1)][(ty + P) * HX + tx + P];
-      const float r2 = (r1 - acs[0]) * 16777216.f;  // 2^24: keeps the squares of a converged residual normal
-      rr = fmaf(r2, r2, rr);
-      aa = fmaf(act[0], act[0], aa);
-      r1q = fmaf(r1, r1, r1q);
-      // a reduction performed at L2: neither a load of the old value nor an
-      // FP64 add on this SM; each entry receives exactly one add
-      atomicAdd(a.delta + ocol + plane * (size_t)zout, f2d_scaled(x1, out_exp));
+    if (zout >= z0 && zout < z1) {
+#pragma unroll
+      for (int r = 0; r < RU_RPT; ++r) {
+        if (own[r]) {
+          const int row = ty + r * (RS_THREADS / RS_TX);
+          const float r1 = r1s_[zout & (R1R - 1)][r][tid];
+          const float x1 = xin[zout & (RU_RING - 1)][(row + P) * HX + tx + P];
+          const float r2 = (r1 - acs[r][0]) * 16777216.f;  // 2^24: keeps the squares of a converged residual normal
+          rr = fmaf(r2, r2, rr);
+          aa = fmaf(act[r][0], act[r][0], aa);
+          r1q = fmaf(r1, r1, r1q);
+          // a reduction performed at L2: neither a load of the old value nor an
+          // FP64 add on this SM; each entry receives exactly one add
+          atomicAdd(a.delta + ocol[r] + plane * (size_t)zout, f2d_scaled(x1, out_exp));
+        }
+      }
     }
 #pragma unroll
-    for (int j = 0; j < W - 1; ++j) { acs[j] = acs[j + 1]; act[j] = act[j + 1]; }
-    acs[W - 1] = 0.f;
-    act[W - 1] = 0.f;
+    for (int r = 0; r < RU_RPT; ++r) {
+#pragma unroll
+      for (int j = 0; j < W - 1; ++j) { acs[r][j] = acs[r][j + 1]; act[r][j] = act[r][j + 1]; }
+      acs[r][W - 1] = 0.f;
+      act[r][W - 1] = 0.f;
+    }
   }
   ru_wait<0>();
   double d0 = f2d_scaled(rr, -48), d1 = f2d_scaled(aa, 0), d2 = f2d_scaled(r1q, 0);
@@ -418,6 +450,8 @@ __global__ void __launch_bounds__(RS_THREADS) k_resid_update(const UpdateArgs a)
     a.part[3 * blockIdx.x + 2] = s2;
   }
 }
+
+int resid_update_rows() { return RU_TY; }
 
 cudaError_t launch_resid_update(int P, const UpdateArgs& a, int grid, cudaStream_t s) {
   switch (P) {

@@ -45,7 +45,7 @@ NCU_TRAFFIC = {
     ("assemble_f32", "heat256p2"): 164.389888e6 + 163.244544e6,
     ("assemble_f64", "heat256p2"): 167.988992e6 + 164.684544e6,
     ("residual_f64", "heat256p2"): 291.368960e6 + 57.232128e6,
-    ("resid_update", "heat256p2"): 280.506368e6 + 92.415488e6,
+    ("resid_update", "heat256p2"): 280.538112e6 + 91.008256e6,
     ("fixup", "heat256p2"): 272.985600e6 + 90.721024e6,
     ("sweep_x_f32", "heat256p2"): 71.094016e6 + 25.629184e6,
     ("sweep_y_f32", "heat256p2"): 71.095808e6 + 25.124864e6,
