@@ -30,6 +30,8 @@ namespace ads {
 constexpr int CS_BLK = 16;        // steps per software-pipelined block
 constexpr int CS_GROUPS = 4;      // position groups of the staged input
 constexpr int CS_MAX_WARPS = 8;
+constexpr int CS_TAIL_BLKS = 3;   // blocks at the end of a line held in registers
+constexpr int CS_SROW = 32;       // floats per staged row: 128 bytes, 32 lanes on 32 banks
 
 __device__ __forceinline__ unsigned cs_smem_u32(const void* p) {
   return static_cast<unsigned>(__cvta_generic_to_shared(p));
@@ -52,8 +54,16 @@ struct CsTab {
   __host__ __device__ static size_t bytes(int L) { return sizeof(float4) * (size_t)(VF + VB) * L; }
 };
 
-constexpr int CS_SROW = 36;  // floats per staged row: 16-byte aligned, 32 lanes on 32 banks
-size_t csweep_warp_bytes(int L) { return sizeof(float) * (size_t)L * CS_SROW; }
+// The last cs_tail_blocks(L) blocks of every line never touch shared memory:
+// their input rows are loaded into registers at the start of the tile, and
+// their forward results stay there for the backward pass.  The rest, Ls
+// positions, is staged.
+__host__ __device__ inline int cs_tail_blocks(int L) {
+  return (L / CS_BLK < CS_TAIL_BLKS) ? L / CS_BLK : CS_TAIL_BLKS;
+}
+size_t csweep_warp_bytes(int L) {
+  return sizeof(float) * (size_t)(L - CS_BLK * cs_tail_blocks(L)) * CS_SROW;
+}
 
 template <int P, int MODE>
 __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a) {
@@ -61,12 +71,15 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
   if (a.skip_flag != nullptr && *a.skip_flag != 0) return;
   using Tab = CsTab<P>;
   constexpr int VF = Tab::VF, VB = Tab::VB;
+  constexpr int NTB = CS_TAIL_BLKS;
   const int L = a.L;
+  const int nt = cs_tail_blocks(L);
+  const int Ls = L - CS_BLK * nt;  // staged positions [0, Ls); the tail [Ls, L) is in registers
   const int j = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const int srow = CS_SROW;
+  constexpr int srow = CS_SROW;
   float4* FT = reinterpret_cast<float4*>(smem);      // [L][VF]
   float4* BT = FT + (size_t)VF * L;                  // [L][VB]
-  float* S = reinterpret_cast<float*>(smem + Tab::bytes(L)) + (size_t)warp * L * srow;
+  float* S = reinterpret_cast<float*>(smem + Tab::bytes(L)) + (size_t)warp * Ls * srow;
 
   // factor rows (global [row][L]): row 0 fs (1 here), 1..P f, P+1 bs, P+2.. g
   for (int i = threadIdx.x; i < L; i += blockDim.x) {
@@ -86,19 +99,29 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
   const int out_exp = pow2_exp(osd);
   const int tiles_l = (a.nl + 31) / 32;
   const int ntiles = tiles_l * a.n3;
-  const int GP = ((L + CS_GROUPS - 1) / CS_GROUPS + CS_BLK - 1) / CS_BLK * CS_BLK;  // positions per group
+  const int GP = ((Ls + CS_GROUPS - 1) / CS_GROUPS + CS_BLK - 1) / CS_BLK * CS_BLK;  // positions per group
 
   for (int tile = blockIdx.x * nwarps + warp; tile < ntiles; tile += gridDim.x * nwarps) {
     const int tl = tile % tiles_l, t3 = tile / tiles_l;
     const int l0 = tl * 32;
     const int nlv = min(32, a.nl - l0);
+    const bool act = j < nlv;
     const float* src = a.in + (size_t)t3 * a.in_ts + (size_t)l0 * a.in_ls;
+
+    // the tail rows, coalesced, straight into registers (lanes beyond the
+    // tile's lines load nothing); they are first used after the staged part
+    float yt[NTB][CS_BLK];
+#pragma unroll
+    for (int b = 0; b < NTB; ++b)
+#pragma unroll
+      for (int t = 0; t < CS_BLK; ++t)
+        yt[b][t] = (b < nt && act) ? src[(size_t)(Ls + b * CS_BLK + t) * a.in_ps + j] : 0.f;
 
     __syncwarp();  // the previous tile is done with S
     // ---- stage: group g holds positions [g*GP, (g+1)*GP) of every line ----
 #pragma unroll 1
     for (int g = 0; g < CS_GROUPS; ++g) {
-      const int p0 = g * GP, p1 = min(L, p0 + GP);
+      const int p0 = g * GP, p1 = min(Ls, p0 + GP);
       // 16-byte copies of the line-contiguous rows (lines up to a multiple
       // of 4: within the row's padded pitch)
       const int nc = (nlv + 3) / 4;
@@ -111,10 +134,10 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
 
     float* Sj = S + j;
     // ---- forward: y_i = b_i - sum_m f[m]_i y_{i-m}, in place ----
-    {
-      float prev[P];
+    float prev[P];
 #pragma unroll
-      for (int m = 0; m < P; ++m) prev[m] = 0.f;
+    for (int m = 0; m < P; ++m) prev[m] = 0.f;
+    {
       int i = 0;
 #pragma unroll 1
       for (int g = 0; g < CS_GROUPS; ++g) {
@@ -125,7 +148,7 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
           default: cs_wait<0>(); break;
         }
         __syncwarp();
-        const int ie = min(L, (g + 1) * GP);
+        const int ie = min(Ls, (g + 1) * GP);
 #pragma unroll 1
         for (; i + CS_BLK <= ie; i += CS_BLK) {
           float bv[CS_BLK];
@@ -166,28 +189,81 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
         }
       }
     }
+    // the tail, in registers
+#pragma unroll
+    for (int b = 0; b < NTB; ++b) {
+      if (b < nt) {
+        const int i0 = Ls + b * CS_BLK;
+        float4 fv[CS_BLK][VF];
+#pragma unroll
+        for (int t = 0; t < CS_BLK; ++t)
+#pragma unroll
+          for (int v = 0; v < VF; ++v) fv[t][v] = FT[(size_t)(i0 + t) * VF + v];
+#pragma unroll
+        for (int t = 0; t < CS_BLK; ++t) {
+          const float* f = reinterpret_cast<const float*>(fv[t]);
+          float y = yt[b][t];
+#pragma unroll
+          for (int m = P; m >= 1; --m) y -= f[m - 1] * prev[m - 1];
+#pragma unroll
+          for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
+          prev[0] = y;
+          yt[b][t] = y;
+        }
+      }
+    }
 
     // ---- backward: x_i = bs_i y_i - sum_m g[m]_i x_{i+m}; row i goes out ----
-    {
-      const bool act = j < nlv;
-      using TO = typename std::conditional<MODE == 1, double, float>::type;
-      TO* op = static_cast<TO*>(a.out) + (size_t)t3 * a.out_ts + (size_t)(l0 + j);
-      const size_t ops = (size_t)a.out_ps;
-      float nxt[P];
+    using TO = typename std::conditional<MODE == 1, double, float>::type;
+    TO* op = static_cast<TO*>(a.out) + (size_t)t3 * a.out_ts + (size_t)(l0 + j);
+    const size_t ops = (size_t)a.out_ps;
+    float nxt[P];
 #pragma unroll
-      for (int m = 0; m < P; ++m) nxt[m] = 0.f;
-      int i = L;
-      const int rem = L % CS_BLK;
+    for (int m = 0; m < P; ++m) nxt[m] = 0.f;
+    // the tail first, from the registers
+#pragma unroll
+    for (int b = NTB - 1; b >= 0; --b) {
+      if (b < nt) {
+        const int i0 = Ls + b * CS_BLK;
+        float4 bw[CS_BLK][VB];
+#pragma unroll
+        for (int t = 0; t < CS_BLK; ++t)
+#pragma unroll
+          for (int v = 0; v < VB; ++v) bw[t][v] = BT[(size_t)(i0 + t) * VB + v];
+#pragma unroll
+        for (int t = CS_BLK - 1; t >= 0; --t) {
+          const float* c = reinterpret_cast<const float*>(bw[t]);
+          float x = c[0] * yt[b][t];
+#pragma unroll
+          for (int m = P; m >= 1; --m) x -= c[m] * nxt[m - 1];
+#pragma unroll
+          for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
+          nxt[0] = x;
+          yt[b][t] = x;
+        }
+        if (act) {
+#pragma unroll
+          for (int t = CS_BLK - 1; t >= 0; --t) {
+            if constexpr (MODE == 1) op[(size_t)(i0 + t) * ops] = f2d_scaled(yt[b][t], out_exp);
+            else op[(size_t)(i0 + t) * ops] = yt[b][t];
+          }
+        }
+      }
+    }
+    // then the staged part
+    {
+      int i = Ls;
+      const int rem = Ls % CS_BLK;
 #pragma unroll 1
       for (int r = 0; r < rem; ++r) {
         --i;
         float4 bw[VB];
 #pragma unroll
         for (int v = 0; v < VB; ++v) bw[v] = BT[(size_t)i * VB + v];
-        const float* b = reinterpret_cast<const float*>(bw);
-        float x = b[0] * Sj[(size_t)i * srow];
+        const float* c = reinterpret_cast<const float*>(bw);
+        float x = c[0] * Sj[(size_t)i * srow];
 #pragma unroll
-        for (int m = P; m >= 1; --m) x -= b[m] * nxt[m - 1];
+        for (int m = P; m >= 1; --m) x -= c[m] * nxt[m - 1];
 #pragma unroll
         for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
         nxt[0] = x;
@@ -209,10 +285,10 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
         }
 #pragma unroll
         for (int t = CS_BLK - 1; t >= 0; --t) {
-          const float* b = reinterpret_cast<const float*>(bw[t]);
-          float x = b[0] * yv[t];
+          const float* c = reinterpret_cast<const float*>(bw[t]);
+          float x = c[0] * yv[t];
 #pragma unroll
-          for (int m = P; m >= 1; --m) x -= b[m] * nxt[m - 1];
+          for (int m = P; m >= 1; --m) x -= c[m] * nxt[m - 1];
 #pragma unroll
           for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
           nxt[0] = x;
@@ -240,7 +316,7 @@ static cudaError_t launch_cs(const CSweepArgs& a, cudaStream_t s) {
   cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t tab = CsTab<P>::bytes(a.L), per = csweep_warp_bytes(a.L);
   if (tab + per > (size_t)smem_max) return cudaErrorInvalidValue;
-  const int nw = (int)std::min<size_t>(CS_MAX_WARPS, ((size_t)smem_max - tab) / per);
+  const int nw = (per == 0) ? CS_MAX_WARPS : (int)std::min<size_t>(CS_MAX_WARPS, ((size_t)smem_max - tab) / per);
   const size_t bytes = tab + per * nw;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e != cudaSuccess) return e;
