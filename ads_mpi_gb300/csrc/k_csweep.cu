@@ -65,6 +65,46 @@ size_t csweep_warp_bytes(int L) {
   return sizeof(float) * (size_t)(L - CS_BLK * cs_tail_blocks(L)) * CS_SROW;
 }
 
+// A block of 16 solution rows (rows i0 .. i0 + 15 of this lane's line) out:
+// FP32 as it is, or the FP64 state 2^e x.  The row pointer steps by the
+// pitch, one 64-bit add per row.  In FP64 the conversion takes the integer
+// fast path for the whole block (normal floats and zeros; `hi_add` holds
+// (896 + e) << 20 for the exponent, valid for |e| <= 896) and falls back to
+// f2d_scaled for every row if any value is subnormal, infinite or NaN.
+template <int MODE>
+__device__ __forceinline__ void cs_store_block(void* out, size_t i0, size_t ops, const float (&v)[CS_BLK],
+                                               int out_exp, bool fast_ok, unsigned hi_add) {
+  if constexpr (MODE == 1) {
+    double* q = static_cast<double*>(out) + i0 * ops;
+    double d[CS_BLK];
+    bool rare = !fast_ok;
+#pragma unroll
+    for (int t = 0; t < CS_BLK; ++t) {
+      const unsigned b = __float_as_uint(v[t]);
+      const unsigned m = b & 0x7fffffffu;
+      rare |= (m - 0x00800000u >= 0x7f000000u) && m != 0u;  // subnormal, inf or NaN
+      const unsigned hi = (m == 0u ? 0u : (m >> 3) + hi_add) | (b & 0x80000000u);
+      d[t] = __hiloint2double((int)hi, (int)(b << 29));
+    }
+    if (rare) {
+#pragma unroll
+      for (int t = 0; t < CS_BLK; ++t) d[t] = f2d_scaled(v[t], out_exp);
+    }
+#pragma unroll
+    for (int t = 0; t < CS_BLK; ++t) {
+      *q = d[t];
+      q += ops;
+    }
+  } else {
+    float* q = static_cast<float*>(out) + i0 * ops;
+#pragma unroll
+    for (int t = 0; t < CS_BLK; ++t) {
+      *q = v[t];
+      q += ops;
+    }
+  }
+}
+
 template <int P, int MODE>
 __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -97,6 +137,8 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
 
   const double osd = (MODE == 1) ? *a.out_scale_dev : 1.0;
   const int out_exp = pow2_exp(osd);
+  const bool fast_ok = out_exp >= -896 && out_exp <= 896;
+  const unsigned hi_add = fast_ok ? (unsigned)(896 + out_exp) << 20 : 0u;
   const int tiles_l = (a.nl + 31) / 32;
   const int ntiles = tiles_l * a.n3;
   const int GP = ((Ls + CS_GROUPS - 1) / CS_GROUPS + CS_BLK - 1) / CS_BLK * CS_BLK;  // positions per group
@@ -241,13 +283,7 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
           nxt[0] = x;
           yt[b][t] = x;
         }
-        if (act) {
-#pragma unroll
-          for (int t = CS_BLK - 1; t >= 0; --t) {
-            if constexpr (MODE == 1) op[(size_t)(i0 + t) * ops] = f2d_scaled(yt[b][t], out_exp);
-            else op[(size_t)(i0 + t) * ops] = yt[b][t];
-          }
-        }
+        if (act) cs_store_block<MODE>(op, (size_t)i0, ops, yt[b], out_exp, fast_ok, hi_add);
       }
     }
     // then the staged part
@@ -294,13 +330,7 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
           nxt[0] = x;
           yv[t] = x;
         }
-        if (act) {
-#pragma unroll
-          for (int t = CS_BLK - 1; t >= 0; --t) {
-            if constexpr (MODE == 1) op[(size_t)(ib + t) * ops] = f2d_scaled(yv[t], out_exp);
-            else op[(size_t)(ib + t) * ops] = yv[t];
-          }
-        }
+        if (act) cs_store_block<MODE>(op, (size_t)ib, ops, yv, out_exp, fast_ok, hi_add);
       }
     }
   }
