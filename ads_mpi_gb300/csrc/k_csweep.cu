@@ -153,11 +153,16 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
     // the tail rows, coalesced, straight into registers (lanes beyond the
     // tile's lines load nothing); they are first used after the staged part
     float yt[NTB][CS_BLK];
+    {
+      const float* q = src + (size_t)Ls * a.in_ps + j;  // steps one row per position
 #pragma unroll
-    for (int b = 0; b < NTB; ++b)
+      for (int b = 0; b < NTB; ++b)
 #pragma unroll
-      for (int t = 0; t < CS_BLK; ++t)
-        yt[b][t] = (b < nt && act) ? src[(size_t)(Ls + b * CS_BLK + t) * a.in_ps + j] : 0.f;
+        for (int t = 0; t < CS_BLK; ++t) {
+          yt[b][t] = (b < nt && act) ? *q : 0.f;
+          q += a.in_ps;
+        }
+    }
 
     __syncwarp();  // the previous tile is done with S
     // ---- stage: group g holds positions [g*GP, (g+1)*GP) of every line ----
@@ -167,9 +172,14 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
       // 16-byte copies of the line-contiguous rows (lines up to a multiple
       // of 4: within the row's padded pitch)
       const int nc = (nlv + 3) / 4;
-      for (int idx = j; idx < (p1 - p0) * nc; idx += 32) {
-        const int i = p0 + idx / nc, c = idx % nc;
-        cs_cp16(S + (size_t)i * srow + 4 * c, src + (size_t)i * a.in_ps + 4 * c);
+      if (nc == 8) {  // whole tile: 4 rows per warp-wide copy
+        for (int i = p0 + (j >> 3); i < p1; i += 4)
+          cs_cp16(S + (size_t)i * srow + 4 * (j & 7), src + (size_t)i * a.in_ps + 4 * (j & 7));
+      } else {
+        for (int idx = j; idx < (p1 - p0) * nc; idx += 32) {
+          const int i = p0 + idx / nc, c = idx % nc;
+          cs_cp16(S + (size_t)i * srow + 4 * c, src + (size_t)i * a.in_ps + 4 * c);
+        }
       }
       cs_commit();
     }
@@ -193,13 +203,15 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
         const int ie = min(Ls, (g + 1) * GP);
 #pragma unroll 1
         for (; i + CS_BLK <= ie; i += CS_BLK) {
+          float* yp = Sj + (size_t)i * srow;
+          const float4* fp = FT + (size_t)i * VF;
           float bv[CS_BLK];
           float4 fv[CS_BLK][VF];
 #pragma unroll
           for (int t = 0; t < CS_BLK; ++t) {
-            bv[t] = Sj[(size_t)(i + t) * srow];
+            bv[t] = yp[t * srow];
 #pragma unroll
-            for (int v = 0; v < VF; ++v) fv[t][v] = FT[(size_t)(i + t) * VF + v];
+            for (int v = 0; v < VF; ++v) fv[t][v] = fp[t * VF + v];
           }
 #pragma unroll
           for (int t = 0; t < CS_BLK; ++t) {
@@ -213,7 +225,7 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
             bv[t] = y;
           }
 #pragma unroll
-          for (int t = 0; t < CS_BLK; ++t) Sj[(size_t)(i + t) * srow] = bv[t];
+          for (int t = 0; t < CS_BLK; ++t) yp[t * srow] = bv[t];
         }
 #pragma unroll 1
         for (; i < ie; ++i) {
@@ -311,13 +323,15 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
 #pragma unroll 1
       for (; i >= CS_BLK; i -= CS_BLK) {
         const int ib = i - CS_BLK;  // block [ib, i), processed downwards
+        const float* yp = Sj + (size_t)ib * srow;
+        const float4* bp = BT + (size_t)ib * VB;
         float yv[CS_BLK];
         float4 bw[CS_BLK][VB];
 #pragma unroll
         for (int t = 0; t < CS_BLK; ++t) {
-          yv[t] = Sj[(size_t)(ib + t) * srow];
+          yv[t] = yp[t * srow];
 #pragma unroll
-          for (int v = 0; v < VB; ++v) bw[t][v] = BT[(size_t)(ib + t) * VB + v];
+          for (int v = 0; v < VB; ++v) bw[t][v] = bp[t * VB + v];
         }
 #pragma unroll
         for (int t = CS_BLK - 1; t >= 0; --t) {
