@@ -118,7 +118,7 @@ struct ads_handle {
   // TMA store maps of the sweeps' transposed outputs
   CUtensorMap tm_u_out64{}, tm_r_out64{};
   CUtensorMap tm_wA_out64{}, tm_wB_out64{};
-  CUtensorMap tm_wA_out32{}, tm_wC_out32{};
+  CUtensorMap tm_wC_out32{};
 
   // form
   bool has_form = false;
@@ -389,14 +389,18 @@ int enqueue_solve32(ads_handle* h, const void* in, int tin, const double* in_sca
   SweepArgs ax = sweep_args(h, 0, h->d_fac32[0], in);
   ax.in_scale_dev = in_scale;
   ax.skip_flag = skip;
-  RUN(h, nx.c_str(), 1, launch_sweep(h->P, tin, 1, 0, false, &h->tm_wA_out32, ax, sweep_grid(h, 0), h->stream));
-  SweepArgs ay = sweep_args(h, 1, h->d_fac32[1], h->d_wA);
-  // lines x (stride PY in L1: y + PY (x + Nx z)), tiles over z
-  ay.lanes_total = (int)Nx; ay.lane_dim = 1; ay.out_line_dim = 1; ay.third_extent = (int)Nz;
-  ay.in_ls = g.PY; ay.in_t3s = g.PY * Nx;
-  ay.tiles_lane = (ay.lanes_total + SW_LANES - 1) / SW_LANES;
-  ay.skip_flag = skip;
-  RUN(h, ny.c_str(), 1, launch_sweep(h->P, 1, 1, 0, false, &h->tm_wC_out32, ay, ay.tiles_lane * (int)Nz, h->stream));
+  // x: skewed, without the transpose, into wC (L0)
+  RUN(h, nx.c_str(), 1, launch_sweep(h->P, tin, 1, 4, false, &h->tm_wC_out32, ax, sweep_grid(h, 0), h->stream));
+  // y: column form in place on wC (lines x contiguous, positions y at stride PX, tiles over z)
+  CSweepArgs cy{};
+  cy.L = (int)Ny; cy.nl = (int)Nx; cy.n3 = (int)Nz;
+  cy.in = h->d_wC;
+  cy.in_ls = 1; cy.in_ps = g.PX; cy.in_ts = g.PX * Ny;
+  cy.out = h->d_wC;
+  cy.out_ps = g.PX; cy.out_ts = g.PX * Ny;
+  cy.fac = h->d_fac32[1];
+  cy.skip_flag = skip;
+  RUN(h, ny.c_str(), 1, launch_csweep(h->P, 0, cy, h->stream));
   CSweepArgs cz{};
   cz.L = (int)Nz; cz.nl = (int)Nx; cz.n3 = (int)Ny;
   cz.in = h->d_wC;
@@ -721,9 +725,8 @@ int create_impl(ads_handle* h) {
   ok &= make_l0_out(h, &h->tm_r_out64, h->d_r, false);
   ok &= make_l1_out(h, &h->tm_wA_out64, h->d_wA, false);
   ok &= make_l2_out(h, &h->tm_wB_out64, h->d_wB, false);
-  ok &= make_l1_out(h, &h->tm_wA_out32, h->d_wA, true);
-  // the FP32 y sweep's output: L0 chunks of 32 x by SW_CH y
-  if (h->d_wC) ok &= encode(&h->tm_wC_out32, h->d_wC, true, h->g.N[0], h->g.N[1], h->g.N[2], h->g.PX, SW_LANES, SW_CH, 1);
+  // the FP32 x sweep's output: L0 chunks of SW_CH x (positions) by 32 y (lines)
+  if (h->d_wC) ok &= encode(&h->tm_wC_out32, h->d_wC, true, h->g.N[0], h->g.N[1], h->g.N[2], h->g.PX, SW_CH, SW_LANES, 1);
   if (!ok) return fail(h, ADS_ERR_CUDA, "cuTensorMapEncodeTiled rejected a layout");
   return ADS_OK;
 }

@@ -24,7 +24,9 @@
 //   z sweep: L2 (z fastest) -> L0 (x fastest)   = solve + ReorderRHSForX
 //
 // Mode 3 skips the solve and is the plain staged transpose used by
-// ads_reorder.
+// ads_reorder.  Mode 4 solves without the transpose: the chunks keep the
+// positions contiguous and go back into the input's layout (the mixed step's
+// FP32 x sweep, L0 -> L0, whose y and z sweeps then run in column form).
 // No wait in this kernel spins: cp.async and bulk-group waits complete in
 // hardware.
 #include "ads_internal.cuh"
@@ -142,6 +144,17 @@ template <typename TC, typename TIn>
 __device__ __forceinline__ TC load_y(const TIn* p) {
   if constexpr (sizeof(TIn) == 8 && sizeof(TC) == 4) return reinterpret_cast<const float*>(p)[0];
   else return (TC)*p;
+}
+
+// Slot of position i of lane j in the output ring.  Modes 0 and 3 write the
+// chunk transposed, [position][line] (the lines become the next layout's
+// contiguous dimension); mode 4 solves like mode 0 but keeps the positions
+// contiguous, [line][position], for an output in the input's own layout.
+template <int MODE>
+__device__ __forceinline__ int sw_tidx(int i, int j) {
+  constexpr int RMASK = SW_RING * SW_CH - 1;
+  if constexpr (MODE == 4) return ((i & RMASK) & ~(SW_CH - 1)) * SW_LANES + j * SW_CH + (i & (SW_CH - 1));
+  else return ((i & RMASK) << 5) + j;
 }
 
 // One warp per CTA, persistent over tiles of 32 lines.  The recurrences run in
@@ -316,7 +329,6 @@ __global__ void __launch_bounds__(SW_LANES)
     if (j == 0) bulk_wait_read<0>();  // the previous tile's stores are done reading the ring
     __syncwarp();
     {
-      constexpr int RMASK = SW_RING * SW_CH - 1;
       TC nxt[P];
 #pragma unroll
       for (int m = 0; m < P; ++m) nxt[m] = TC(0);
@@ -335,7 +347,7 @@ __global__ void __launch_bounds__(SW_LANES)
           for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
           nxt[0] = x;
         }
-        T[((i & RMASK) << 5) + j] = x;
+        T[sw_tidx<MODE>(i, j)] = x;
       };
       int s = 0;
       for (int c = nchunk - 1; c >= 0; --c) {
@@ -368,7 +380,7 @@ __global__ void __launch_bounds__(SW_LANES)
               }
             }
 #pragma unroll
-            for (int t = 0; t < SW_BLK; ++t) T[(((i0 - t) & RMASK) << 5) + j] = yv[t];
+            for (int t = 0; t < SW_BLK; ++t) T[sw_tidx<MODE>(i0 - t, j)] = yv[t];
             s += SW_BLK;
           } else if (s + SW_BLK <= sb) {
             // ramp block: lanes outside their line read a clamped position,
@@ -394,7 +406,7 @@ __global__ void __launch_bounds__(SW_LANES)
                 for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
                 nxt[0] = x;
               }
-              if (act) T[((ic & RMASK) << 5) + j] = x;
+              if (act) T[sw_tidx<MODE>(ic, j)] = x;
             }
             s += SW_BLK;
           } else {
@@ -407,7 +419,8 @@ __global__ void __launch_bounds__(SW_LANES)
         fence_proxy_async();
         __syncwarp();
         if (j == 0) {
-          if (a.out_line_dim == 1) tma_store_3d(&tmout, lane_base, c * SW_CH, t3, slot);
+          if (MODE == 4) tma_store_3d(&tmout, c * SW_CH, lane_base, t3, slot);
+          else if (a.out_line_dim == 1) tma_store_3d(&tmout, lane_base, c * SW_CH, t3, slot);
           else tma_store_3d(&tmout, lane_base, t3, c * SW_CH, slot);
           bulk_commit();
           // lane 0 enters chunk c-2 two steps after this event; its slot was
@@ -459,6 +472,11 @@ static cudaError_t launch_mode(int tin, int tc, int mode, bool trans, const CUte
       if (tin == 0 && tc == 0) return launch_t<double, double, P, 0, true>(tmout, a, grid, s);
       return cudaErrorInvalidValue;
     case 3: return launch_types<P, 3, false>(tin, tc, tmout, a, grid, s);
+    case 4:  // FP32 solve, output in the input's layout
+      if (trans) return cudaErrorInvalidValue;
+      if (tin == 0 && tc == 1) return launch_t<double, float, P, 4, false>(tmout, a, grid, s);
+      if (tin == 1 && tc == 1) return launch_t<float, float, P, 4, false>(tmout, a, grid, s);
+      return cudaErrorInvalidValue;
   }
   return cudaErrorInvalidValue;
 }

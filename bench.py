@@ -48,10 +48,9 @@ NCU_TRAFFIC = {
     ("resid_update", "heat256p2"): 280.538112e6 + 91.008256e6,
     ("fixup", "heat256p2"): 272.985600e6 + 90.721024e6,
     ("sweep_x_f32", "heat256p2"): 71.094016e6 + 25.629184e6,
-    ("sweep_y_f32", "heat256p2"): 71.095808e6 + 25.124864e6,
     ("sweep_x_f32_corr", "heat256p2"): 71.097344e6 + 25.651200e6,
-    ("sweep_y_f32_corr", "heat256p2"): 71.095040e6 + 25.052672e6,
-    ("sweep_z_f32", "heat256p2"): 71.513088e6 + 80.461568e6,
+    ("sweep_z_f32", "heat256p2"): 71.630592e6 + 80.654592e6,
+    ("sweep_z_f32_corr", "heat256p2"): 70.957568e6 + 19.331328e6,
 }
 
 
