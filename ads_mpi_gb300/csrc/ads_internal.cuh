@@ -127,7 +127,8 @@ struct SweepArgs {
 // positions i in [0, L), third index t in [0, n3).  Element (l, i, t) of the
 // input is in[l*in_ls + i*in_ps + t*in_ts] (in_ls == 1: lines contiguous), of the
 // output out[l + i*out_ps + t*out_ts]: float (mode 0) or, in mode 1, the FP64
-// state 2^e x with 2^e = *out_scale_dev.
+// state 2^e x with 2^e = *out_scale_dev.  In mode 0 out may be in (a tile
+// reads all of its input before it writes).
 struct CSweepArgs {
   int L, nl, n3;
   const float* in;
@@ -186,7 +187,9 @@ cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s);
 
 // kind: 0 = x sweep (L0 -> L1), 1 = y sweep (L1 -> L2), 2 = z sweep (L2 -> L0)
 // mode: 0 = TMA store to the next layout through tmout, 3 = identity transpose
-//       (no solve); trans (the adjoint's transposed solve) in FP64 only
+//       (no solve), 4 = FP32 solve stored back into the input's layout through
+//       tmout (box: SW_CH positions by SW_LANES lines); trans (the adjoint's
+//       transposed solve) in FP64 only
 // tin: 0 = double input, 1 = float input; tc: 0 = double compute, 1 = float compute
 // The input is read through a.in (set with sweep_input in the host code).
 cudaError_t launch_sweep(int P, int tin, int tc, int mode, bool trans, const CUtensorMap* tmout,

@@ -1,22 +1,25 @@
-// k_csweep.cu — the FP32 z sweep of the mixed step in column form.
+// k_csweep.cu — the FP32 y and z sweeps of the mixed step in column form.
 //
-// Replaces SolveOneDirection (src/ADS.F90:294-379) along z and the reorder
-// back to the x-fastest layout (src/reorderRHS.F90:7-93) for the FP32
-// solves.  The input (the y sweep's output) has the lines contiguous: 32
-// consecutive x at one y form a 128-byte row at every z.  One warp solves 32
-// lines with the lanes ACROSS the lines: at every step all 32 lanes are at
-// the same position, so
-//   * the tile is staged position-major by 16-byte copies, S[pos][line] with
-//     a row stride of 36 floats: a row of 32 lanes hits 32 different banks;
+// Replaces SolveOneDirection (src/ADS.F90:294-379) along y and z, and the
+// reorders between the directions (src/reorderRHS.F90:7-93), for the FP32
+// solves: both sweeps read and write the x-fastest layout L0, the y sweep in
+// place.  In L0 the lines of a y or z tile are contiguous: 32 consecutive x
+// form a 128-byte row at every position.  One warp solves 32 lines with the
+// lanes ACROSS the lines: at every step all 32 lanes are at the same
+// position, so
+//   * the tile is staged position-major by 16-byte copies, S[pos][line] in
+//     128-byte rows: a row of 32 lanes hits 32 different banks;
+//   * the last blocks of every line skip shared memory: their rows are loaded
+//     straight into registers, which also keep their forward results;
 //   * the LU factors of a position are the same for every lane: one
 //     broadcast vector load per step from a per-CTA table;
 //   * there is no wavefront skew, so no ramp steps;
-//   * each solution row (32 consecutive x) is stored straight to global
-//     memory, coalesced, during the backward pass: FP32, or the FP64 state
-//     2^e x.
-// (The x and y sweeps read inputs whose positions are contiguous; staging
-// those position-major takes 4-byte transposing copies, measured slower than
-// k_sweep's skewed form, so they stay there.)  A CTA holds as many warps
+//   * each block of solution rows (32 consecutive x) is stored straight to
+//     global memory, coalesced, during the backward pass: FP32, or the FP64
+//     state 2^e x.
+// (The x sweep reads lines whose positions are contiguous; staging those
+// position-major takes 4-byte transposing copies, measured slower than
+// k_sweep's skewed form, so it stays there.)  A CTA holds as many warps
 // (tiles) as shared memory allows next to one copy of the factor tables;
 // warps loop over tiles on their own.  No wait spins: cp.async groups
 // complete in hardware.
