@@ -311,7 +311,11 @@ __device__ __forceinline__ float d2f_scaled(double d, int sexp) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(d);
   const int ed = (int)((b >> 52) & 0x7ffull);
   const int ef = ed + sexp - 896;  // biased float exponent after scaling (1023 - 127)
-  if ((unsigned)(ed - 1) >= 2046u || (unsigned)(ef - 1) >= 254u) return d2f_scaled_rare(d, sexp);
+  if ((unsigned)(ed - 1) >= 2046u || (unsigned)(ef - 1) >= 254u) {
+    // zeros (and double subnormals, which flush) inline: no call for the common zero
+    if (ed == 0) return __uint_as_float((unsigned)(b >> 63) << 31);
+    return d2f_scaled_rare(d, sexp);
+  }
   const unsigned sign = (unsigned)(b >> 63) << 31;
   const unsigned m23 = (unsigned)(b >> 29) & 0x7fffffu;
   const unsigned rem = (unsigned)b & 0x1fffffffu;
@@ -343,7 +347,10 @@ __device__ __forceinline__ double f2d_scaled(float f, int sexp) {
   const unsigned b = __float_as_uint(f);
   const unsigned e8 = (b >> 23) & 0xffu;
   const int edn = (int)e8 + 896 + sexp;
-  if (e8 - 1u >= 254u || (unsigned)(edn - 1) >= 2046u) return f2d_scaled_rare(f, sexp);
+  if (e8 - 1u >= 254u || (unsigned)(edn - 1) >= 2046u) {
+    if ((b << 1) == 0u) return __longlong_as_double((long long)((unsigned long long)(b >> 31) << 63));  // zero inline
+    return f2d_scaled_rare(f, sexp);
+  }
   return __longlong_as_double((long long)(((unsigned long long)(b >> 31) << 63) | ((unsigned long long)edn << 52) |
                                           ((unsigned long long)(b & 0x7fffffu) << 29)));
 }
@@ -356,7 +363,8 @@ __device__ __forceinline__ void split_scaled(double d, int sexp, float& hi, floa
   const int ef = ed + sexp - 896;
   lo = 0.f;
   if ((unsigned)(ed - 1) >= 2046u || (unsigned)(ef - 1) >= 254u) {
-    hi = d2f_scaled_rare(d, sexp);  // zero, inf, NaN, under- or overflow: lo = 0
+    // zero (inline), inf, NaN, under- or overflow: lo = 0
+    hi = (ed == 0) ? __uint_as_float((unsigned)(b >> 63) << 31) : d2f_scaled_rare(d, sexp);
     return;
   }
   const unsigned sign = (unsigned)(b >> 63) << 31;
