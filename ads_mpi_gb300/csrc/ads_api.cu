@@ -81,7 +81,7 @@ struct ads_handle {
   double* d_delta = nullptr;  // mixed: increment of the heat step
   float* d_g32 = nullptr;     // mixed: the FP32 solve's scaled input (G, then each residual), L0
   float* d_x32 = nullptr;     // mixed: the FP32 correction x1, L0
-  float* d_wC = nullptr;      // mixed: the y sweep's FP32 output, L0
+  float* d_wC = nullptr;      // mixed: the FP32 x and y sweeps' output, L0
   double* d_wA = nullptr;  // L1 (double-sized; float view uses the same memory)
   double* d_wB = nullptr;  // L2
   double* d_shadow = nullptr;
