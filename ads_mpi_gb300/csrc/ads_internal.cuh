@@ -187,9 +187,9 @@ cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s);
 
 // kind: 0 = x sweep (L0 -> L1), 1 = y sweep (L1 -> L2), 2 = z sweep (L2 -> L0)
 // mode: 0 = TMA store to the next layout through tmout, 3 = identity transpose
-//       (no solve), 4 = FP32 solve stored back into the input's layout through
-//       tmout (box: SW_CH positions by SW_LANES lines); trans (the adjoint's
-//       transposed solve) in FP64 only
+//       (no solve), both FP64; 4 = FP32 solve stored back into the input's
+//       layout through tmout (box: SW_CH positions by SW_LANES lines); trans
+//       (the adjoint's transposed solve) in mode 0 only
 // tin: 0 = double input, 1 = float input; tc: 0 = double compute, 1 = float compute
 // The input is read through a.in (set with sweep_input in the host code).
 cudaError_t launch_sweep(int P, int tin, int tc, int mode, bool trans, const CUtensorMap* tmout,
@@ -384,7 +384,6 @@ __device__ __forceinline__ void split_scaled(double d, int sexp, float& hi, floa
 __device__ __forceinline__ int pow2_exp(double s) {
   return (int)(((unsigned long long)__double_as_longlong(s) >> 52) & 0x7ffull) - 1023;
 }
-size_t sweep_smem_bytes(int tin, int tc, int P, int L);
 cudaError_t launch_csweep(int P, int mode, const CSweepArgs& a, cudaStream_t s);
 
 }  // namespace ads

@@ -453,25 +453,20 @@ static cudaError_t launch_t(const CUtensorMap* tmout, const SweepArgs& a, int gr
   return cudaGetLastError();
 }
 
-template <int P, int MODE, bool TRANS>
-static cudaError_t launch_types(int tin, int tc, const CUtensorMap* tmout, const SweepArgs& a, int grid,
-                                cudaStream_t s) {
-  if (tin == 0 && tc == 0) return launch_t<double, double, P, MODE, TRANS>(tmout, a, grid, s);
-  if (tin == 0 && tc == 1) return launch_t<double, float, P, MODE, TRANS>(tmout, a, grid, s);
-  if (tin == 1 && tc == 1) return launch_t<float, float, P, MODE, TRANS>(tmout, a, grid, s);
-  return cudaErrorInvalidValue;
-}
-
+// The combinations the solves use: modes 0 and 3 in FP64 (the FP64 solves,
+// the adjoint's transposed solve, ads_reorder), mode 4 from FP64 or FP32 input
+// in FP32 (the mixed step's x sweep).
 template <int P>
 static cudaError_t launch_mode(int tin, int tc, int mode, bool trans, const CUtensorMap* tmout,
                                const SweepArgs& a, int grid, cudaStream_t s) {
   switch (mode) {
     case 0:
-      if (!trans) return launch_types<P, 0, false>(tin, tc, tmout, a, grid, s);
-      // the transposed solve (adjoint) is FP64 only
-      if (tin == 0 && tc == 0) return launch_t<double, double, P, 0, true>(tmout, a, grid, s);
-      return cudaErrorInvalidValue;
-    case 3: return launch_types<P, 3, false>(tin, tc, tmout, a, grid, s);
+      if (tin != 0 || tc != 0) return cudaErrorInvalidValue;
+      if (trans) return launch_t<double, double, P, 0, true>(tmout, a, grid, s);
+      return launch_t<double, double, P, 0, false>(tmout, a, grid, s);
+    case 3:
+      if (tin != 0 || tc != 0) return cudaErrorInvalidValue;
+      return launch_t<double, double, P, 3, false>(tmout, a, grid, s);
     case 4:  // FP32 solve, output in the input's layout
       if (trans) return cudaErrorInvalidValue;
       if (tin == 0 && tc == 1) return launch_t<double, float, P, 4, false>(tmout, a, grid, s);
@@ -479,12 +474,6 @@ static cudaError_t launch_mode(int tin, int tc, int mode, bool trans, const CUte
       return cudaErrorInvalidValue;
   }
   return cudaErrorInvalidValue;
-}
-
-size_t sweep_smem_bytes(int tin, int tc, int P, int L) {
-  if (tin == 0 && tc == 0) return SweepSmem<double, double>::total(P, L, true);
-  if (tin == 0 && tc == 1) return SweepSmem<double, float>::total(P, L, false);
-  return SweepSmem<float, float>::total(P, L, false);
 }
 
 cudaError_t launch_sweep(int P, int tin, int tc, int mode, bool trans, const CUtensorMap* tmout,
