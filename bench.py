@@ -47,8 +47,6 @@ NCU_TRAFFIC = {
     ("residual_f64", "heat256p2"): 291.368960e6 + 57.232128e6,
     ("resid_update", "heat256p2"): 280.538112e6 + 91.008256e6,
     ("fixup", "heat256p2"): 272.985600e6 + 90.721024e6,
-    ("sweep_x_f32", "heat256p2"): 71.094016e6 + 25.629184e6,
-    ("sweep_x_f32_corr", "heat256p2"): 71.097344e6 + 25.651200e6,
     ("sweep_z_f32", "heat256p2"): 71.630592e6 + 80.654592e6,
     ("sweep_z_f32_corr", "heat256p2"): 70.957568e6 + 19.331328e6,
 }
