@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark of the explicit ADS heat step on GB300.
 
-Metric (the benchmark spec): DOF-updates/s per ADS step at 256^3 elements, p = 2,
+Metric: DOF-updates/s per ADS step at 256^3 elements, p = 2,
 FP64 vs FP32 + FP64 refinement (each Kronecker solve refined to <= 1e-10
 relative residual).  Workload: heat equation, kappa = 1, dt = 1e-5, initial
 state = L2 projection of 16 seeded Gaussian bumps (synthetic, seed 0).
