@@ -17,6 +17,7 @@ from . import build as _build
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_MIXED_FAST = 2
 FORM_PROJECT = 0
 FORM_HEAT = 1
 FORM_OIL = 2
@@ -164,7 +165,7 @@ def fma_peak(fp64, device=0):
 class ADS:
     """One ADS configuration on one GPU (ADS_setup + ADS_compute_data of one rank)."""
 
-    def __init__(self, n, p, precision=PREC_FP64, refine_tol=1e-10, max_refine=3, device=0):
+    def __init__(self, n, p, precision=PREC_FP64, refine_tol=1e-13, max_refine=3, device=0):
         L = load()
         o = Opts()
         L.ads_default_opts(ctypes.byref(o))

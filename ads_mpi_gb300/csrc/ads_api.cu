@@ -72,6 +72,8 @@ struct ads_handle {
   double* d_tfac64[3] = {nullptr, nullptr, nullptr};
   float* d_fac32[3] = {nullptr, nullptr, nullptr};
   double* d_band[3] = {nullptr, nullptr, nullptr};
+  float2* d_nndf[3] = {nullptr, nullptr, nullptr};  // double-float tables (ADS_PREC_MIXED)
+  float2* d_jwdf[3] = {nullptr, nullptr, nullptr};
   float* d_band32[3] = {nullptr, nullptr, nullptr};  // FP32 copies for the updated residual
 
   // device buffers
@@ -152,6 +154,11 @@ int fail(ads_handle* h, int code, const std::string& msg) {
   if (h) h->err = msg;
   return code;
 }
+
+// FP32 sweeps with FP64 refinement (either mixed precision)
+bool is_mixed(const ads_handle* h) { return h->opts.precision != ADS_PREC_FP64; }
+// the heat increment assembled in double-float arithmetic
+bool df_increment(const ads_handle* h) { return h->opts.precision == ADS_PREC_MIXED && h->form == ADS_FORM_HEAT; }
 
 int cuda_fail(ads_handle* h, cudaError_t e, const char* where) {
   return fail(h, ADS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
@@ -347,12 +354,19 @@ int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool 
   if (fp32 && (h->form == ADS_FORM_HEAT || h->form == ADS_FORM_OIL))
     RUN(h, "uscale", 2, launch_uscale(u, (long long)h->n0, h->d_part, h->norm_parts, h->d_scal, h->stream));
   a.uscale = h->d_scal + SC_USCALE;
-  const void* tx = fp32 ? (const void*)&t32[0] : (const void*)&t64[0];
-  const void* ty = fp32 ? (const void*)&t32[1] : (const void*)&t64[1];
-  const void* tz = fp32 ? (const void*)&t32[2] : (const void*)&t64[2];
   int used = h->asm_grid;
-  RUN(h, fp32 ? "assemble_f32" : "assemble_f64", 1,
-      launch_assemble(fp32, incr, a, tx, ty, tz, h->asm_grid, &used, h->stream));
+  if (fp32 && incr && df_increment(h)) {
+    DfTabs3 tb;
+    DfTab* t[3] = {&tb.x, &tb.y, &tb.z};
+    for (int d = 0; d < 3; ++d) { t[d]->nn = h->d_nndf[d]; t[d]->jw = h->d_jwdf[d]; }
+    RUN(h, "assemble_df", 1, launch_assemble_df(a, tb, h->asm_grid, &used, h->stream));
+  } else {
+    const void* tx = fp32 ? (const void*)&t32[0] : (const void*)&t64[0];
+    const void* ty = fp32 ? (const void*)&t32[1] : (const void*)&t64[1];
+    const void* tz = fp32 ? (const void*)&t32[2] : (const void*)&t64[2];
+    RUN(h, fp32 ? "assemble_f32" : "assemble_f64", 1,
+        launch_assemble(fp32, incr, a, tx, ty, tz, h->asm_grid, &used, h->stream));
+  }
   FixupArgs f = fixup_args(h, F);
   f.nl2 = used;
   if (fp32 && incr) f.g32 = h->d_g32;  // the heat increment also feeds the FP32 solve as float
@@ -467,7 +481,7 @@ int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready, bool f32_in
 }
 
 int enqueue_solve(ads_handle* h) {
-  if (h->opts.precision == ADS_PREC_MIXED) return enqueue_solve_mixed(h, h->d_u, false, false);
+  if (is_mixed(h)) return enqueue_solve_mixed(h, h->d_u, false, false);
   return enqueue_solve64(h, h->d_F, &h->tm_u_out64, false);
 }
 
@@ -481,11 +495,11 @@ int enqueue_solve(ads_handle* h) {
 int enqueue_step(ads_handle* h) {
   RUN(h, "step_reset", 1, launch_step_reset(h->d_scal, h->d_flags, h->stream));
   int st;
-  if (h->opts.precision == ADS_PREC_MIXED && (h->form == ADS_FORM_HEAT || h->form == ADS_FORM_OIL)) {
+  if (is_mixed(h) && (h->form == ADS_FORM_HEAT || h->form == ADS_FORM_OIL)) {
     if ((st = enqueue_assemble(h, h->d_u, h->d_F, true, true, true))) return st;
     if ((st = enqueue_solve_mixed(h, h->d_delta, true, true))) return st;
     RUN(h, "update", 1, launch_add(h->d_u, h->d_delta, (long long)h->n0, h->stream));
-  } else if (h->opts.precision == ADS_PREC_MIXED) {
+  } else if (is_mixed(h)) {
     if ((st = enqueue_assemble(h, h->d_u, h->d_F, false, false, true))) return st;
     if ((st = enqueue_solve_mixed(h, h->d_u, true, false))) return st;
   } else {
@@ -548,7 +562,7 @@ int finish_stats(ads_handle* h, int k, double* l2norms) {
     if (l2norms) l2norms[i] = hist[4 * i];
   const double* last = &hist[4 * (size_t)(k - 1)];
   h->last.l2norm = last[0];
-  const bool mixed = h->opts.precision == ADS_PREC_MIXED;
+  const bool mixed = is_mixed(h);
   h->last.rel_residual = mixed ? last[1] : 0.0;
   h->last.refinements = mixed ? (int)last[2] : 0;
   h->last.converged = mixed ? (int)last[3] : 1;
@@ -583,7 +597,7 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_nn64[d]); cudaFree(h->d_jw64[d]); cudaFree(h->d_nn32[d]); cudaFree(h->d_jw32[d]);
     cudaFree(h->d_dd64[d]); cudaFree(h->d_dd32[d]);
     cudaFree(h->d_fac64[d]); cudaFree(h->d_tfac64[d]); cudaFree(h->d_fac32[d]); cudaFree(h->d_band[d]);
-    cudaFree(h->d_band32[d]);
+    cudaFree(h->d_band32[d]); cudaFree(h->d_nndf[d]); cudaFree(h->d_jwdf[d]);
   }
   cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_g32); cudaFree(h->d_x32); cudaFree(h->d_wC); cudaFree(h->d_wA); cudaFree(h->d_wB);
   cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_dqp); cudaFree(h->d_l2part); cudaFree(h->d_stage); cudaFree(h->d_un); cudaFree(h->d_ms);
@@ -640,6 +654,19 @@ int create_impl(ads_handle* h) {
     if ((st = upload(h, &h->d_fac32[d], fac32))) return st;
     if ((st = upload(h, &h->d_band[d], a.band))) return st;
     if ((st = upload(h, &h->d_band32[d], band32))) return st;
+    if (h->opts.precision == ADS_PREC_MIXED) {
+      // double-float tables: the nearest float and the float nearest to the remainder
+      auto split = [](const std::vector<double>& v) {
+        std::vector<float2> o(v.size());
+        for (size_t i = 0; i < v.size(); ++i) {
+          const float hi = (float)v[i];
+          o[i] = make_float2(hi, (float)(v[i] - (double)hi));
+        }
+        return o;
+      };
+      if ((st = upload(h, &h->d_nndf[d], split(a.NN)))) return st;
+      if ((st = upload(h, &h->d_jwdf[d], split(a.JW)))) return st;
+    }
   }
 
   auto zalloc = [&](double** p, size_t n) -> int {
@@ -651,8 +678,8 @@ int create_impl(ads_handle* h) {
   if ((st = zalloc(&h->d_u, h->n0))) return st;
   if ((st = zalloc(&h->d_F, h->n0))) return st;
   if ((st = zalloc(&h->d_r, h->n0))) return st;
-  if (h->opts.precision == ADS_PREC_MIXED && (st = zalloc(&h->d_delta, h->n0))) return st;
-  if (h->opts.precision == ADS_PREC_MIXED) {
+  if (is_mixed(h) && (st = zalloc(&h->d_delta, h->n0))) return st;
+  if (is_mixed(h)) {
     double* g32 = nullptr;
     if ((st = zalloc(&g32, (h->n0 + 1) / 2))) return st;
     h->d_g32 = reinterpret_cast<float*>(g32);
@@ -673,10 +700,13 @@ int create_impl(ads_handle* h) {
   const int nsm = prop.multiProcessorCount;
   const size_t smem_max = prop.sharedMemPerMultiprocessor;
   {
-    // expected residency: 3 CTAs/SM for FP32 at p <= 2, else 2 (registers)
-    const bool f32 = h->opts.precision == ADS_PREC_MIXED;
-    const size_t b = assemble_smem_bytes(h->P, f32) + 1024;
-    int per_sm = (int)std::min<size_t>(smem_max / b, (f32 && h->P <= 2) ? 3 : 2);
+    // expected residency of the step's assembly: the FP32 kernel 3 CTAs/SM at
+    // p <= 2, else 2; the double-float and FP64 kernels 2 at p <= 2, else 1
+    // (registers)
+    const bool f32 = h->opts.precision == ADS_PREC_MIXED_FAST;
+    const bool df = h->opts.precision == ADS_PREC_MIXED;
+    const size_t b = (df ? assemble_df_smem_bytes(h->P) : assemble_smem_bytes(h->P, f32)) + 1024;
+    int per_sm = (int)std::min<size_t>(smem_max / b, f32 ? (h->P <= 2 ? 3 : 2) : (h->P <= 2 ? 2 : 1));
     if (per_sm < 1) per_sm = 1;
     const int resident = nsm * per_sm;
     h->asm_nix = (g.E[0] + as_tx(h->P) - 1) / as_tx(h->P);
@@ -773,7 +803,7 @@ extern "C" {
 int ads_default_opts(ads_opts* o) {
   if (!o) return ADS_ERR_ARG;
   o->precision = ADS_PREC_FP64;
-  o->refine_tol = 1e-10;
+  o->refine_tol = 1e-13;
   o->max_refine = 3;
   o->device = 0;
   return ADS_OK;
@@ -809,7 +839,8 @@ int ads_create(const int n[3], const int p[3], const ads_opts* opts, ads_handle*
   h->Q = p[0] + 1;
   if (opts) h->opts = *opts;
   else ads_default_opts(&h->opts);
-  if (h->opts.precision != ADS_PREC_FP64 && h->opts.precision != ADS_PREC_MIXED) { delete h; return ADS_ERR_ARG; }
+  if (h->opts.precision != ADS_PREC_FP64 && h->opts.precision != ADS_PREC_MIXED &&
+      h->opts.precision != ADS_PREC_MIXED_FAST) { delete h; return ADS_ERR_ARG; }
   if (h->opts.max_refine < 0 || h->opts.max_refine > 16 || !(h->opts.refine_tol >= 0.0)) { delete h; return ADS_ERR_ARG; }
   h->dev = h->opts.device;
   int st = create_impl(h);
@@ -1161,7 +1192,7 @@ int ads_assemble(ads_handle* h, double* F_out, double* l2norm) {
   if (!h->has_form) return fail(h, ADS_ERR_STATE, "ads_set_form must be called before assembling");
   if (h->form == ADS_FORM_OIL && !h->has_oil) return fail(h, ADS_ERR_STATE, "ads_set_oil must be called before assembling the oil form");
   ADS_CUDA(h, cudaSetDevice(h->dev));
-  int st = enqueue_assemble(h, h->d_u, h->d_F, h->opts.precision == ADS_PREC_MIXED, false, true);
+  int st = enqueue_assemble(h, h->d_u, h->d_F, is_mixed(h), false, true);
   if (st) return st;
   if ((st = copy_l0_out(h, F_out, h->d_F, cudaMemcpyDeviceToHost))) return st;
   double l2 = 0.0;
@@ -1184,7 +1215,7 @@ int ads_solve(ads_handle* h, const double* F, double* u_out) {
   int fl[FL_COUNT];
   ADS_CUDA(h, cudaMemcpy(sc, h->d_scal, sizeof(sc), cudaMemcpyDeviceToHost));
   ADS_CUDA(h, cudaMemcpy(fl, h->d_flags, sizeof(fl), cudaMemcpyDeviceToHost));
-  const bool mixed = h->opts.precision == ADS_PREC_MIXED;
+  const bool mixed = is_mixed(h);
   h->last.rel_residual = mixed ? sc[SC_RELRES] : 0.0;
   h->last.refinements = mixed ? fl[FL_ITERS] : 0;
   h->last.converged = mixed ? fl[FL_CONV] : 1;

@@ -52,6 +52,16 @@ struct AxisTab {
   const T* dd;   // [E][Q][P]: difference weights D_b, b = 1..P (dN_b = D_b - D_{b+1})
 };
 
+// The same tables as double-floats (float2: high part, low part) for the
+// double-float heat increment assembly (k_assemble_df.cu)
+struct DfTab {
+  const float2* nn;  // [E][Q][P+1][2]
+  const float2* jw;  // [E][Q]
+};
+struct DfTabs3 {
+  DfTab x, y, z;
+};
+
 // Factors of the banded LU of one 1-D matrix, as rows of length N:
 //   row 0        : fs[i]     forward scale
 //   rows 1..P    : f[m][i]   forward coefficients (y_i -= f[m][i] * y_{i-m})
@@ -184,6 +194,10 @@ cudaError_t launch_assemble(bool fp32, bool incr, const AssembleArgs& a, const v
 cudaError_t launch_assemble_oil(bool fp32, bool incr, const AssembleArgs& a, const void* tabs_x,
                                 const void* tabs_y, const void* tabs_z, int grid, int* used_grid, cudaStream_t s);
 cudaError_t launch_fixup(const FixupArgs& a, cudaStream_t s);
+// the heat increment G = F - M u (form HEAT only) in double-float arithmetic
+// on the FP32 pipe, from coefficients scaled by *a.uscale (k_assemble_df.cu)
+cudaError_t launch_assemble_df(const AssembleArgs& a, const DfTabs3& tb, int grid, int* used_grid, cudaStream_t s);
+size_t assemble_df_smem_bytes(int P);
 
 // kind: 0 = x sweep (L0 -> L1), 1 = y sweep (L1 -> L2), 2 = z sweep (L2 -> L0)
 // mode: 0 = TMA store to the next layout through tmout, 3 = identity transpose

@@ -17,7 +17,7 @@ module ads_gpu
    implicit none
 
    integer(c_int), parameter :: ADS_OK = 0
-   integer(c_int), parameter :: ADS_PREC_FP64 = 0, ADS_PREC_MIXED = 1
+   integer(c_int), parameter :: ADS_PREC_FP64 = 0, ADS_PREC_MIXED = 1, ADS_PREC_MIXED_FAST = 2
    integer(c_int), parameter :: ADS_FORM_PROJECT = 0, ADS_FORM_HEAT = 1, ADS_FORM_OIL = 2
 
    type, bind(c) :: ads_opts

@@ -65,8 +65,15 @@ extern "C" {
 #define ADS_ERR_DEVICE 10      /* a kernel reported an error flag */
 
 /* precision of the time step */
-#define ADS_PREC_FP64 0   /* FP64 assembly and FP64 banded sweeps (the drop-in) */
-#define ADS_PREC_MIXED 1  /* FP32 assembly/sweeps, FP64 residual + refinement */
+#define ADS_PREC_FP64 0        /* FP64 assembly and FP64 banded sweeps (the drop-in) */
+#define ADS_PREC_MIXED 1       /* heat increment assembled in double-float arithmetic on the
+                                  FP32 pipe (~44 bits), FP32 banded sweeps, FP64 residual and
+                                  iterative refinement: the step matches FP64 to the
+                                  refinement tolerance (the oil form's increment is
+                                  assembled in plain FP32, as in ADS_PREC_MIXED_FAST) */
+#define ADS_PREC_MIXED_FAST 2  /* as ADS_PREC_MIXED with the increment assembled in plain
+                                  FP32: faster, but its rounding (~1e-7 relative in the
+                                  increment) stays in the step */
 
 /* integrand forms (replace the RHS_fun callback) */
 #define ADS_FORM_PROJECT 0  /* J W v f: L2Projection, heat at t = 0 */
@@ -80,8 +87,8 @@ extern "C" {
 #define ADS_REORDER_FOR_X 2 /* F3(z, x+y*Nx) -> F(x, y+z*Ny) */
 
 typedef struct ads_opts {
-  int precision;      /* ADS_PREC_FP64 or ADS_PREC_MIXED */
-  double refine_tol;  /* mixed: stop when ||F - M u||_2 <= refine_tol * ||F||_2 */
+  int precision;      /* ADS_PREC_FP64, ADS_PREC_MIXED or ADS_PREC_MIXED_FAST */
+  double refine_tol;  /* mixed: stop when ||F - M u||_2 <= refine_tol * ||F||_2 (default 1e-13) */
   int max_refine;     /* mixed: maximum refinement corrections per solve */
   int device;         /* CUDA device ordinal */
 } ads_opts;

@@ -32,12 +32,12 @@ def test_multistep_heat_matches_oracle(ads_mod, oracle_mod, E, p):
     l2 = g.multistep(MIXES)
     l2o = o.multistep(oracle_mod.FORM_HEAT, MIXES, fqp=f, kappa_qp=kq, dt=dt)
     assert any(o.pivoted())
-    assert rel_l2(g.coeffs(), o.coeffs()) < 1e-10
+    assert rel_l2(g.coeffs(), o.coeffs()) < 1e-12
     assert abs(l2 - l2o) < 1e-12 * abs(l2o)
     # a second MultiStep reuses the cached factors
     l2b = g.multistep(MIXES)
     l2ob = o.multistep(oracle_mod.FORM_HEAT, MIXES, fqp=f, kappa_qp=kq, dt=dt)
-    assert rel_l2(g.coeffs(), o.coeffs()) < 1e-10
+    assert rel_l2(g.coeffs(), o.coeffs()) < 1e-12
     assert abs(l2b - l2ob) < 1e-12 * abs(l2ob)
 
 
