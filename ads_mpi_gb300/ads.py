@@ -76,6 +76,7 @@ ABI = [
     ("ads_residual_noalloc", [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _dp],
      ctypes.c_int),
     ("ads_heat_adjoint", [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
+    ("ads_heat_jvp", [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
     ("ads_axis_setup", [ctypes.c_int, ctypes.c_int, _dp, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
     ("ads_fma_peak", [ctypes.c_int, ctypes.c_int, _dp], ctypes.c_int),
     ("ads_get_stream", [ctypes.c_void_p], ctypes.c_void_p),
@@ -362,6 +363,18 @@ class ADS:
         self._check(self._L.ads_heat_adjoint(self.h, K, checkpoint_every, _ptr(u0), _ptr(ut),
                                              ctypes.byref(loss), _ptr(g), _ptr(gk)))
         return loss.value, g, gk
+
+    def heat_jvp(self, K, u0, du0=None, dkappa=None):
+        """Tangent-linear model of K heat steps: (u^K, du^K) with du^K the
+        derivative of u^K along du0 (initial state) and dkappa (per-point
+        conductivity, quadrature-point layout); either may be None."""
+        u0 = _c64(u0)
+        du0 = None if du0 is None else _c64(du0)
+        dk = None if dkappa is None else _c64(dkappa)
+        uK = np.zeros(self.N)
+        duK = np.zeros(self.N)
+        self._check(self._L.ads_heat_jvp(self.h, K, _ptr(u0), _ptr(du0), _ptr(dk), _ptr(uK), _ptr(duK)))
+        return uK, duK
 
     # device interop
     def stream(self):

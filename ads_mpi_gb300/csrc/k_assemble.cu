@@ -143,6 +143,12 @@ static cudaError_t dispatch_form(bool fp32, bool incr, const AssembleArgs& a, co
   }
   if (fp32) return incr ? dispatch_heat<P, float, true>(a, tx, ty, tz, grid, used_grid, s)
                         : dispatch_heat<P, float, false>(a, tx, ty, tz, grid, used_grid, s);
+  // FP64 increment form: -dt K(kappa) u alone, with a per-point kappa and no
+  // source (the tangent model's conductivity term)
+  if (incr) {
+    if (a.fqp != nullptr || a.kqp == nullptr) return cudaErrorInvalidValue;
+    return launch_one<P, double, ADS_FORM_HEAT, false, true, true>(a, tx, ty, tz, grid, used_grid, s);
+  }
   return dispatch_heat<P, double, false>(a, tx, ty, tz, grid, used_grid, s);
 }
 

@@ -26,6 +26,7 @@
  *   ads_save_spline_plot  SaveSplinePlot + VtkOutput of PrintSolution  src/ADS.F90:955-989
  *   ads_write_vti       VtkOutput                                    src/vtk.F90:15-77
  *   ads_heat_adjoint    new: hand-written adjoint of the explicit heat step
+ *   ads_heat_jvp        new: tangent-linear model of the explicit heat step
  *
  * Layouts.  Coefficient vectors are x-fastest, u[x + Nx*(y + Ny*z)], which is
  * the Fortran F(x, y+z*Ny) and R(:,2,2,2) of the reference.  Quadrature-point
@@ -215,6 +216,19 @@ int ads_residual_noalloc(ads_handle* h, const double* d_F, const double* d_u, do
 int ads_heat_adjoint(ads_handle* h, int K, int checkpoint_every, const double* u0,
                      const double* u_target, double* loss, double* grad_u0,
                      double* grad_kappa_qp);
+
+/* Tangent-linear (forward-mode) model of K explicit heat steps from u0 with
+ * the current HEAT form, the companion of ads_heat_adjoint: duK (ndof) =
+ * d u^K along the direction (du0, dkappa_qp) of the initial state (ndof, may
+ * be NULL = 0) and of the per-point conductivity (quadrature-point layout,
+ * may be NULL = 0; needs no per-point kappa in the form).  uK (may be NULL)
+ * receives u^K.  Each step assembles A w^n with the FP64 kernels (the source
+ * does not depend on u0 or kappa and is left out), adds -dt K(dkappa) u^n,
+ * and solves with the FP64 sweeps; the forward uses the handle's precision.
+ * With loss L = 1/2 e^T M e, e = u^K - u_target, the directional derivative
+ * is e^T M duK: no finite-difference cancellation at any step size. */
+int ads_heat_jvp(ads_handle* h, int K, const double* u0, const double* du0, const double* dkappa_qp,
+                 double* uK, double* duK);
 
 /* Host-only setup helpers (no GPU needed): the tables ads_create builds for
  * one axis.  U[n+p+2], O[E], J[E], W[p+1], X[E*(p+1)], NN[E*(p+1)*(p+1)*2],

@@ -1,7 +1,9 @@
 """Hand-written adjoint of the explicit heat step (K6) through the C-ABI:
 against the oracle's FP64 reference gradient, against central finite
-differences (h = 1e-6) along seeded random directions, and through a thin
-torch.autograd.Function checked with torch.autograd.gradcheck."""
+differences (h = 1e-6) along seeded random directions, against the tangent-
+linear model (ads_heat_jvp: forward mode, no finite-difference cancellation),
+and through a thin torch.autograd.Function checked with
+torch.autograd.gradcheck."""
 import numpy as np
 import pytest
 
@@ -53,6 +55,60 @@ def test_adjoint_matches_central_differences(ads_mod, oracle_mod):
         g.set_form(ads_mod.FORM_HEAT, kappa_qp=kq, dt=dt)
         fd = (lp - lm) / (2 * h)
         assert abs(fd - gk @ dk) <= 1e-6 * abs(fd)
+
+
+@pytest.mark.parametrize("E,p,dt", [(7, 2, 2e-3), ((9, 8, 6), 3, 1e-2), (6, 1, 5e-3)])
+def test_tangent_model_matches_adjoint_dot_products(ads_mod, oracle_mod, E, p, dt):
+    """Forward-mode (ads_heat_jvp) against reverse mode (ads_heat_adjoint):
+    e^T M du^K along (d, dk) equals grad_u0 . d + grad_kappa . dk for any
+    direction, to rounding, with a per-point kappa and a source term.  At
+    these dt the explicit scheme is unstable (values grow by orders of
+    magnitude), which the identity is indifferent to."""
+    if isinstance(E, int):
+        E = (E, E, E)
+    n = tuple(e + p - 1 for e in E)
+    g = ads_mod.ADS(n, (p, p, p))
+    rng = np.random.default_rng(sum(E) + p)
+    kq = np.exp(0.4 * rng.standard_normal(g.nqp))
+    f = rng.standard_normal(g.nqp)
+    g.set_form(ads_mod.FORM_HEAT, f_qp=f, kappa_qp=kq, dt=dt)
+    u0 = rng.standard_normal(g.N)
+    ut = rng.standard_normal(g.N)
+    K = 6
+    loss, gu, gk = g.heat_adjoint(K, 2, u0, ut, grad=True, grad_kappa=True)
+    g.set_coeffs(u0)
+    g.steps(K)
+    u_fwd = g.coeffs()
+    for _ in range(3):
+        d = rng.standard_normal(g.N)
+        dk = rng.standard_normal(g.nqp) * kq
+        uK, duK = g.heat_jvp(K, u0, du0=d, dkappa=dk)
+        assert rel_l2(uK, u_fwd) < 1e-14
+        jvp = float((uK - ut) @ g.apply_mass(duK))
+        vjp = float(gu @ d + gk @ dk)
+        assert abs(jvp - vjp) <= 1e-11 * abs(vjp)
+        # each direction on its own
+        _, du_only = g.heat_jvp(K, u0, du0=d)
+        _, dk_only = g.heat_jvp(K, u0, dkappa=dk)
+        assert abs(float((uK - ut) @ g.apply_mass(du_only)) - float(gu @ d)) <= 1e-11 * abs(float(gu @ d))
+        assert abs(float((uK - ut) @ g.apply_mass(dk_only)) - float(gk @ dk)) <= 1e-11 * abs(float(gk @ dk))
+
+
+def test_tangent_model_of_initial_state_is_the_homogeneous_step(ads_mod):
+    """Along du0 alone the tangent of the (affine) heat step is the step
+    without its source, applied to du0."""
+    n = (9, 10, 8)
+    g = ads_mod.ADS(n, (2, 2, 2))
+    rng = np.random.default_rng(2)
+    f = rng.standard_normal(g.nqp)
+    u0 = rng.standard_normal(g.N)
+    d = rng.standard_normal(g.N)
+    g.set_form(ads_mod.FORM_HEAT, f_qp=f, kappa=0.8, dt=1e-3)
+    _, duK = g.heat_jvp(4, u0, du0=d)
+    g.set_form(ads_mod.FORM_HEAT, kappa=0.8, dt=1e-3)
+    g.set_coeffs(d)
+    g.steps(4)
+    assert rel_l2(duK, g.coeffs()) < 1e-14
 
 
 def test_adjoint_gradcheck_through_autograd(ads_mod, oracle_mod):
