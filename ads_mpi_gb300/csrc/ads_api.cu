@@ -516,7 +516,6 @@ int check_flags(ads_handle* h) {
   int fl[FL_COUNT];
   ADS_CUDA(h, cudaMemcpyAsync(fl, h->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, h->stream));
   ADS_CUDA(h, cudaStreamSynchronize(h->stream));
-  if (fl[FL_ERR] & ERRF_TMA_TIMEOUT) return fail(h, ADS_ERR_TIMEOUT, "a TMA wait timed out on the device");
   if (fl[FL_ERR]) return fail(h, ADS_ERR_DEVICE, "a kernel reported error bits " + std::to_string(fl[FL_ERR]));
   return ADS_OK;
 }

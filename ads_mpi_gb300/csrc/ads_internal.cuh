@@ -35,13 +35,6 @@ constexpr int RS_TX = 32;
 constexpr int RS_TY = 8;
 constexpr int RS_THREADS = 256;
 
-// Upper bound of spin iterations of any device-side wait.
-constexpr long long WAIT_LIMIT = 1ll << 26;
-
-// error-flag bits written by kernels
-constexpr int ERRF_TMA_TIMEOUT = 1;
-constexpr int ERRF_BOUNDS = 2;
-
 // ---------------------------------------------------------------------------
 // Device-side per-axis tables
 // ---------------------------------------------------------------------------

@@ -20,7 +20,10 @@
 // Set-up: the first call on each device, with that device current, looks up
 // the array's device address once (cudaGetSymbolAddress; this also loads the
 // module holding the array if it is not loaded yet).  Make that first call
-// before any stream capture.
+// before any stream capture.  The address is kept per device ordinal for the
+// life of the process: do not use this entry point on a device after a
+// cudaDeviceReset of it (the kept address would belong to the destroyed
+// context).
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -30,7 +33,8 @@
 namespace {
 
 // largest residual grid the scratch covers: one CTA per tile of 32 x 8 x 32
-// DOFs, so up to 8192 tiles (about 67M DOFs, e.g. 406^3)
+// DOFs, ceil(Nx/32) * ceil(Ny/8) * ceil(Nz/32) <= 8192 (the largest cube is
+// 384^3 DOFs: 12 * 48 * 12 = 6912 tiles; 385^3 needs 13 * 49 * 13 = 8281)
 constexpr int kMaxCtas = ADS_NOALLOC_MAX_CTAS;
 constexpr int kResultOffset = 3 * kMaxCtas;          // [rr, ff, rmax] after the partials
 constexpr int kScratchDoubles = 3 * kMaxCtas + 8;    // 196,672 bytes

@@ -199,10 +199,13 @@ int ads_get_coeffs_device(ads_handle* h, double* d_u);
  * into the library (3 * ADS_NOALLOC_MAX_CTAS + 8 doubles, 196,672 bytes per
  * GPU, held until exit); it calls no cudaMalloc, cudaFree or allocating
  * library routine.  Sizes needing more than ADS_NOALLOC_MAX_CTAS residual
- * tiles of 32 x 8 x 32 DOFs (about 67M DOFs) return ADS_ERR_ARG.  The array
- * is shared by all calls on a device and keeps the last call's contents:
- * calls that overlap on the GPU race on it.  The first call on each device
- * looks up the array's address; make it before any stream capture. */
+ * tiles of 32 x 8 x 32 DOFs, ceil(Nx/32) * ceil(Ny/8) * ceil(Nz/32) > 8192
+ * (the largest cube is 384^3 DOFs), return ADS_ERR_ARG.  The array is shared
+ * by all calls on a device and keeps the last call's contents: calls that
+ * overlap on the GPU race on it.  The first call on each device looks up the
+ * array's address and keeps it for the process: make that call before any
+ * stream capture, and do not call again on a device after a cudaDeviceReset
+ * of it. */
 #define ADS_NOALLOC_MAX_CTAS 8192
 int ads_residual_noalloc(ads_handle* h, const double* d_F, const double* d_u, double* d_r,
                          double norms[3]);

@@ -11,7 +11,7 @@ reference test:
   n = -1 case has its vector assertion commented out in the reference ("FIX
   THIS"), which is recorded as ``"check_vector": false``.
 
-Usage: python tests/golden/make_knot_vectors.py [path/to/test_knot.pf]
+Usage: python tests/golden/make_knot_vectors.py <path to the reference's tests/test_knot.pf>
 """
 import json
 import os
@@ -71,7 +71,9 @@ def parse(text):
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/tests/test_knot.pf"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_knot_vectors.py <path to the reference's tests/test_knot.pf>")
+    src = sys.argv[1]
     with open(src) as f:
         records = parse(f.read())
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "knot_vectors.json")

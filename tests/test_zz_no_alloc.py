@@ -68,6 +68,27 @@ def test_noalloc_residual_matches_apply_mass_twice(E, p):
     g.cleanup()
 
 
+def test_noalloc_calls_allocate_no_device_memory():
+    """After a first call (which looks up the scratch address), further calls
+    leave the device's free memory unchanged."""
+    torch = pytest.importorskip("torch")
+    A, lib, f = _abi()
+    g = A.ADS((25, 22, 19), (2, 2, 2))
+    rng = np.random.default_rng(43)
+    du = torch.from_numpy(rng.standard_normal(g.N)).cuda()
+    dF = torch.from_numpy(rng.standard_normal(g.N)).cuda()
+    dr = torch.empty_like(du)
+    _call(lib, f, g, dF, du, dr)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        _call(lib, f, g, dF, du, dr)
+        _call(lib, f, g, None, du, dr)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    g.cleanup()
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     """448 x 448 x 352 DOFs need 14 x 56 x 11 = 8624 residual tiles of
     32 x 8 x 32 DOFs, more than the fixed scratch's 8192 CTAs: the call
