@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libadsgpu.so")
-SOURCES = ["ads_api.cu", "k_assemble.cu", "k_assemble_oil.cu", "k_assemble_df.cu", "k_sweep.cu", "k_csweep.cu", "k_misc.cu", "noalloc.cu", "setup.cpp"]
+SOURCES = ["ads_api.cu", "k_assemble.cu", "k_assemble_oil.cu", "k_assemble_df.cu", "k_general.cu", "k_sweep.cu", "k_csweep.cu", "k_misc.cu", "noalloc.cu", "setup.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

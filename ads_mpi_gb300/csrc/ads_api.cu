@@ -73,6 +73,13 @@ struct ads_handle {
   float* d_fac32[3] = {nullptr, nullptr, nullptr};
   double* d_band[3] = {nullptr, nullptr, nullptr};
   float2* d_nndf[3] = {nullptr, nullptr, nullptr};  // double-float tables (ADS_PREC_MIXED)
+  // general geometry: unequal degrees (general) or an axis longer than the
+  // sweeps' shared-memory lines (banded: every solve by k_band_solve with the
+  // mass matrix's banded LU, d_gab/d_gpiv per axis)
+  bool general = false, banded = false;
+  double* d_gab[3] = {nullptr, nullptr, nullptr};
+  int* d_gpiv[3] = {nullptr, nullptr, nullptr};
+  double* d_gpart = nullptr;  // l2 partials of the general assembly
   float2* d_jwdf[3] = {nullptr, nullptr, nullptr};
   float* d_band32[3] = {nullptr, nullptr, nullptr};  // FP32 copies for the updated residual
 
@@ -341,9 +348,42 @@ ResidualArgs residual_args(const ads_handle* h, const double* u, const double* F
   return a;
 }
 
+// r = F - (Mx (x) My (x) Mz) u, or M u with F null (FP64)
+int enqueue_mass(ads_handle* h, const double* u, const double* F, double* r, const char* name) {
+  if (h->general) {
+    RUN(h, name, 1, launch_residual_gen(h->g, u, F, r, h->d_band, h->stream));
+    return ADS_OK;
+  }
+  ResidualArgs ra = residual_args(h, u, F, r);
+  RUN(h, name, 1, launch_residual(h->P, ra, h->res_grid, h->stream));
+  return ADS_OK;
+}
+
 // assembly (+ fixup) of F from coefficients u with the handle's form
+// the general-geometry assembly (k_general.cu), FP64
+int enqueue_assemble_gen(ads_handle* h, const double* u, double* F, bool incr, bool with_f, const double* kqp_override) {
+  if (h->form == ADS_FORM_OIL)
+    return fail(h, ADS_ERR_UNSUPPORTED, "the oil form needs equal degrees on all axes");
+  GenAssembleArgs a{};
+  a.g = h->g;
+  a.form = h->form;
+  a.incr = incr ? 1 : 0;
+  a.dt = h->dt;
+  a.kappa = h->kappa;
+  a.u = u;
+  a.F = F;
+  a.fqp = (with_f && h->has_f) ? h->d_fqp : nullptr;
+  a.kqp = kqp_override ? kqp_override : (h->has_k ? h->d_kqp : nullptr);
+  for (int d = 0; d < 3; ++d) { a.nn[d] = h->d_nn64[d]; a.jw[d] = h->d_jw64[d]; }
+  a.part = h->d_gpart;
+  const int ncol = (h->p[0] + 1) * (h->p[1] + 1) * (h->p[2] + 1);
+  RUN(h, "assemble_gen", ncol + 1, launch_assemble_gen(a, h->d_scal, h->stream));
+  return ADS_OK;
+}
+
 int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool incr, bool with_f,
                      const double* kqp_override = nullptr) {
+  if (h->general) return enqueue_assemble_gen(h, u, F, incr, with_f, kqp_override);
   AssembleArgs a = assemble_args(h, u, F, with_f);
   if (kqp_override) a.kqp = kqp_override;
   AxisTab<double> t64[3];
@@ -376,8 +416,23 @@ int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool 
   return ADS_OK;
 }
 
-// FP64 Kronecker solve: in (L0) -> out (L0 via the map tm_out)
-int enqueue_solve64(ads_handle* h, const double* in, const CUtensorMap* tm_out, bool trans) {
+// FP64 Kronecker solve: in (L0) -> out (L0, through the map tm_out on the
+// sweep path).  Banded geometry: in is copied to out and each direction is
+// solved in place by k_band_solve with the mass matrix's LU (M is symmetric,
+// so the transposed solve is the same).
+int enqueue_solve64(ads_handle* h, const double* in, const CUtensorMap* tm_out, bool trans, double* out) {
+  if (h->banded) {
+    const Geometry& g = h->g;
+    const long long Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
+    if (in != out) ADS_CUDA(h, cudaMemcpyAsync(out, in, sizeof(double) * h->n0, cudaMemcpyDeviceToDevice, h->stream));
+    RUN(h, "band_solve_x", 1, launch_band_solve(out, Ny, Nz, g.PX, g.PX * Ny, 1, (int)Nx, h->p[0], h->p[0],
+                                                h->d_gab[0], h->d_gpiv[0], h->stream));
+    RUN(h, "band_solve_y", 1, launch_band_solve(out, Nx, Nz, 1, g.PX * Ny, g.PX, (int)Ny, h->p[1], h->p[1],
+                                                h->d_gab[1], h->d_gpiv[1], h->stream));
+    RUN(h, "band_solve_z", 1, launch_band_solve(out, Nx, Ny, 1, g.PX, g.PX * Ny, (int)Nz, h->p[2], h->p[2],
+                                                h->d_gab[2], h->d_gpiv[2], h->stream));
+    return ADS_OK;
+  }
   double* const* fac = trans ? h->d_tfac64 : h->d_fac64;
   SweepArgs ax = sweep_args(h, 0, fac[0], in);
   RUN(h, "sweep_x_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, &h->tm_wA_out64, ax, sweep_grid(h, 0), h->stream));
@@ -484,7 +539,7 @@ int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready, bool f32_in
 
 int enqueue_solve(ads_handle* h) {
   if (is_mixed(h)) return enqueue_solve_mixed(h, h->d_u, false, false);
-  return enqueue_solve64(h, h->d_F, &h->tm_u_out64, false);
+  return enqueue_solve64(h, h->d_F, &h->tm_u_out64, false, h->d_u);
 }
 
 // one Step (src/ADS.F90:437-461): FormUn+Form3DRHS, three sweeps, R := F.
@@ -506,7 +561,7 @@ int enqueue_step(ads_handle* h) {
     if ((st = enqueue_solve_mixed(h, h->d_u, true, false))) return st;
   } else {
     if ((st = enqueue_assemble(h, h->d_u, h->d_F, false, false, true))) return st;
-    if ((st = enqueue_solve64(h, h->d_F, &h->tm_u_out64, false))) return st;
+    if ((st = enqueue_solve64(h, h->d_F, &h->tm_u_out64, false, h->d_u))) return st;
   }
   RUN(h, "record", 1, launch_record(h->d_scal, h->d_flags, h->d_hist, h->hist_cap, h->stream));
   return ADS_OK;
@@ -599,7 +654,9 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_dd64[d]); cudaFree(h->d_dd32[d]);
     cudaFree(h->d_fac64[d]); cudaFree(h->d_tfac64[d]); cudaFree(h->d_fac32[d]); cudaFree(h->d_band[d]);
     cudaFree(h->d_band32[d]); cudaFree(h->d_nndf[d]); cudaFree(h->d_jwdf[d]);
+    cudaFree(h->d_gab[d]); cudaFree(h->d_gpiv[d]);
   }
+  cudaFree(h->d_gpart);
   cudaFree(h->d_u); cudaFree(h->d_F); cudaFree(h->d_r); cudaFree(h->d_delta); cudaFree(h->d_g32); cudaFree(h->d_x32); cudaFree(h->d_wC); cudaFree(h->d_wA); cudaFree(h->d_wB);
   cudaFree(h->d_shadow); cudaFree(h->d_fqp); cudaFree(h->d_kqp); cudaFree(h->d_dqp); cudaFree(h->d_l2part); cudaFree(h->d_stage); cudaFree(h->d_un); cudaFree(h->d_ms);
   for (int d = 0; d < 3; ++d) { cudaFree(h->d_mab[d]); cudaFree(h->d_mpiv[d]); } cudaFree(h->d_slab); cudaFree(h->d_xslab);
@@ -626,21 +683,47 @@ int create_impl(ads_handle* h) {
   Geometry& g = h->g;
   g.P = h->P;
   g.Q = h->Q;
-  for (int d = 0; d < 3; ++d) { g.E[d] = h->ax[d].E; g.N[d] = h->ax[d].N; }
+  for (int d = 0; d < 3; ++d) {
+    g.E[d] = h->ax[d].E;
+    g.N[d] = h->ax[d].N;
+    g.p[d] = h->p[d];
+    g.q[d] = h->p[d] + 1;
+  }
+  // unequal degrees: the general kernels; an axis longer than the sweeps'
+  // shared-memory lines: banded solves (with the tuned assembly and residual
+  // when the degrees are equal).  Both are FP64 paths.
+  // (and an x axis beyond the fixup's one-CTA rows of 4096 DOFs)
+  h->general = !(h->p[0] == h->p[1] && h->p[1] == h->p[2]) || g.N[0] > 4096;
+  h->banded = h->general;
   for (int d = 0; d < 3; ++d)
-    if (g.N[d] > ADS_MAX_AXIS_DOFS) return fail(h, ADS_ERR_UNSUPPORTED, "the GPU sweeps support at most 448 DOFs per axis");
+    if (g.N[d] > ADS_MAX_AXIS_DOFS) h->banded = true;
+  if (h->banded && is_mixed(h))
+    return fail(h, ADS_ERR_UNSUPPORTED, "mixed precision needs equal degrees and at most 448 DOFs per axis");
   g.PX = round_up(g.N[0], 8);
   g.PY = round_up(g.N[1], 8);
   g.PZ = round_up(g.N[2], 8);
   h->n0 = (size_t)g.PX * g.N[1] * g.N[2];
   h->n1 = (size_t)g.PY * g.N[0] * g.N[2];
   h->n2 = (size_t)g.PZ * g.N[0] * g.N[1];
-  h->nqp = (long long)g.E[0] * g.E[1] * g.E[2] * g.Q * g.Q * g.Q;
+  h->nqp = (long long)g.E[0] * g.E[1] * g.E[2] * g.q[0] * g.q[1] * g.q[2];
 
   for (int d = 0; d < 3; ++d) {
     const AxisHost& a = h->ax[d];
     std::vector<double> fac, tfac;
     if (band_factor(a, fac, tfac)) return fail(h, ADS_ERR_ZERO_PIVOT, "zero pivot in the 1-D mass matrix");
+    if (h->banded) {
+      // the mass matrix in LAPACK band storage with its banded LU (MKBBT's
+      // mass mix; the mass matrix is SPD, so the LU does not pivot)
+      const double mass[4] = {1.0, 0.0, 0.0, 0.0};
+      std::vector<double> AB;
+      mix_band(a, mass, AB);
+      std::vector<int> ipiv(a.N);
+      if (band_lu(a.N, a.p, a.p, AB.data(), 3 * a.p + 1, ipiv.data()))
+        return fail(h, ADS_ERR_ZERO_PIVOT, "zero pivot in the 1-D mass matrix");
+      int st;
+      if ((st = upload(h, &h->d_gab[d], AB))) return st;
+      if ((st = upload(h, &h->d_gpiv[d], ipiv))) return st;
+    }
     std::vector<float> nn32(a.NN.begin(), a.NN.end()), jw32(a.JW.begin(), a.JW.end()), fac32(fac.begin(), fac.end());
     std::vector<float> dd32(a.DD.begin(), a.DD.end()), band32(a.band.begin(), a.band.end());
     int st;
@@ -691,16 +774,17 @@ int create_impl(ads_handle* h) {
     if ((st = zalloc(&wc, (h->n0 + 1) / 2))) return st;
     h->d_wC = reinterpret_cast<float*>(wc);
   }
-  if ((st = zalloc(&h->d_wA, h->n1))) return st;
-  if ((st = zalloc(&h->d_wB, h->n2))) return st;
-  if ((st = zalloc(&h->d_shadow, 7 * h->n0))) return st;
+  if (!h->banded && (st = zalloc(&h->d_wA, h->n1))) return st;
+  if (!h->banded && (st = zalloc(&h->d_wB, h->n2))) return st;
+  if (!h->general && (st = zalloc(&h->d_shadow, 7 * h->n0))) return st;
+  if (h->general && (st = zalloc(&h->d_gpart, (size_t)assemble_gen_parts(g)))) return st;
 
   // assembly launch geometry
   cudaDeviceProp prop;
   ADS_CUDA(h, cudaGetDeviceProperties(&prop, h->dev));
   const int nsm = prop.multiProcessorCount;
   const size_t smem_max = prop.sharedMemPerMultiprocessor;
-  {
+  if (!h->general) {
     // expected residency of the step's assembly: the FP32 kernel 3 CTAs/SM at
     // p <= 2, else 2; the double-float and FP64 kernels 2 at p <= 2, else 1
     // (registers)
@@ -716,7 +800,7 @@ int create_impl(ads_handle* h) {
     h->asm_niz = (g.E[2] + h->asm_zc - 1) / h->asm_zc;
     h->asm_grid = nsm * 8;  // bound of persistent CTAs; the launch uses the real residency
   }
-  {
+  if (!h->general) {
     h->res_nix = (g.N[0] + RS_TX - 1) / RS_TX;
     h->res_niy = (g.N[1] + RS_TY - 1) / RS_TY;
     h->res_zc = std::min(g.N[2], 32);
@@ -725,7 +809,7 @@ int create_impl(ads_handle* h) {
     h->upd_niy = (g.N[1] + resid_update_rows() - 1) / resid_update_rows();
     h->upd_grid = h->res_nix * h->upd_niy * h->res_niz;
   }
-  {
+  if (!h->general) {
     // spill-slab membership of each DOF index (the assembly's bricks spill the
     // first p DOFs of every brick after the first one into the shadows)
     auto in_slab = [&](int v, int tile, int nitems) { return v >= tile && (v % tile) < h->P && (v / tile) <= nitems - 1; };
@@ -751,6 +835,7 @@ int create_impl(ads_handle* h) {
   ADS_CUDA(h, cudaMemset(h->d_flags, 0, sizeof(int) * FL_COUNT));
   if ((st = ensure_hist(h, 64))) return st;
 
+  if (h->banded) return ADS_OK;  // no sweep, no tensor map
   bool ok = true;
   ok &= make_l0_out(h, &h->tm_u_out64, h->d_u, false);
   ok &= make_l0_out(h, &h->tm_r_out64, h->d_r, false);
@@ -832,12 +917,13 @@ int ads_create(const int n[3], const int p[3], const ads_opts* opts, ads_handle*
   *out = nullptr;
   for (int d = 0; d < 3; ++d)
     if (p[d] < 0 || n[d] < p[d]) return ADS_ERR_ARG;
-  if (p[0] != p[1] || p[1] != p[2] || p[0] < 1 || p[0] > 4) return ADS_ERR_UNSUPPORTED;
+  for (int d = 0; d < 3; ++d)
+    if (p[d] < 1 || p[d] > 4) return ADS_ERR_UNSUPPORTED;
   ads_handle* h = new (std::nothrow) ads_handle();
   if (!h) return ADS_ERR_ALLOC;
   for (int d = 0; d < 3; ++d) { h->n[d] = n[d]; h->p[d] = p[d]; }
-  h->P = p[0];
-  h->Q = p[0] + 1;
+  h->P = std::max(p[0], std::max(p[1], p[2]));
+  h->Q = h->P + 1;
   if (opts) h->opts = *opts;
   else ads_default_opts(&h->opts);
   if (h->opts.precision != ADS_PREC_FP64 && h->opts.precision != ADS_PREC_MIXED &&
@@ -870,7 +956,7 @@ int ads_dims(const ads_handle* h, int nelem[3], int ndof[3], int nq[3]) {
   for (int d = 0; d < 3; ++d) {
     if (nelem) nelem[d] = h->g.E[d];
     if (ndof) ndof[d] = h->g.N[d];
-    if (nq) nq[d] = h->g.Q;
+    if (nq) nq[d] = h->g.q[d];
   }
   return ADS_OK;
 }
@@ -1092,16 +1178,15 @@ int ads_multistep(ads_handle* h, const double mix[12], double* l2norm) {
     } else if (h->form == ADS_FORM_HEAT) {
       ADS_CUDA(h, cudaMemcpyAsync(h->d_ms, h->d_un, bytes, cudaMemcpyDeviceToDevice, h->stream));
       RUN(h, "axpby", 1, launch_axpby(h->d_ms, h->d_u, -1.0, 1.0, (long long)h->n0, h->stream));
-      ResidualArgs ra = residual_args(h, h->d_ms, nullptr, h->d_r);  // d_r = M (u^n - current)
-      RUN(h, "mass_apply", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
+      if ((st = enqueue_mass(h, h->d_ms, nullptr, h->d_r, "mass_apply"))) return st;  // d_r = M (u^n - current)
       RUN(h, "add", 1, launch_add(h->d_F, h->d_r, (long long)h->n0, h->stream));
     }
     // Sub_Step's three solves with the mix, in place on F (L0)
-    RUN(h, "band_solve_x", 1, launch_band_solve(h->d_F, Ny, Nz, g.PX, g.PX * Ny, 1, (int)Nx, h->P, h->P,
+    RUN(h, "band_solve_x", 1, launch_band_solve(h->d_F, Ny, Nz, g.PX, g.PX * Ny, 1, (int)Nx, h->p[0], h->p[0],
                                                 h->d_mab[0], h->d_mpiv[0], h->stream));
-    RUN(h, "band_solve_y", 1, launch_band_solve(h->d_F, Nx, Nz, 1, g.PX * Ny, g.PX, (int)Ny, h->P, h->P,
+    RUN(h, "band_solve_y", 1, launch_band_solve(h->d_F, Nx, Nz, 1, g.PX * Ny, g.PX, (int)Ny, h->p[1], h->p[1],
                                                 h->d_mab[1], h->d_mpiv[1], h->stream));
-    RUN(h, "band_solve_z", 1, launch_band_solve(h->d_F, Nx, Ny, 1, g.PX, g.PX * Ny, (int)Nz, h->P, h->P,
+    RUN(h, "band_solve_z", 1, launch_band_solve(h->d_F, Nx, Ny, 1, g.PX, g.PX * Ny, (int)Nz, h->p[2], h->p[2],
                                                 h->d_mab[2], h->d_mpiv[2], h->stream));
     ADS_CUDA(h, cudaMemcpyAsync(h->d_u, h->d_F, bytes, cudaMemcpyDeviceToDevice, h->stream));
   }
@@ -1229,8 +1314,7 @@ int ads_apply_mass(ads_handle* h, const double* u, double* out) {
   ADS_CUDA(h, cudaSetDevice(h->dev));
   int st = copy_l0_in(h, h->d_F, u, cudaMemcpyHostToDevice);
   if (st) return st;
-  ResidualArgs ra = residual_args(h, h->d_F, nullptr, h->d_r);
-  RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
+  if ((st = enqueue_mass(h, h->d_F, nullptr, h->d_r, "residual_f64"))) return st;
   if ((st = copy_l0_out(h, out, h->d_r, cudaMemcpyDeviceToHost))) return st;
   return check_flags(h);
 }
@@ -1240,6 +1324,19 @@ int ads_reorder(ads_handle* h, int kind, const double* in, double* out) {
   ADS_CUDA(h, cudaSetDevice(h->dev));
   const Geometry& g = h->g;
   const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
+  if (kind != ADS_REORDER_FOR_Y && kind != ADS_REORDER_FOR_Z && kind != ADS_REORDER_FOR_X)
+    return fail(h, ADS_ERR_ARG, "unknown reorder kind");
+  if (h->banded) {
+    // no transposing sweeps here: a plain permutation of dense arrays (the
+    // packed stage buffer in, d_r as a dense out)
+    int st = ensure_stage(h);
+    if (st) return st;
+    const size_t bytes = sizeof(double) * (size_t)Nx * Ny * Nz;
+    ADS_CUDA(h, cudaMemcpyAsync(h->d_stage, in, bytes, cudaMemcpyHostToDevice, h->stream));
+    RUN(h, "permute", 1, launch_permute(h->d_stage, h->d_r, g, kind, h->stream));
+    ADS_CUDA(h, cudaMemcpyAsync(out, h->d_r, bytes, cudaMemcpyDeviceToHost, h->stream));
+    return check_flags(h);
+  }
   const CUtensorMap* tout;
   const double* src;
   double* dst;
@@ -1325,8 +1422,7 @@ int ads_heat_adjoint(ads_handle* h, int K, int ck, const double* u0, const doubl
     // loss = 1/2 e^T M e, e = u^K - ut; lambda^K = M e
     ADS_CUDA(h, cudaMemcpyAsync(e, h->d_u, sizeof(double) * n0, cudaMemcpyDeviceToDevice, h->stream));
     RUN(h, "axpby", 1, launch_axpby(e, d_ut, -1.0, 1.0, (long long)n0, h->stream));
-    ResidualArgs ra = residual_args(h, e, nullptr, lam);
-    RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
+    if ((s = enqueue_mass(h, e, nullptr, lam, "residual_f64"))) return s;
     RUN(h, "dot", 2, launch_dot(e, lam, (long long)n0, dpart, 512, h->d_scal + SC_DOT, h->stream));
     double Lval = 0.0;
     ADS_CUDA(h, cudaMemcpyAsync(&Lval, h->d_scal + SC_DOT, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -1346,8 +1442,14 @@ int ads_heat_adjoint(ads_handle* h, int K, int ck, const double* u0, const doubl
       }
       for (int n = s1 - 1; n >= s0; --n) {
         // mu = M^{-T} lambda (transposed sweeps, FP64)
-        if ((s = enqueue_solve64(h, lam, &tm_mu_out, true))) return s;
-        if (gk) RUN(h, "kappa_grad", 1, launch_kappa_grad(h->g, seg + (size_t)(n - s0) * n0, mu, h->dt, gk, t64[0], t64[1], t64[2], h->stream));
+        if ((s = enqueue_solve64(h, lam, &tm_mu_out, true, mu))) return s;
+        if (gk) {
+          const double* un = seg + (size_t)(n - s0) * n0;
+          if (h->general)
+            RUN(h, "kappa_grad", 1, launch_kappa_grad_gen(h->g, un, mu, h->dt, gk, t64[0], t64[1], t64[2], h->stream));
+          else
+            RUN(h, "kappa_grad", 1, launch_kappa_grad(h->g, un, mu, h->dt, gk, t64[0], t64[1], t64[2], h->stream));
+        }
         // lambda = A^T mu: the heat operator is symmetric, so the same assembly
         // kernels apply it (the source term does not depend on u and is left out)
         if ((s = enqueue_assemble(h, mu, lam, false, false, false))) return s;
@@ -1421,7 +1523,7 @@ int ads_heat_jvp(ads_handle* h, int K, const double* u0, const double* du0, cons
       // A w^n (+ t), solved into w^{n+1}
       if ((s = enqueue_assemble(h, w, h->d_F, false, false, false))) return s;
       if (dkappa_qp) RUN(h, "add", 1, launch_add(h->d_F, t, (long long)n0, h->stream));
-      if ((s = enqueue_solve64(h, h->d_F, &tm_w_out, false))) return s;
+      if ((s = enqueue_solve64(h, h->d_F, &tm_w_out, false, w))) return s;
       // the forward step u^n -> u^{n+1}
       if ((s = enqueue_step(h))) return s;
     }
@@ -1528,6 +1630,7 @@ namespace ads {
 void handle_noalloc_view(ads_handle* h, NoallocView* v) {
   v->dev = h->dev;
   v->P = h->P;
+  v->general = h->general;
   v->grid = h->res_grid;
   v->stream = h->stream;
   v->args = residual_args(h, nullptr, nullptr, nullptr);

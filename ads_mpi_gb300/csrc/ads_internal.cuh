@@ -68,8 +68,9 @@ struct DfTabs3 {
 // ---------------------------------------------------------------------------
 struct Geometry {
   int E[3];      // elements per axis
-  int N[3];      // DOFs per axis (E + P)
-  int P, Q;
+  int N[3];      // DOFs per axis (E + p)
+  int P, Q;      // the common degree and Gauss points per axis (the largest if they differ)
+  int p[3], q[3];  // degree and Gauss points of each axis
   long long PX, PY, PZ;  // padded pitches of the three layouts (elements)
   // L0 index: x + PX*(y + Ny*z); L1 index: y + PY*(x + Nx*z); L2 index: z + PZ*(x + Nx*y)
 };
@@ -275,6 +276,41 @@ cudaError_t launch_kappa_grad(const Geometry& g, const double* u, const double* 
                               double* gk, const AxisTab<double>& tx, const AxisTab<double>& ty,
                               const AxisTab<double>& tz, cudaStream_t s);
 
+// ---------------------------------------------------------------------------
+// General geometry (k_general.cu): per-axis degrees p[3] (1..4 each, not all
+// equal).  FP64 kernels with the degrees as run-time values: one thread per
+// element of one colour class for the assembly (elements of a class share no
+// DOF, so the scatter needs no atomics and the sum order is fixed), one thread
+// per DOF for the mass product.
+// ---------------------------------------------------------------------------
+struct GenAssembleArgs {
+  Geometry g;
+  int form;             // ADS_FORM_PROJECT or ADS_FORM_HEAT
+  int incr;             // heat: leave out the mass term J W v u
+  double dt, kappa;
+  const double* u;      // L0 coefficients
+  double* F;            // L0 output, accumulated (zeroed before the first colour)
+  const double* fqp;    // qp-grid layout, may be null
+  const double* kqp;    // qp-grid layout, may be null
+  const double* nn[3];  // per axis [E][q][p+1][2]
+  const double* jw[3];  // per axis [E][q]
+  double* part;         // l2 partial per (colour, block)
+};
+// all colour classes in order, then the l2norm into scal[SC_L2]
+cudaError_t launch_assemble_gen(const GenAssembleArgs& a, double* scal, cudaStream_t s);
+// partials needed by launch_assemble_gen
+long long assemble_gen_parts(const Geometry& g);
+// r = F - (Mx (x) My (x) Mz) u (or M u with F null), band[d][(m+p_d)*N_d + i] = M_{i,i+m}
+cudaError_t launch_residual_gen(const Geometry& g, const double* u, const double* F, double* r,
+                                const double* const band[3], cudaStream_t s);
+// dL/dkappa at the points, as launch_kappa_grad
+cudaError_t launch_kappa_grad_gen(const Geometry& g, const double* u, const double* mu, double dt, double* gk,
+                                  const AxisTab<double>& tx, const AxisTab<double>& ty, const AxisTab<double>& tz,
+                                  cudaStream_t s);
+// the reorders of ReorderRHSFor{Y,Z,X} as plain permutations (kind: ADS_REORDER_*),
+// dense arrays in and out
+cudaError_t launch_permute(const double* in, double* out, const Geometry& g, int kind, cudaStream_t s);
+
 // FMA throughput of the FP32 or FP64 pipe (TFLOP/s, an FMA counted as 2 flops)
 cudaError_t measure_fma_peak(bool fp64, double* tflops);
 
@@ -285,6 +321,7 @@ size_t assemble_smem_bytes(int P, bool fp32);
 // Nx of caller-owned arrays.  No buffer of the handle is used.
 struct NoallocView {
   int dev = 0, P = 0, grid = 0;
+  bool general = false;  // unequal degrees: the tuned residual does not apply
   cudaStream_t stream = nullptr;
   ResidualArgs args{};
   long long* launches = nullptr;

@@ -638,26 +638,23 @@ cudaError_t launch_record(double* scal, int* flags, double* hist, int cap, cudaS
 // fastest).  The host tabulates each axis's span and p+1 nonzero B-splines
 // per sample; the (p+1)^3 products are summed in the reference's order.
 // ---------------------------------------------------------------------------
-template <int P>
 __global__ void k_eval_grid(const double* __restrict__ u, Geometry g, const double* __restrict__ tab,
                             const int* __restrict__ first, int rx, int ry, int rz, double* __restrict__ vals) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long n = (long long)rx * ry * rz;
   if (idx >= n) return;
   const int ix = (int)(idx % rx), iy = (int)((idx / rx) % ry), iz = (int)(idx / ((long long)rx * ry));
-  // tables: x samples, then y, then z
-  const double* bx = tab + (size_t)ix * (P + 1);
-  const double* by = tab + (size_t)(rx + iy) * (P + 1);
-  const double* bz = tab + (size_t)(rx + ry + iz) * (P + 1);
+  const int sx = g.p[0] + 1, sy = g.p[1] + 1, sz = g.p[2] + 1;
+  // tables: x samples (p_x + 1 values each), then y, then z
+  const double* bx = tab + (size_t)ix * sx;
+  const double* by = tab + (size_t)rx * sx + (size_t)iy * sy;
+  const double* bz = tab + (size_t)rx * sx + (size_t)ry * sy + (size_t)iz * sz;
   const int x0 = first[ix], y0 = first[rx + iy], z0 = first[rx + ry + iz];
   const int Ny = g.N[1];
   double val = 0.0;
-#pragma unroll
-  for (int a = 0; a <= P; ++a)
-#pragma unroll
-    for (int b = 0; b <= P; ++b)
-#pragma unroll
-      for (int c = 0; c <= P; ++c) {
+  for (int a = 0; a < sx; ++a)
+    for (int b = 0; b < sy; ++b)
+      for (int c = 0; c < sz; ++c) {
         const double w = bx[a] * by[b] * bz[c];
         val = val + w * u[(size_t)(x0 + a) + (size_t)g.PX * ((size_t)(y0 + b) + (size_t)Ny * (z0 + c))];
       }
@@ -668,13 +665,9 @@ cudaError_t launch_eval_grid(const double* u, const Geometry& g, const double* t
                              int ry, int rz, double* vals, cudaStream_t s) {
   const long long n = (long long)rx * ry * rz;
   const unsigned blocks = (unsigned)((n + 255) / 256);
-  switch (g.P) {
-    case 1: k_eval_grid<1><<<blocks, 256, 0, s>>>(u, g, tab, first, rx, ry, rz, vals); break;
-    case 2: k_eval_grid<2><<<blocks, 256, 0, s>>>(u, g, tab, first, rx, ry, rz, vals); break;
-    case 3: k_eval_grid<3><<<blocks, 256, 0, s>>>(u, g, tab, first, rx, ry, rz, vals); break;
-    case 4: k_eval_grid<4><<<blocks, 256, 0, s>>>(u, g, tab, first, rx, ry, rz, vals); break;
-    default: return cudaErrorInvalidValue;
-  }
+  for (int d = 0; d < 3; ++d)
+    if (g.p[d] < 1 || g.p[d] > 4) return cudaErrorInvalidValue;
+  k_eval_grid<<<blocks, 256, 0, s>>>(u, g, tab, first, rx, ry, rz, vals);
   return cudaGetLastError();
 }
 
@@ -739,20 +732,20 @@ cudaError_t launch_repack(const double* src, double* dst, const Geometry& g, boo
   return cudaGetLastError();
 }
 __global__ void k_qp_convert(const double* src, double* dst, Geometry g, int to_grid) {
-  const int Q = g.Q;
+  const int qx = g.q[0], qy = g.q[1], qz = g.q[2];
   const long long Ex = g.E[0], Ey = g.E[1], Ez = g.E[2];
-  const long long total = Ex * Ey * Ez * Q * Q * Q;
-  const long long QX = Ex * Q, QY = Ey * Q;
+  const long long total = Ex * Ey * Ez * qx * qy * qz;
+  const long long QX = Ex * qx, QY = Ey * qy;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
     long long t = i;
-    const int kx = (int)(t % Q); t /= Q;
-    const int ky = (int)(t % Q); t /= Q;
-    const int kz = (int)(t % Q); t /= Q;
+    const int kx = (int)(t % qx); t /= qx;
+    const int ky = (int)(t % qy); t /= qy;
+    const int kz = (int)(t % qz); t /= qz;
     const long long ex = t % Ex; t /= Ex;
     const long long ey = t % Ey; t /= Ey;
     const long long ez = t;
-    const long long gi = (ex * Q + kx) + QX * ((ey * Q + ky) + QY * (ez * Q + kz));
+    const long long gi = (ex * qx + kx) + QX * ((ey * qy + ky) + QY * (ez * qz + kz));
     if (to_grid) dst[gi] = src[i];
     else dst[i] = src[gi];
   }
@@ -765,12 +758,12 @@ static int blocks_for(long long n) {
 }
 
 cudaError_t launch_qp_to_grid(const double* src, double* dst, const Geometry& g, cudaStream_t s) {
-  const long long n = (long long)g.E[0] * g.E[1] * g.E[2] * g.Q * g.Q * g.Q;
+  const long long n = (long long)g.E[0] * g.E[1] * g.E[2] * g.q[0] * g.q[1] * g.q[2];
   k_qp_convert<<<blocks_for(n), 256, 0, s>>>(src, dst, g, 1);
   return cudaGetLastError();
 }
 cudaError_t launch_grid_to_qp(const double* src, double* dst, const Geometry& g, cudaStream_t s) {
-  const long long n = (long long)g.E[0] * g.E[1] * g.E[2] * g.Q * g.Q * g.Q;
+  const long long n = (long long)g.E[0] * g.E[1] * g.E[2] * g.q[0] * g.q[1] * g.q[2];
   k_qp_convert<<<blocks_for(n), 256, 0, s>>>(src, dst, g, 0);
   return cudaGetLastError();
 }

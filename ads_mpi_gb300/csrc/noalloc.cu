@@ -99,6 +99,8 @@ extern "C" int ads_residual_noalloc(ads_handle* h, const double* d_F, const doub
   if (!h || !d_u || !d_r) return ADS_ERR_ARG;
   ads::NoallocView v;
   ads::handle_noalloc_view(h, &v);
+  if (v.general)
+    return ads::handle_fail(h, ADS_ERR_UNSUPPORTED, "ads_residual_noalloc needs equal degrees on all axes");
   cudaError_t e = cudaSetDevice(v.dev);
   if (e != cudaSuccess) return ads::handle_cuda_fail(h, e, "ads_residual_noalloc: cudaSetDevice");
   if (v.grid > kMaxCtas)

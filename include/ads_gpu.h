@@ -109,8 +109,13 @@ typedef struct ads_stats {
 int ads_default_opts(ads_opts* opts);
 
 /* initialize: n[3] = functions minus one per axis, p[3] = degrees.
- * The GPU kernels need p[0] == p[1] == p[2] in {1,2,3,4} and >= 2 elements
- * per axis; anything else returns ADS_ERR_UNSUPPORTED. */
+ * Each degree must be in {1,2,3,4} and each axis needs >= 2 elements; anything
+ * else returns ADS_ERR_UNSUPPORTED.  Equal degrees with at most 448 DOFs per
+ * axis run the tuned kernels in every precision.  Unequal degrees, or a longer
+ * axis, run FP64 only (general assembly and mass kernels for unequal degrees,
+ * banded LU solves along every axis): ADS_PREC_MIXED and ADS_PREC_MIXED_FAST
+ * return ADS_ERR_UNSUPPORTED there, as do the oil form and
+ * ads_residual_noalloc with unequal degrees. */
 int ads_create(const int n[3], const int p[3], const ads_opts* opts, ads_handle** out);
 int ads_destroy(ads_handle* h);
 const char* ads_last_error(const ads_handle* h);

@@ -400,7 +400,7 @@ def test_errors_are_status_codes(ads_mod):
         ads_mod.ADS((10, 10, 10), (5, 5, 5))
     assert e.value.status == 7
     with pytest.raises(ads_mod.ADSError) as e:
-        ads_mod.ADS((10, 10, 10), (2, 3, 2))
+        ads_mod.ADS((10, 10, 10), (2, 5, 2))
     assert e.value.status == 7
     g, _ = make(ads_mod, 6, 2)
     with pytest.raises(ads_mod.ADSError) as e:
