@@ -27,6 +27,13 @@ module ads_gpu
       integer(c_int) :: device
    end type ads_opts
 
+   type, bind(c) :: ads_stats
+      real(c_double) :: l2norm
+      real(c_double) :: rel_residual
+      integer(c_int) :: refinements
+      integer(c_int) :: converged
+   end type ads_stats
+
    type :: ads_gpu_handle
       type(c_ptr) :: h = c_null_ptr
       integer(c_int) :: nelem(3), ndof(3), nq(3)
@@ -104,6 +111,55 @@ module ads_gpu
          import :: c_int, c_ptr, c_double
          type(c_ptr), value :: h
          real(c_double), intent(out) :: l2norm
+      end function
+      integer(c_int) function ads_steps(h, k, l2norms) bind(c, name="ads_steps")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         integer(c_int), value :: k
+         real(c_double), intent(out) :: l2norms(*)
+      end function
+      integer(c_int) function ads_get_stats(h, st) bind(c, name="ads_get_stats")
+         import :: c_int, c_ptr, ads_stats
+         type(c_ptr), value :: h
+         type(ads_stats), intent(out) :: st
+      end function
+      integer(c_int) function ads_assemble(h, F, l2norm) bind(c, name="ads_assemble")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         real(c_double), intent(out) :: F(*)
+         real(c_double), intent(out) :: l2norm
+      end function
+      integer(c_int) function ads_solve(h, F, u) bind(c, name="ads_solve")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         real(c_double), intent(in) :: F(*)
+         real(c_double), intent(out) :: u(*)
+      end function
+      integer(c_int) function ads_apply_mass(h, u, out) bind(c, name="ads_apply_mass")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         real(c_double), intent(in) :: u(*)
+         real(c_double), intent(out) :: out(*)
+      end function
+      integer(c_int) function ads_heat_adjoint(h, k, checkpoint_every, u0, u_target, loss, grad_u0, &
+                                               grad_kappa_qp) bind(c, name="ads_heat_adjoint")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         integer(c_int), value :: k, checkpoint_every
+         real(c_double), intent(in) :: u0(*), u_target(*)
+         real(c_double), intent(out) :: loss
+         type(c_ptr), value :: grad_u0, grad_kappa_qp
+      end function
+      integer(c_int) function ads_heat_jvp(h, k, u0, du0, dkappa_qp, uk, duk) bind(c, name="ads_heat_jvp")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         integer(c_int), value :: k
+         real(c_double), intent(in) :: u0(*)
+         type(c_ptr), value :: du0, dkappa_qp, uk, duk
+      end function
+      type(c_ptr) function ads_status_string(status) bind(c, name="ads_status_string")
+         import :: c_int, c_ptr
+         integer(c_int), value :: status
       end function
    end interface
 
