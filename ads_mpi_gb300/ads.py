@@ -84,6 +84,8 @@ ABI = [
     ("ads_timing_enable", [ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     ("ads_timing_read", [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, _dp, _ip, ctypes.c_int, _ip], ctypes.c_int),
     ("ads_timing_reset", [ctypes.c_void_p], ctypes.c_int),
+    ("ads_phase_timing_read", [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, _dp, _ip, ctypes.c_int, _ip],
+     ctypes.c_int),
     ("ads_launch_count", [ctypes.c_void_p], ctypes.c_longlong),
     ("ads_launch_count_reset", [ctypes.c_void_p], ctypes.c_int),
 ]
@@ -402,6 +404,18 @@ class ADS:
         n = ctypes.c_int(0)
         self._check(self._L.ads_timing_read(self.h, names, 8192, _ptr(t), c.ctypes.data_as(_ip), max_kernels,
                                             ctypes.byref(n)))
+        nm = names.value.decode().split(",") if n.value else []
+        return {nm[i]: (float(t[i]), int(c[i])) for i in range(n.value)}
+
+    def phase_timing_read(self, max_phases=16):
+        """Per-phase CUDA-event totals {name: (ms, launches)} under the
+        reference's PERFORMANCE names ("Form 3D RHS", "Solve 1", ...)."""
+        names = ctypes.create_string_buffer(1024)
+        t = np.zeros(max_phases)
+        c = np.zeros(max_phases, dtype=np.int32)
+        n = ctypes.c_int(0)
+        self._check(self._L.ads_phase_timing_read(self.h, names, 1024, _ptr(t), c.ctypes.data_as(_ip), max_phases,
+                                                  ctypes.byref(n)))
         nm = names.value.decode().split(",") if n.value else []
         return {nm[i]: (float(t[i]), int(c[i])) for i in range(n.value)}
 

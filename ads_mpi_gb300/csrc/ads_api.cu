@@ -17,6 +17,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "ads_internal.cuh"
 #include "setup.h"
 
@@ -146,6 +148,13 @@ struct ads_handle {
   std::vector<int> tcount;
   std::vector<cudaEvent_t> evpool;
   std::vector<int> pending;  // kernel index of each recorded event pair
+  // phases under the reference's PERFORMANCE names (src/ADS.F90:497-754):
+  // the current one, and the per-phase totals of the timed launches
+  const char* phase = "Other";
+  std::vector<std::string> pnames;
+  std::vector<double> pms;
+  std::vector<int> pcount;
+  std::vector<int> ppending;  // phase index of each recorded event pair
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   long long launches = 0;
 
@@ -186,10 +195,29 @@ void resolve_timing(ads_handle* h) {
     if (cudaEventElapsedTime(&ms, h->evpool[2 * i], h->evpool[2 * i + 1]) == cudaSuccess) {
       h->tms[h->pending[i]] += ms;
       h->tcount[h->pending[i]] += 1;
+      h->pms[h->ppending[i]] += ms;
+      h->pcount[h->ppending[i]] += 1;
     }
   }
   h->pending.clear();
+  h->ppending.clear();
 }
+
+// A phase of the step named as the reference's PERFORMANCE output names it
+// ("Form 3D RHS", "Solve 1", ...): an NVTX range over its launches and the
+// phase that the per-kernel timers also add into.
+struct Phase {
+  ads_handle* h;
+  const char* prev;
+  Phase(ads_handle* hh, const char* name) : h(hh), prev(hh->phase) {
+    h->phase = name;
+    nvtxRangePushA(name);
+  }
+  ~Phase() {
+    nvtxRangePop();
+    h->phase = prev;
+  }
+};
 
 template <typename F>
 int run_kernel(ads_handle* h, const char* name, int nlaunch, F&& f) {
@@ -204,6 +232,14 @@ int run_kernel(ads_handle* h, const char* name, int nlaunch, F&& f) {
       h->tcount.push_back(0);
     }
     if (h->pending.size() >= 4096) resolve_timing(h);
+    size_t pk = 0;
+    for (; pk < h->pnames.size(); ++pk)
+      if (h->pnames[pk] == h->phase) break;
+    if (pk == h->pnames.size()) {
+      h->pnames.push_back(h->phase);
+      h->pms.push_back(0.0);
+      h->pcount.push_back(0);
+    }
     const size_t i = h->pending.size();
     while (h->evpool.size() < 2 * (i + 1)) {
       cudaEvent_t ev;
@@ -216,6 +252,7 @@ int run_kernel(ads_handle* h, const char* name, int nlaunch, F&& f) {
     if (have) {
       cudaEventRecord(h->evpool[2 * i + 1], h->stream);
       h->pending.push_back((int)k);
+      h->ppending.push_back((int)pk);
     }
   } else {
     e = f();
@@ -383,6 +420,7 @@ int enqueue_assemble_gen(ads_handle* h, const double* u, double* F, bool incr, b
 
 int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool incr, bool with_f,
                      const double* kqp_override = nullptr) {
+  Phase ph(h, "Form 3D RHS");
   if (h->general) return enqueue_assemble_gen(h, u, F, incr, with_f, kqp_override);
   AssembleArgs a = assemble_args(h, u, F, with_f);
   if (kqp_override) a.kqp = kqp_override;
@@ -425,21 +463,21 @@ int enqueue_solve64(ads_handle* h, const double* in, const CUtensorMap* tm_out, 
     const Geometry& g = h->g;
     const long long Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
     if (in != out) ADS_CUDA(h, cudaMemcpyAsync(out, in, sizeof(double) * h->n0, cudaMemcpyDeviceToDevice, h->stream));
-    RUN(h, "band_solve_x", 1, launch_band_solve(out, Ny, Nz, g.PX, g.PX * Ny, 1, (int)Nx, h->p[0], h->p[0],
-                                                h->d_gab[0], h->d_gpiv[0], h->stream));
-    RUN(h, "band_solve_y", 1, launch_band_solve(out, Nx, Nz, 1, g.PX * Ny, g.PX, (int)Ny, h->p[1], h->p[1],
-                                                h->d_gab[1], h->d_gpiv[1], h->stream));
-    RUN(h, "band_solve_z", 1, launch_band_solve(out, Nx, Ny, 1, g.PX, g.PX * Ny, (int)Nz, h->p[2], h->p[2],
-                                                h->d_gab[2], h->d_gpiv[2], h->stream));
+    { Phase ph(h, "Solve 1"); RUN(h, "band_solve_x", 1, launch_band_solve(out, Ny, Nz, g.PX, g.PX * Ny, 1, (int)Nx, h->p[0], h->p[0],
+                                                h->d_gab[0], h->d_gpiv[0], h->stream)); }
+    { Phase ph(h, "Solve 2"); RUN(h, "band_solve_y", 1, launch_band_solve(out, Nx, Nz, 1, g.PX * Ny, g.PX, (int)Ny, h->p[1], h->p[1],
+                                                h->d_gab[1], h->d_gpiv[1], h->stream)); }
+    { Phase ph(h, "Solve 3"); RUN(h, "band_solve_z", 1, launch_band_solve(out, Nx, Ny, 1, g.PX, g.PX * Ny, (int)Nz, h->p[2], h->p[2],
+                                                h->d_gab[2], h->d_gpiv[2], h->stream)); }
     return ADS_OK;
   }
   double* const* fac = trans ? h->d_tfac64 : h->d_fac64;
   SweepArgs ax = sweep_args(h, 0, fac[0], in);
-  RUN(h, "sweep_x_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, &h->tm_wA_out64, ax, sweep_grid(h, 0), h->stream));
+  { Phase ph(h, "Solve 1"); RUN(h, "sweep_x_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, &h->tm_wA_out64, ax, sweep_grid(h, 0), h->stream)); }
   SweepArgs ay = sweep_args(h, 1, fac[1], h->d_wA);
-  RUN(h, "sweep_y_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, &h->tm_wB_out64, ay, sweep_grid(h, 1), h->stream));
+  { Phase ph(h, "Solve 2"); RUN(h, "sweep_y_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, &h->tm_wB_out64, ay, sweep_grid(h, 1), h->stream)); }
   SweepArgs az = sweep_args(h, 2, fac[2], h->d_wB);
-  RUN(h, "sweep_z_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, tm_out, az, sweep_grid(h, 2), h->stream));
+  { Phase ph(h, "Solve 3"); RUN(h, "sweep_z_f64", 1, launch_sweep(h->P, 0, 0, 0, trans, tm_out, az, sweep_grid(h, 2), h->stream)); }
   return ADS_OK;
 }
 
@@ -461,7 +499,9 @@ int enqueue_solve32(ads_handle* h, const void* in, int tin, const double* in_sca
   ax.in_scale_dev = in_scale;
   ax.skip_flag = skip;
   // x: skewed, without the transpose, into wC (L0)
-  RUN(h, nx.c_str(), 1, launch_sweep(h->P, tin, 1, 4, false, &h->tm_wC_out32, ax, sweep_grid(h, 0), h->stream));
+  const bool corr = tag[0] != '\0';  // a refinement correction, not the first solve
+  { Phase ph(h, corr ? "Refinement" : "Solve 1");
+    RUN(h, nx.c_str(), 1, launch_sweep(h->P, tin, 1, 4, false, &h->tm_wC_out32, ax, sweep_grid(h, 0), h->stream)); }
   // y: column form in place on wC (lines x contiguous, positions y at stride PX, tiles over z)
   CSweepArgs cy{};
   cy.L = (int)Ny; cy.nl = (int)Nx; cy.n3 = (int)Nz;
@@ -471,7 +511,7 @@ int enqueue_solve32(ads_handle* h, const void* in, int tin, const double* in_sca
   cy.out_ps = g.PX; cy.out_ts = g.PX * Ny;
   cy.fac = h->d_fac32[1];
   cy.skip_flag = skip;
-  RUN(h, ny.c_str(), 1, launch_csweep(h->P, 0, cy, h->stream));
+  { Phase ph(h, corr ? "Refinement" : "Solve 2"); RUN(h, ny.c_str(), 1, launch_csweep(h->P, 0, cy, h->stream)); }
   CSweepArgs cz{};
   cz.L = (int)Nz; cz.nl = (int)Nx; cz.n3 = (int)Ny;
   cz.in = h->d_wC;
@@ -481,7 +521,7 @@ int enqueue_solve32(ads_handle* h, const void* in, int tin, const double* in_sca
   cz.fac = h->d_fac32[2];
   cz.out_scale_dev = out_scale;
   cz.skip_flag = skip;
-  RUN(h, nz.c_str(), 1, launch_csweep(h->P, final_mode, cz, h->stream));
+  { Phase ph(h, corr ? "Refinement" : "Solve 3"); RUN(h, nz.c_str(), 1, launch_csweep(h->P, final_mode, cz, h->stream)); }
   return ADS_OK;
 }
 
@@ -502,6 +542,7 @@ int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready, bool f32_in
                      : enqueue_solve32(h, h->d_F, 0, in_s, out_s, 1, nullptr, "", x);
   if (st) return st;
   const int* conv = h->d_flags + FL_CONV;
+  Phase ph(h, "Refinement");
   auto residual = [&](bool want_ff) -> int {
     ResidualArgs ra = residual_args(h, x, h->d_F, h->d_r);
     ra.skip_flag = conv;
@@ -555,6 +596,7 @@ int enqueue_step(ads_handle* h) {
   if (is_mixed(h) && (h->form == ADS_FORM_HEAT || h->form == ADS_FORM_OIL)) {
     if ((st = enqueue_assemble(h, h->d_u, h->d_F, true, true, true))) return st;
     if ((st = enqueue_solve_mixed(h, h->d_delta, true, true))) return st;
+    Phase ph(h, "Update");
     RUN(h, "update", 1, launch_add(h->d_u, h->d_delta, (long long)h->n0, h->stream));
   } else if (is_mixed(h)) {
     if ((st = enqueue_assemble(h, h->d_u, h->d_F, false, false, true))) return st;
@@ -1182,10 +1224,13 @@ int ads_multistep(ads_handle* h, const double mix[12], double* l2norm) {
       RUN(h, "add", 1, launch_add(h->d_F, h->d_r, (long long)h->n0, h->stream));
     }
     // Sub_Step's three solves with the mix, in place on F (L0)
+    Phase phx(h, "Solve 1");
     RUN(h, "band_solve_x", 1, launch_band_solve(h->d_F, Ny, Nz, g.PX, g.PX * Ny, 1, (int)Nx, h->p[0], h->p[0],
                                                 h->d_mab[0], h->d_mpiv[0], h->stream));
+    Phase phy(h, "Solve 2");
     RUN(h, "band_solve_y", 1, launch_band_solve(h->d_F, Nx, Nz, 1, g.PX * Ny, g.PX, (int)Ny, h->p[1], h->p[1],
                                                 h->d_mab[1], h->d_mpiv[1], h->stream));
+    Phase phz(h, "Solve 3");
     RUN(h, "band_solve_z", 1, launch_band_solve(h->d_F, Nx, Ny, 1, g.PX, g.PX * Ny, (int)Nz, h->p[2], h->p[2],
                                                 h->d_mab[2], h->d_mpiv[2], h->stream));
     ADS_CUDA(h, cudaMemcpyAsync(h->d_u, h->d_F, bytes, cudaMemcpyDeviceToDevice, h->stream));
@@ -1592,6 +1637,27 @@ int ads_timing_reset(ads_handle* h) {
   if (!h) return ADS_ERR_ARG;
   resolve_timing(h);
   h->tnames.clear(); h->tms.clear(); h->tcount.clear();
+  h->pnames.clear(); h->pms.clear(); h->pcount.clear();
+  return ADS_OK;
+}
+
+int ads_phase_timing_read(ads_handle* h, char* names, int names_len, double* times_ms, int* launches,
+                          int max_phases, int* n_phases) {
+  if (!h) return ADS_ERR_ARG;
+  resolve_timing(h);
+  const int n = (int)std::min<size_t>(h->pnames.size(), (size_t)std::max(max_phases, 0));
+  std::string all;
+  for (int i = 0; i < n; ++i) {
+    if (i) all += ",";
+    all += h->pnames[i];
+    if (times_ms) times_ms[i] = h->pms[i];
+    if (launches) launches[i] = h->pcount[i];
+  }
+  if (names && names_len > 0) {
+    std::strncpy(names, all.c_str(), (size_t)names_len - 1);
+    names[names_len - 1] = '\0';
+  }
+  if (n_phases) *n_phases = n;
   return ADS_OK;
 }
 

@@ -281,11 +281,13 @@ def time_e2e(torch, g, K, host_in, host_out):
     return time.perf_counter() - t0
 
 
-def kernel_profile(g, K):
+def kernel_profile(g, K, phases=None):
     g.timing(True)
     g.timing_reset()
     g.steps(K)
     t = g.timing_read()
+    if phases is not None:
+        phases.update(g.phase_timing_read())
     g.timing(False)
     return t
 
@@ -732,9 +734,11 @@ def run_ours(args, world, rank, local):
 
     # per-kernel CUDA events (a separate pass over the same steps)
     prof = {}
+    phases = {}
     for name, g in handles:
         g.set_coeffs(u0)
-        prof[name] = kernel_profile(g, K)
+        phases[name] = {}
+        prof[name] = kernel_profile(g, K, phases[name])
 
     if rank != 0:
         return
@@ -891,6 +895,8 @@ def run_ours(args, world, rank, local):
         "roofline_sweeps": sweeps,
         "roofline_residual": roof_res,
         "kernel_ms_per_step": {k: v[0] / K for k, v in sorted(pm.items(), key=lambda kv: -kv[1][0])},
+        # the same CUDA-event timings per phase, under the reference's PERFORMANCE names
+        "phase_ms_per_step": {name: {k: v[0] / K for k, v in ph.items()} for name, ph in phases.items()},
         "gpu_launches": res["mixed"]["launches"],
         "cpu_baseline": cpu,
         "other_configs": finite_or_none(aux),

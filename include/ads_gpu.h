@@ -261,6 +261,19 @@ int ads_timing_enable(ads_handle* h, int on);
 int ads_timing_read(ads_handle* h, char* names, int names_len, double* times_ms, int* launches,
                     int max_kernels, int* n_kernels);
 int ads_timing_reset(ads_handle* h);
+/* The same timings summed per phase of the step, named as the reference's
+ * PERFORMANCE output names them (src/ADS.F90:497-754): "Form 3D RHS"
+ * (FormUn + Form3DRHS, with the FP32/double-float scaling pass and the
+ * fixup), "Solve 1", "Solve 2", "Solve 3" (each direction's sweep, which also
+ * does that direction's Gather, Scatter and ReorderRHSFor*: they have no
+ * launches of their own), and, with no counterpart in the reference,
+ * "Refinement" (the mixed solve's FP64 residuals and corrections), "Update"
+ * (u += delta of the mixed heat step) and "Other" (bookkeeping).  The mass
+ * matrices are factorised once at ads_create (the reference's "Mass matrix n"
+ * rebuilds them every substep), so that phase never appears.  Each phase
+ * is also an NVTX range around its launches. */
+int ads_phase_timing_read(ads_handle* h, char* names, int names_len, double* times_ms, int* launches,
+                          int max_phases, int* n_phases);
 /* number of this library's kernel launches since the last reset */
 long long ads_launch_count(const ads_handle* h);
 int ads_launch_count_reset(ads_handle* h);
