@@ -83,7 +83,7 @@ struct ads_handle {
   int* d_gpiv[3] = {nullptr, nullptr, nullptr};
   double* d_gpart = nullptr;  // l2 partials of the general assembly
   float2* d_jwdf[3] = {nullptr, nullptr, nullptr};
-  float* d_band32[3] = {nullptr, nullptr, nullptr};  // FP32 copies for the updated residual
+  float2* d_band32[3] = {nullptr, nullptr, nullptr};  // double-float copies for the updated residual
 
   // device buffers
   double* d_u = nullptr;
@@ -767,7 +767,16 @@ int create_impl(ads_handle* h) {
       if ((st = upload(h, &h->d_gpiv[d], ipiv))) return st;
     }
     std::vector<float> nn32(a.NN.begin(), a.NN.end()), jw32(a.JW.begin(), a.JW.end()), fac32(fac.begin(), fac.end());
-    std::vector<float> dd32(a.DD.begin(), a.DD.end()), band32(a.band.begin(), a.band.end());
+    std::vector<float> dd32(a.DD.begin(), a.DD.end());
+    // double-float copy of a table: the nearest float and the float nearest to the remainder
+    auto split = [](const std::vector<double>& v) {
+      std::vector<float2> o(v.size());
+      for (size_t i = 0; i < v.size(); ++i) {
+        const float hi = (float)v[i];
+        o[i] = make_float2(hi, (float)(v[i] - (double)hi));
+      }
+      return o;
+    };
     int st;
     if ((st = upload(h, &h->d_nn64[d], a.NN))) return st;
     if ((st = upload(h, &h->d_jw64[d], a.JW))) return st;
@@ -779,17 +788,8 @@ int create_impl(ads_handle* h) {
     if ((st = upload(h, &h->d_tfac64[d], tfac))) return st;
     if ((st = upload(h, &h->d_fac32[d], fac32))) return st;
     if ((st = upload(h, &h->d_band[d], a.band))) return st;
-    if ((st = upload(h, &h->d_band32[d], band32))) return st;
+    if ((st = upload(h, &h->d_band32[d], split(a.band)))) return st;
     if (h->opts.precision == ADS_PREC_MIXED) {
-      // double-float tables: the nearest float and the float nearest to the remainder
-      auto split = [](const std::vector<double>& v) {
-        std::vector<float2> o(v.size());
-        for (size_t i = 0; i < v.size(); ++i) {
-          const float hi = (float)v[i];
-          o[i] = make_float2(hi, (float)(v[i] - (double)hi));
-        }
-        return o;
-      };
       if ((st = upload(h, &h->d_nndf[d], split(a.NN)))) return st;
       if ((st = upload(h, &h->d_jwdf[d], split(a.JW)))) return st;
     }

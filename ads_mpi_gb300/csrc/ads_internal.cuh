@@ -161,8 +161,8 @@ struct ResidualArgs {
 
 // Updated residual of an FP32 correction (mixed solve).  r1 = float(r 2^-e)
 // is the scaled FP64 residual that the correction x1 (FP32) was solved for:
-// delta += 2^e x1, and r2 = r1 - M x1 and a = M |x1| are formed in FP32 for
-// the certified bound of k_certify.
+// delta += 2^e x1, r2 = r1 - M x1 with M x1 in double-float arithmetic (FP32
+// at P = 4), and a = M |x1| in FP32, for the certified bound of k_certify.
 struct UpdateArgs {
   Geometry g;
   int zc, nix, niy, niz;
@@ -170,7 +170,7 @@ struct UpdateArgs {
   const float* r1;           // L0: the scaled FP32 residual it solved for
   double* delta;             // L0: += 2^e x1
   const double* out_scale;   // 2^e
-  const float* band[3];      // FP32 copies (round to nearest) of the 1-D mass bands
+  const float2* band[3];     // double-float copies of the 1-D mass bands (.x: the FP32 rounding)
   double* part;              // per CTA: [sum (2^24 r2)^2, sum a^2, sum r1^2]
   const int* skip_flag;
 };

@@ -39,6 +39,26 @@ __device__ __forceinline__ dfl df_mulf(dfl a, float b) {
   return make_float2(p, e);
 }
 
+// s + a * b with b a plain float
+__device__ __forceinline__ dfl df_macf(dfl s, dfl a, float b) {
+  const float p = __fmul_rn(a.x, b);
+  float e = __fmaf_rn(a.x, b, -p);
+  e = __fmaf_rn(a.y, b, e);
+  const float t = __fadd_rn(s.x, p);
+  const float bp = __fsub_rn(t, s.x);
+  const float err = __fadd_rn(__fsub_rn(s.x, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  return make_float2(t, __fadd_rn(s.y, __fadd_rn(err, e)));
+}
+
+// r - a as a float: the two-sum of r and -a.x is exact, then its error and
+// the low part are added, with at most two roundings
+__device__ __forceinline__ float df_sub_to_float(float r, dfl a) {
+  const float t = __fsub_rn(r, a.x);
+  const float bp = __fsub_rn(t, r);
+  const float err = __fadd_rn(__fsub_rn(r, __fsub_rn(t, bp)), __fsub_rn(-a.x, bp));
+  return __fadd_rn(t, __fsub_rn(err, a.y));
+}
+
 // a + b
 __device__ __forceinline__ dfl df_add(dfl a, dfl b) {
   const float t = __fadd_rn(a.x, b.x);

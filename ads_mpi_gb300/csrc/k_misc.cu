@@ -1,8 +1,10 @@
 // k_misc.cu — Kronecker residual (K5), reductions, refinement control, layout
 // conversions and the quadrature-point gradient kernel of the adjoint (K6).
 #include "ads_internal.cuh"
+#include "df32.cuh"
 
 #include <cfloat>
+#include <type_traits>
 
 namespace ads {
 
@@ -216,17 +218,25 @@ cudaError_t launch_decide(const double* part, int n, double tol, bool count_iter
 // The correction x1 solves M x1 = r1 with r1 = float(r 2^-e) and r = F - M x
 // the FP64 residual.  The residual after adding 2^e x1 to x is
 //   F - M (x + 2^e x1) = 2^e (r 2^-e - M x1),
-// and since |r| is already ~1e-7 |F|, computing r1 - M x1 in FP32 leaves an
-// error ~1e-14 |F|, far below refine_tol, so the second FP64 residual of a
-// step is not needed to certify convergence.  The error is bounded
-// rigorously (k_certify): M has non-negative entries (B-splines are
-// non-negative), so each 1-D pass with FP32 band entries m' = fl(m) and an
-// FMA chain of 2P+1 terms returns (A + D) y with |D| <= g_{2P+2} A
-// (g_k = k u / (1 - k u), u = 2^-24), and three passes give
-//   |fl(M x1) - M x1| <= g_K M|x1|,   K = 3 (2P + 2),
-// with M|x1| <= a / (1 - g_K) for the computed a = fl(M |x1|).  With the
-// rounding of r1 itself (u |r1|) and of the subtraction (u |r2| / (1 - u)):
-//   ||r_true|| 2^-e <= (1 + u/(1-u)) ||r2|| + u ||r1|| + g_K/(1-g_K) ||a||.
+// and r2 = r1 - M x1 is formed here with M x1 in double-float arithmetic
+// (df32.cuh: the band entries as float pairs, exact products, two-sum
+// additions; FP32 at P = 4), so the error of r2 is ~1e-19 |F|: the bound
+// below certifies a relative residual of a few 1e-14 after one correction,
+// and the step needs no second FP64 residual to reach a tolerance of 1e-13.
+// The bound is rigorous (k_certify): M has non-negative entries (B-splines
+// are non-negative), so every term of each 1-D pass is bounded by the same
+// pass applied to |x1|.  A double-float multiply-add errs by at most 15 u^2
+// (u = 2^-24) of the sum of |terms| that formed it, so a pass of W = 2P+1
+// terms errs by 15 W u^2 of the pass of |input|; three passes, the float-pair
+// band entries (2^-48 relative each) and the final subtraction give
+//   |fl(M x1) - M x1| <= g_df M|x1|,   g_df = 64 W u^2 >= (45 W + 4) u^2.
+// In FP32 (P = 4) each pass with FP32 band entries m' = fl(m) and an FMA
+// chain of W terms returns (A + D) y with |D| <= g_{W+1} A, so three passes
+// give g_df = g_K (g_k = k u / (1 - k u), K = 3 (2P + 2)).  M|x1| <= a /
+// (1 - g_K) for a = fl(M |x1|) computed in FP32 with the FP32 band entries.
+// With the rounding of r1 itself (u |r1|) and at most two roundings of r2
+// (2u |r2| / (1 - 2u)):
+//   ||r_true|| 2^-e <= (1 + 2u/(1-2u)) ||r2|| + u ||r1|| + g_df/(1-g_K) ||a||.
 // The FP64 rounding of x + 2^e x1 and of the FP64 residual itself are not
 // counted, as for any FP64 residual.  Same tiling as k_residual.
 // ---------------------------------------------------------------------------
@@ -248,13 +258,56 @@ __device__ __forceinline__ void ru_wait() {
 // stay zero (set once).  A CTA owns 32 x RU_TY DOF columns, each thread two
 // rows (ty and ty + 8), so the per-plane work of the staging, the barriers
 // and the loop is shared by two outputs.
+// The M x1 channel: double-float (float2) up to P = 3; FP32 at P = 4, where
+// the float-pair staging would take the static shared memory past 48 KB (the
+// certified bound then uses the FP32 g_K, see launch_certify)
+template <int P>
+struct RuValue {
+  static constexpr bool DF = P <= 3;
+  using T = typename std::conditional<DF, float2, float>::type;
+  static __device__ __forceinline__ T zero() {
+    if constexpr (DF) return make_float2(0.f, 0.f);
+    else return 0.f;
+  }
+  static __device__ __forceinline__ T band(float2 b) {
+    if constexpr (DF) return b;
+    else return b.x;
+  }
+  static __device__ __forceinline__ float hi(T v) {
+    if constexpr (DF) return v.x;
+    else return v;
+  }
+  static __device__ __forceinline__ T mulf(T a, float b) {
+    if constexpr (DF) return df_mulf(a, b);
+    else return a * b;
+  }
+  static __device__ __forceinline__ T macf(T s, T a, float b) {
+    if constexpr (DF) return df_macf(s, a, b);
+    else return fmaf(a, b, s);
+  }
+  static __device__ __forceinline__ T mul(T a, T b) {
+    if constexpr (DF) return df_mul(a, b);
+    else return a * b;
+  }
+  static __device__ __forceinline__ T mac(T s, T a, T b) {
+    if constexpr (DF) return df_mac(s, a, b);
+    else return fmaf(a, b, s);
+  }
+  static __device__ __forceinline__ float sub_to_float(float r, T a) {
+    if constexpr (DF) return df_sub_to_float(r, a);
+    else return r - a;
+  }
+};
+
 constexpr int RU_RING = 8;
 constexpr int RU_PD = 3;
 constexpr int RU_RPT = 2;                          // DOF rows per thread
 constexpr int RU_TY = RU_RPT * (RS_THREADS / RS_TX);  // 16 rows per CTA
 
 template <int P>
-__global__ void __launch_bounds__(RS_THREADS, (P <= 2 ? 3 : 2)) k_resid_update(const UpdateArgs a) {
+__global__ void __launch_bounds__(RS_THREADS, 2) k_resid_update(const UpdateArgs a) {
+  using V = RuValue<P>;
+  using VT = typename V::T;
   constexpr int W = 2 * P + 1;
   constexpr int HX = RS_TX + 2 * P, HY = RU_TY + 2 * P;
   constexpr int PD = RU_PD;
@@ -270,8 +323,9 @@ __global__ void __launch_bounds__(RS_THREADS, (P <= 2 ? 3 : 2)) k_resid_update(c
   constexpr int ZMAX = 32 + 2 * P;                                  // input planes of a chunk (zc <= 32)
   __shared__ float xin[RU_RING][HY * HX];
   __shared__ float r1s_[R1R][RU_RPT][RS_THREADS];
-  __shared__ float bys[RU_TY * HX], bya[RU_TY * HX];
-  __shared__ float cz[ZMAX * W];  // cz[(zin - z0 + P) * W + j] = Mz(zin - P + j, zin), 0 outside the grid
+  __shared__ VT bys[RU_TY * HX];     // y pass of M x1
+  __shared__ float bya[RU_TY * HX];  // y pass of M |x1| (FP32)
+  __shared__ VT cz[ZMAX * W];  // cz[(zin - z0 + P) * W + j] = Mz(zin - P + j, zin), 0 outside the grid
   __shared__ double red[3][RS_THREADS / 32];
 
   if (a.skip_flag != nullptr && *a.skip_flag != 0) return;
@@ -299,14 +353,15 @@ __global__ void __launch_bounds__(RS_THREADS, (P <= 2 ? 3 : 2)) k_resid_update(c
     const int zl = it / W, j = it % W;
     const int zin = z0 - P + zl, zout = zin - P + j;
     // band[(m + P) N + i] = M_{i, i+m}: row zout, column zin, m = P - j
-    cz[it] = (zin >= 0 && zin < Nz && zout >= 0 && zout < Nz) ? a.band[2][(size_t)(2 * P - j) * Nz + zout] : 0.f;
+    cz[it] = (zin >= 0 && zin < Nz && zout >= 0 && zout < Nz) ? V::band(a.band[2][(size_t)(2 * P - j) * Nz + zout])
+                                                              : V::zero();
   }
 
   // the y-pass items of this thread (fixed for every plane): smem offset of
   // their first halo row and their My rows
   int yoff[NYI];
   bool yact[NYI];
-  float byc[NYI][W];
+  VT byc[NYI][W];
 #pragma unroll
   for (int k = 0; k < NYI; ++k) {
     const int it = tid + k * RS_THREADS;
@@ -315,11 +370,11 @@ __global__ void __launch_bounds__(RS_THREADS, (P <= 2 ? 3 : 2)) k_resid_update(c
     yact[k] = it < RU_TY * HX;
     yoff[k] = yact[k] ? yy * HX + hx : 0;
 #pragma unroll
-    for (int m = 0; m < W; ++m) byc[k][m] = (yact[k] && y < Ny) ? a.band[1][(size_t)m * Ny + y] : 0.f;
+    for (int m = 0; m < W; ++m) byc[k][m] = (yact[k] && y < Ny) ? V::band(a.band[1][(size_t)m * Ny + y]) : V::zero();
   }
-  float mx[W];
+  VT mx[W];
 #pragma unroll
-  for (int m = 0; m < W; ++m) mx[m] = (xo < Nx) ? a.band[0][(size_t)m * Nx + xo] : 0.f;
+  for (int m = 0; m < W; ++m) mx[m] = (xo < Nx) ? V::band(a.band[0][(size_t)m * Nx + xo]) : V::zero();
 
   // this thread's halo entries: their source pointers in plane 0, advanced one
   // plane per fetch
@@ -356,12 +411,14 @@ __global__ void __launch_bounds__(RS_THREADS, (P <= 2 ? 3 : 2)) k_resid_update(c
     ru_commit();
   };
 
-  // acc[r][j]: partial sums of output plane zin - P + j of row r (value and |.| channel)
-  float acs[RU_RPT][W], act[RU_RPT][W];
+  // partial sums of output plane zin - P + j of row r: acs (M x1) and act
+  // (M |x1|, FP32)
+  VT acs[RU_RPT][W];
+  float act[RU_RPT][W];
 #pragma unroll
   for (int r = 0; r < RU_RPT; ++r)
 #pragma unroll
-    for (int j = 0; j < W; ++j) { acs[r][j] = 0.f; act[r][j] = 0.f; }
+    for (int j = 0; j < W; ++j) { acs[r][j] = V::zero(); act[r][j] = 0.f; }
   float rr = 0.f, aa = 0.f, r1q = 0.f;
 
 #pragma unroll 1
@@ -376,32 +433,34 @@ __global__ void __launch_bounds__(RS_THREADS, (P <= 2 ? 3 : 2)) k_resid_update(c
 #pragma unroll
       for (int k = 0; k < NYI; ++k) {
         if (yact[k]) {
-          float sv = 0.f, tv = 0.f;
+          VT sv = V::zero();
+          float tv = 0.f;
 #pragma unroll
           for (int m = 0; m < W; ++m) {
             const float v = up[yoff[k] + m * HX];
-            sv = fmaf(byc[k][m], v, sv);
-            tv = fmaf(byc[k][m], fabsf(v), tv);
+            sv = (m == 0) ? V::mulf(byc[k][0], v) : V::macf(sv, byc[k][m], v);
+            tv = fmaf(V::hi(byc[k][m]), fabsf(v), tv);
           }
           bys[tid + k * RS_THREADS] = sv;
           bya[tid + k * RS_THREADS] = tv;
         }
       }
       __syncthreads();
-      const float* c = cz + (zin - z0 + P) * W;
+      const VT* c = cz + (zin - z0 + P) * W;
 #pragma unroll
       for (int r = 0; r < RU_RPT; ++r) {
         const int row = ty + r * (RS_THREADS / RS_TX);
-        float sv = 0.f, tv = 0.f;
+        VT sv = V::mul(mx[0], bys[row * HX + tx]);
+        float tv = V::hi(mx[0]) * bya[row * HX + tx];
 #pragma unroll
-        for (int m = 0; m < W; ++m) {
-          sv = fmaf(mx[m], bys[row * HX + tx + m], sv);
-          tv = fmaf(mx[m], bya[row * HX + tx + m], tv);
+        for (int m = 1; m < W; ++m) {
+          sv = V::mac(sv, mx[m], bys[row * HX + tx + m]);
+          tv = fmaf(V::hi(mx[m]), bya[row * HX + tx + m], tv);
         }
 #pragma unroll
         for (int j = 0; j < W; ++j) {
-          acs[r][j] = fmaf(c[j], sv, acs[r][j]);
-          act[r][j] = fmaf(c[j], tv, act[r][j]);
+          acs[r][j] = V::mac(acs[r][j], c[j], sv);
+          act[r][j] = fmaf(V::hi(c[j]), tv, act[r][j]);
         }
       }
     }
@@ -413,7 +472,7 @@ __global__ void __launch_bounds__(RS_THREADS, (P <= 2 ? 3 : 2)) k_resid_update(c
           const int row = ty + r * (RS_THREADS / RS_TX);
           const float r1 = r1s_[zout & (R1R - 1)][r][tid];
           const float x1 = xin[zout & (RU_RING - 1)][(row + P) * HX + tx + P];
-          const float r2 = (r1 - acs[r][0]) * 16777216.f;  // 2^24: keeps the squares of a converged residual normal
+          const float r2 = V::sub_to_float(r1, acs[r][0]) * 16777216.f;  // 2^24: keeps the squares of a converged residual normal
           rr = fmaf(r2, r2, rr);
           aa = fmaf(act[r][0], act[r][0], aa);
           r1q = fmaf(r1, r1, r1q);
@@ -427,7 +486,7 @@ __global__ void __launch_bounds__(RS_THREADS, (P <= 2 ? 3 : 2)) k_resid_update(c
     for (int r = 0; r < RU_RPT; ++r) {
 #pragma unroll
       for (int j = 0; j < W - 1; ++j) { acs[r][j] = acs[r][j + 1]; act[r][j] = act[r][j + 1]; }
-      acs[r][W - 1] = 0.f;
+      acs[r][W - 1] = V::zero();
       act[r][W - 1] = 0.f;
     }
   }
@@ -464,11 +523,12 @@ cudaError_t launch_resid_update(int P, const UpdateArgs& a, int grid, cudaStream
   return cudaGetLastError();
 }
 
-// gK = g_K of the bound above; tiny (in the scaled units) covers underflow:
+// gdf, gK: g_df and g_K of the bound above; tiny (in the scaled units) covers underflow:
 // r1 entries below 2^-126 flushed to zero, subnormal FP32 results (2^-149 per
 // operation) and squares lost below the FP32 range in the norm sums (at most
 // sqrt(n) 2^-74.5 on a norm, 2^24 below it for ||r2||)
-__global__ void k_certify(const double* part, int n, double gK, double tiny, double tol, double* scal, int* flags) {
+__global__ void k_certify(const double* part, int n, double gdf, double gK, double tiny, double tol, double* scal,
+                          int* flags) {
   __shared__ double s0[256], s1[256], s2[256];
   if (flags[FL_CONV] != 0) return;
   double rr = 0.0, aa = 0.0, r1 = 0.0;
@@ -492,7 +552,7 @@ __global__ void k_certify(const double* part, int n, double gK, double tiny, dou
     // the per-thread FP32 sums of squares (at most 32 terms each) carry a
     // relative error below 33 u; 1e-4 covers it with room
     const double nr2 = sqrt(s0[0]), na = sqrt(s1[0]), nr1 = sqrt(s2[0]);
-    const double b = (1.0 + 1e-4) * ((1.0 + u / (1.0 - u)) * nr2 + u * nr1 + gK / (1.0 - gK) * na) + tiny;
+    const double b = (1.0 + 1e-4) * ((1.0 + 2.0 * u / (1.0 - 2.0 * u)) * nr2 + u * nr1 + gdf / (1.0 - gK) * na) + tiny;
     const double bound = b * scal[SC_OUT_SCALE];  // back to the units of F
     const double nf = sqrt(scal[SC_FF]);
     scal[SC_RELRES] = (nf > 0.0) ? bound / nf : (bound > 0.0 ? INFINITY : 0.0);
@@ -506,8 +566,10 @@ cudaError_t launch_certify(const double* part, int n, int P, long long ndof, dou
   const double u = 0x1p-24;
   const double K = 3.0 * (2 * P + 2);
   const double gK = K * u / (1.0 - K * u);
+  // the M x1 channel's error factor: double-float up to P = 3, FP32 at P = 4
+  const double gdf = (P <= 3) ? 64.0 * (2 * P + 1) * u * u : gK;
   const double tiny = sqrt((double)ndof) * 0x1p-90;
-  k_certify<<<1, 256, 0, s>>>(part, n, gK, tiny, tol, scal, flags);
+  k_certify<<<1, 256, 0, s>>>(part, n, gdf, gK, tiny, tol, scal, flags);
   return cudaGetLastError();
 }
 
