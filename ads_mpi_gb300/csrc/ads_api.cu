@@ -500,8 +500,23 @@ int enqueue_solve32(ads_handle* h, const void* in, int tin, const double* in_sca
   ax.skip_flag = skip;
   // x: skewed, without the transpose, into wC (L0)
   const bool corr = tag[0] != '\0';  // a refinement correction, not the first solve
-  { Phase ph(h, corr ? "Refinement" : "Solve 1");
-    RUN(h, nx.c_str(), 1, launch_sweep(h->P, tin, 1, 4, false, &h->tm_wC_out32, ax, sweep_grid(h, 0), h->stream)); }
+  if (tin == 1) {
+    // FP32 input: the column-form x sweep (lines y, positions x contiguous) into wC
+    CSweepArgs cx{};
+    cx.L = (int)Nx; cx.nl = (int)Ny; cx.n3 = (int)Nz;
+    cx.in = static_cast<const float*>(in);
+    cx.in_ls = g.PX; cx.in_ps = 1; cx.in_ts = g.PX * Ny;
+    cx.out = h->d_wC;
+    cx.out_ls = g.PX; cx.out_ps = 1; cx.out_ts = g.PX * Ny;
+    cx.fac = h->d_fac32[0];
+    cx.skip_flag = skip;
+    Phase ph(h, corr ? "Refinement" : "Solve 1");
+    RUN(h, nx.c_str(), 1, launch_xsweep(h->P, cx, h->stream));
+  } else {
+    // FP64 input (a caller's right-hand side), scaled on load: the skewed form
+    Phase ph(h, corr ? "Refinement" : "Solve 1");
+    RUN(h, nx.c_str(), 1, launch_sweep(h->P, tin, 1, 4, false, &h->tm_wC_out32, ax, sweep_grid(h, 0), h->stream));
+  }
   // y: column form in place on wC (lines x contiguous, positions y at stride PX, tiles over z)
   CSweepArgs cy{};
   cy.L = (int)Ny; cy.nl = (int)Nx; cy.n3 = (int)Nz;

@@ -139,6 +139,7 @@ struct CSweepArgs {
   long long in_ls, in_ps, in_ts;
   void* out;
   long long out_ps, out_ts;
+  long long out_ls;              // k_xsweep only: the output's line stride
   const float* fac;              // factor rows (2P+2) x L, as for k_sweep
   const double* out_scale_dev;
   const int* skip_flag;
@@ -429,5 +430,10 @@ __device__ __forceinline__ int pow2_exp(double s) {
   return (int)(((unsigned long long)__double_as_longlong(s) >> 52) & 0x7ffull) - 1023;
 }
 cudaError_t launch_csweep(int P, int mode, const CSweepArgs& a, cudaStream_t s);
+// The FP32 x sweep of the mixed step in column form (k_csweep.cu): lines l
+// (y) in tiles of 32, positions i (x) contiguous, in[l*in_ls + i + t*in_ts] ->
+// out[l*out_ls + i + t*out_ts] (FP32; out may be in); in_ls, out_ls, in_ts and
+// out_ts multiples of 4 entries with at least round_up(L, 4) entries per line
+cudaError_t launch_xsweep(int P, const CSweepArgs& a, cudaStream_t s);
 
 }  // namespace ads

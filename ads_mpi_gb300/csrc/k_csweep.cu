@@ -18,8 +18,8 @@
 //     global memory, coalesced, during the backward pass: FP32, or the FP64
 //     state 2^e x.
 // (The x sweep reads lines whose positions are contiguous; staging those
-// position-major takes 4-byte transposing copies, measured slower than
-// k_sweep's skewed form, so it stays there.)  A CTA holds as many warps
+// position-major would take 4-byte transposing copies, so k_xsweep below
+// stages them line-major instead.)  A CTA holds as many warps
 // (tiles) as shared memory allows next to one copy of the factor tables;
 // warps loop over tiles on their own.  No wait spins: cp.async groups
 // complete in hardware.
@@ -352,6 +352,251 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
     }
   }
   cs_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
+// The FP32 x sweep in column form (k_xsweep).  Along x the positions of a line
+// are contiguous, so a tile of 32 lines (32 consecutive y) is staged LINE-major
+// by 16-byte cp.async copies (coalesced: consecutive lanes copy consecutive
+// chunks of a line) into rows whose pitch is an odd number of 16-byte chunks.
+// Lane j then reads its own line four positions at a time: the eight lanes of
+// a quarter-warp read the same chunk index of eight rows, which the odd pitch
+// puts on eight different bank quads, so the 128-bit loads and stores are
+// conflict-free.  The lanes run across the lines as in k_csweep (all at the
+// same position, the LU factors of a position one broadcast load), forward and
+// backward in place in the staged rows, and the finished rows leave by 16-byte
+// stores, coalesced again.  Positions are processed in software-pipelined
+// blocks of 16; the input is staged in four position groups (separate commit
+// groups) so the forward pass starts when the first group has landed.  No wait
+// spins: cp.async groups complete in hardware.
+// ---------------------------------------------------------------------------
+constexpr int XS_MAX_WARPS = 8;
+constexpr int XS_GROUPS = 4;
+
+// staged row pitch in floats: round_up(L, 4) positions, as an odd number of
+// 16-byte chunks
+__host__ __device__ inline int xs_pitch(int L) {
+  int c = (L + 3) / 4;
+  if ((c & 1) == 0) ++c;
+  return 4 * c;
+}
+size_t xsweep_warp_bytes(int L) { return sizeof(float) * 32 * (size_t)xs_pitch(L); }
+
+template <int P>
+__global__ void __launch_bounds__(XS_MAX_WARPS * 32) k_xsweep(const CSweepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  if (a.skip_flag != nullptr && *a.skip_flag != 0) return;
+  using Tab = CsTab<P>;
+  constexpr int VF = Tab::VF, VB = Tab::VB;
+  const int L = a.L;
+  const int Lp = xs_pitch(L);
+  const int nch = (L + 3) / 4;  // 16-byte chunks of a line
+  const int j = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  float4* FT = reinterpret_cast<float4*>(smem);  // [L][VF]
+  float4* BT = FT + (size_t)VF * L;              // [L][VB]
+  float* S = reinterpret_cast<float*>(smem + Tab::bytes(L)) + (size_t)warp * 32 * Lp;
+
+  // factor rows (global [row][L]): row 0 fs (1 here), 1..P f, P+1 bs, P+2.. g
+  for (int i = threadIdx.x; i < L; i += blockDim.x) {
+    float fw[4 * VF], bw[4 * VB];
+#pragma unroll
+    for (int m = 0; m < 4 * VF; ++m) fw[m] = (m < P) ? a.fac[(size_t)(1 + m) * L + i] : 0.f;
+#pragma unroll
+    for (int m = 0; m < 4 * VB; ++m) bw[m] = (m <= P) ? a.fac[(size_t)(P + 1 + m) * L + i] : 0.f;
+#pragma unroll
+    for (int v = 0; v < VF; ++v) FT[(size_t)i * VF + v] = make_float4(fw[4 * v], fw[4 * v + 1], fw[4 * v + 2], fw[4 * v + 3]);
+#pragma unroll
+    for (int v = 0; v < VB; ++v) BT[(size_t)i * VB + v] = make_float4(bw[4 * v], bw[4 * v + 1], bw[4 * v + 2], bw[4 * v + 3]);
+  }
+  __syncthreads();
+
+  float* out = static_cast<float*>(a.out);
+  const int tiles_l = (a.nl + 31) / 32;
+  const int ntiles = tiles_l * a.n3;
+  const int GP = ((L + XS_GROUPS - 1) / XS_GROUPS + CS_BLK - 1) / CS_BLK * CS_BLK;  // positions per group
+
+  for (int tile = blockIdx.x * nwarps + warp; tile < ntiles; tile += gridDim.x * nwarps) {
+    const int tl = tile % tiles_l, t3 = tile / tiles_l;
+    const int l0 = tl * 32;
+    const int nlv = min(32, a.nl - l0);
+    const float* src = a.in + (size_t)t3 * a.in_ts + (size_t)l0 * a.in_ls;
+
+    __syncwarp();  // the previous tile is done with S
+    // ---- stage: group g holds chunks [g*GP/4, (g+1)*GP/4) of every line ----
+#pragma unroll 1
+    for (int g = 0; g < XS_GROUPS; ++g) {
+      const int c0 = g * (GP / 4), c1 = min(nch, (g + 1) * (GP / 4));
+      const int ncg = c1 - c0;
+      for (int idx = j; idx < nlv * ncg; idx += 32) {
+        const int l = idx / ncg, c = c0 + idx % ncg;
+        cs_cp16(S + (size_t)l * Lp + 4 * c, src + (size_t)l * a.in_ls + 4 * c);
+      }
+      cs_commit();
+    }
+
+    float* Sj = S + (size_t)j * Lp;
+    // ---- forward: y_i = b_i - sum_m f[m]_i y_{i-m}, in place ----
+    float prev[P];
+#pragma unroll
+    for (int m = 0; m < P; ++m) prev[m] = 0.f;
+    {
+      int i = 0;
+#pragma unroll 1
+      for (int g = 0; g < XS_GROUPS; ++g) {
+        switch (g) {
+          case 0: cs_wait<XS_GROUPS - 1>(); break;
+          case 1: cs_wait<XS_GROUPS - 2>(); break;
+          case 2: cs_wait<XS_GROUPS - 3>(); break;
+          default: cs_wait<0>(); break;
+        }
+        __syncwarp();
+        const int ie = min(L, (g + 1) * GP);
+#pragma unroll 1
+        for (; i + CS_BLK <= ie; i += CS_BLK) {
+          float4* yp = reinterpret_cast<float4*>(Sj + i);
+          const float4* fp = FT + (size_t)i * VF;
+          float bv[CS_BLK];
+          float4 fv[CS_BLK][VF];
+#pragma unroll
+          for (int q = 0; q < CS_BLK / 4; ++q) {
+            const float4 v4 = yp[q];
+            bv[4 * q] = v4.x; bv[4 * q + 1] = v4.y; bv[4 * q + 2] = v4.z; bv[4 * q + 3] = v4.w;
+          }
+#pragma unroll
+          for (int t = 0; t < CS_BLK; ++t)
+#pragma unroll
+            for (int v = 0; v < VF; ++v) fv[t][v] = fp[t * VF + v];
+#pragma unroll
+          for (int t = 0; t < CS_BLK; ++t) {
+            const float* f = reinterpret_cast<const float*>(fv[t]);
+            float y = bv[t];
+#pragma unroll
+            for (int m = P; m >= 1; --m) y -= f[m - 1] * prev[m - 1];
+#pragma unroll
+            for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
+            prev[0] = y;
+            bv[t] = y;
+          }
+#pragma unroll
+          for (int q = 0; q < CS_BLK / 4; ++q) yp[q] = make_float4(bv[4 * q], bv[4 * q + 1], bv[4 * q + 2], bv[4 * q + 3]);
+        }
+#pragma unroll 1
+        for (; i < ie; ++i) {
+          float4 fv[VF];
+#pragma unroll
+          for (int v = 0; v < VF; ++v) fv[v] = FT[(size_t)i * VF + v];
+          const float* f = reinterpret_cast<const float*>(fv);
+          float y = Sj[i];
+#pragma unroll
+          for (int m = P; m >= 1; --m) y -= f[m - 1] * prev[m - 1];
+#pragma unroll
+          for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
+          prev[0] = y;
+          Sj[i] = y;
+        }
+      }
+    }
+
+    // ---- backward: x_i = bs_i y_i - sum_m g[m]_i x_{i+m}, in place ----
+    {
+      float nxt[P];
+#pragma unroll
+      for (int m = 0; m < P; ++m) nxt[m] = 0.f;
+      int i = L;
+      const int rem = L % CS_BLK;
+#pragma unroll 1
+      for (int r = 0; r < rem; ++r) {
+        --i;
+        float4 bw[VB];
+#pragma unroll
+        for (int v = 0; v < VB; ++v) bw[v] = BT[(size_t)i * VB + v];
+        const float* c = reinterpret_cast<const float*>(bw);
+        float x = c[0] * Sj[i];
+#pragma unroll
+        for (int m = P; m >= 1; --m) x -= c[m] * nxt[m - 1];
+#pragma unroll
+        for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
+        nxt[0] = x;
+        Sj[i] = x;
+      }
+#pragma unroll 1
+      for (; i >= CS_BLK; i -= CS_BLK) {
+        const int ib = i - CS_BLK;  // block [ib, i), processed downwards
+        float4* yp = reinterpret_cast<float4*>(Sj + ib);
+        const float4* bp = BT + (size_t)ib * VB;
+        float yv[CS_BLK];
+        float4 bw[CS_BLK][VB];
+#pragma unroll
+        for (int q = 0; q < CS_BLK / 4; ++q) {
+          const float4 v4 = yp[q];
+          yv[4 * q] = v4.x; yv[4 * q + 1] = v4.y; yv[4 * q + 2] = v4.z; yv[4 * q + 3] = v4.w;
+        }
+#pragma unroll
+        for (int t = 0; t < CS_BLK; ++t)
+#pragma unroll
+          for (int v = 0; v < VB; ++v) bw[t][v] = bp[t * VB + v];
+#pragma unroll
+        for (int t = CS_BLK - 1; t >= 0; --t) {
+          const float* c = reinterpret_cast<const float*>(bw[t]);
+          float x = c[0] * yv[t];
+#pragma unroll
+          for (int m = P; m >= 1; --m) x -= c[m] * nxt[m - 1];
+#pragma unroll
+          for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
+          nxt[0] = x;
+          yv[t] = x;
+        }
+#pragma unroll
+        for (int q = 0; q < CS_BLK / 4; ++q) yp[q] = make_float4(yv[4 * q], yv[4 * q + 1], yv[4 * q + 2], yv[4 * q + 3]);
+      }
+    }
+
+    // ---- the solved rows out, 16-byte coalesced stores ----
+    __syncwarp();
+    float* dst = out + (size_t)t3 * a.out_ts + (size_t)l0 * a.out_ls;
+    for (int idx = j; idx < nlv * nch; idx += 32) {
+      const int l = idx / nch, c = idx % nch;
+      *reinterpret_cast<float4*>(dst + (size_t)l * a.out_ls + 4 * c) =
+          *reinterpret_cast<const float4*>(S + (size_t)l * Lp + 4 * c);
+    }
+  }
+  cs_wait<0>();
+}
+
+template <int P>
+static cudaError_t launch_xs(const CSweepArgs& a, cudaStream_t s) {
+  auto kern = k_xsweep<P>;
+  int dev = 0, nsm = 0, smem_max = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t tab = CsTab<P>::bytes(a.L), per = xsweep_warp_bytes(a.L);
+  if (tab + per > (size_t)smem_max) return cudaErrorInvalidValue;
+  const int nw = (int)std::min<size_t>(XS_MAX_WARPS, ((size_t)smem_max - tab) / per);
+  const size_t bytes = tab + per * nw;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return e;
+  const int tiles = (a.nl + 31) / 32 * a.n3;
+  const int grid = std::max(1, std::min(nsm, (tiles + nw - 1) / nw));
+  kern<<<grid, 32 * nw, bytes, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_xsweep(int P, const CSweepArgs& a, cudaStream_t s) {
+  if (a.in == nullptr || a.out == nullptr || a.fac == nullptr) return cudaErrorInvalidValue;
+  // positions contiguous; lines and planes 16-byte aligned with room for
+  // round_up(L, 4) entries per line
+  const long long Lr = (a.L + 3) / 4 * 4;
+  if (a.in_ps != 1 || a.in_ls % 4 != 0 || a.in_ts % 4 != 0 || a.out_ls % 4 != 0 || a.out_ts % 4 != 0 ||
+      a.in_ls < Lr || a.out_ls < Lr)
+    return cudaErrorInvalidValue;
+  switch (P) {
+    case 1: return launch_xs<1>(a, s);
+    case 2: return launch_xs<2>(a, s);
+    case 3: return launch_xs<3>(a, s);
+    case 4: return launch_xs<4>(a, s);
+  }
+  return cudaErrorInvalidValue;
 }
 
 template <int P, int MODE>
