@@ -43,7 +43,7 @@ class Opts(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [("l2norm", ctypes.c_double), ("rel_residual", ctypes.c_double),
-                ("refinements", ctypes.c_int), ("converged", ctypes.c_int)]
+                ("refinements", ctypes.c_int), ("converged", ctypes.c_int), ("fp64_residuals", ctypes.c_int)]
 
 
 # (name, argtypes, restype) of every entry point declared in include/ads_gpu.h
@@ -330,7 +330,7 @@ class ADS:
         s = Stats()
         self._check(self._L.ads_get_stats(self.h, ctypes.byref(s)))
         return dict(l2norm=s.l2norm, rel_residual=s.rel_residual, refinements=s.refinements,
-                    converged=bool(s.converged))
+                    converged=bool(s.converged), fp64_residuals=s.fp64_residuals)
 
     def assemble(self):
         F = np.zeros(self.N)

@@ -121,7 +121,8 @@ struct ads_handle {
 
   // launch geometry
   int asm_grid = 0, asm_zc = 0, asm_nix = 0, asm_niy = 0, asm_niz = 0;
-  int res_grid = 0, res_zc = 0, res_nix = 0, res_niy = 0, res_niz = 0;
+  int res_grid = 0, res_zc = 0, res_nix = 0, res_niy = 0, res_niz = 0;  // 32-plane chunks
+  int rsd_grid = 0, rsd_zc = 0, rsd_niz = 0;  // k_residual's own z chunking (whole waves)
   int upd_grid = 0, upd_niy = 0;  // k_resid_update: the x and z tiling of res_*, its own rows
   int norm_parts = 0;
 
@@ -376,8 +377,8 @@ FixupArgs fixup_args(const ads_handle* h, double* F) {
 ResidualArgs residual_args(const ads_handle* h, const double* u, const double* F, double* r) {
   ResidualArgs a{};
   a.g = h->g;
-  a.zc = h->res_zc;
-  a.nix = h->res_nix; a.niy = h->res_niy; a.niz = h->res_niz;
+  a.zc = h->rsd_zc;
+  a.nix = h->res_nix; a.niy = h->res_niy; a.niz = h->rsd_niz;
   a.u = u; a.F = F; a.r = r;
   for (int d = 0; d < 3; ++d) a.band[d] = h->d_band[d];
   a.part = h->d_part;
@@ -392,7 +393,7 @@ int enqueue_mass(ads_handle* h, const double* u, const double* F, double* r, con
     return ADS_OK;
   }
   ResidualArgs ra = residual_args(h, u, F, r);
-  RUN(h, name, 1, launch_residual(h->P, ra, h->res_grid, h->stream));
+  RUN(h, name, 1, launch_residual(h->P, ra, h->rsd_grid, h->stream));
   return ADS_OK;
 }
 
@@ -564,7 +565,7 @@ int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready, bool f32_in
     ra.want_ff = want_ff;
     ra.r32 = h->d_g32;
     ra.r32_scale = in_s;
-    RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->res_grid, h->stream));
+    RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->rsd_grid, h->stream));
     return ADS_OK;
   };
   UpdateArgs ua{};
@@ -581,14 +582,14 @@ int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready, bool f32_in
   const long long ndof = (long long)h->g.N[0] * h->g.N[1] * h->g.N[2];
   for (int k = 0; k < h->opts.max_refine; ++k) {
     if ((st = residual(k == 0))) return st;
-    RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, true, k == 0, h->d_scal, h->d_flags, h->stream));
+    RUN(h, "decide", 1, launch_decide(h->d_part, h->rsd_grid, h->opts.refine_tol, true, k == 0, h->d_scal, h->d_flags, h->stream));
     if ((st = enqueue_solve32(h, h->d_g32, 1, nullptr, nullptr, 0, conv, "_corr", nullptr))) return st;
     RUN(h, "resid_update", 1, launch_resid_update(h->P, ua, h->upd_grid, h->stream));
     RUN(h, "certify", 1, launch_certify(h->d_part, h->upd_grid, h->P, ndof, h->opts.refine_tol, h->d_scal,
                                         h->d_flags, h->stream));
   }
   if ((st = residual(h->opts.max_refine == 0))) return st;
-  RUN(h, "decide", 1, launch_decide(h->d_part, h->res_grid, h->opts.refine_tol, false, h->opts.max_refine == 0,
+  RUN(h, "decide", 1, launch_decide(h->d_part, h->rsd_grid, h->opts.refine_tol, false, h->opts.max_refine == 0,
                                     h->d_scal, h->d_flags, h->stream));
   return ADS_OK;
 }
@@ -636,7 +637,7 @@ int ensure_hist(ads_handle* h, int cap) {
   if (cap <= h->hist_cap) return ADS_OK;
   if (h->d_hist) cudaFree(h->d_hist);
   h->d_hist = nullptr;
-  ADS_CUDA(h, cudaMalloc(&h->d_hist, sizeof(double) * 4 * (size_t)cap));
+  ADS_CUDA(h, cudaMalloc(&h->d_hist, sizeof(double) * HIST_W * (size_t)cap));
   h->hist_cap = cap;
   h->graph_valid = false;
   return ADS_OK;
@@ -669,23 +670,24 @@ int build_graph(ads_handle* h) {
 int finish_stats(ads_handle* h, int k, double* l2norms) {
   int st = check_flags(h);
   if (st) return st;
-  std::vector<double> hist((size_t)4 * k);
-  ADS_CUDA(h, cudaMemcpy(hist.data(), h->d_hist, sizeof(double) * 4 * (size_t)k, cudaMemcpyDeviceToHost));
+  std::vector<double> hist((size_t)HIST_W * k);
+  ADS_CUDA(h, cudaMemcpy(hist.data(), h->d_hist, sizeof(double) * HIST_W * (size_t)k, cudaMemcpyDeviceToHost));
   for (int i = 0; i < k; ++i)
-    if (l2norms) l2norms[i] = hist[4 * i];
-  const double* last = &hist[4 * (size_t)(k - 1)];
+    if (l2norms) l2norms[i] = hist[HIST_W * i];
+  const double* last = &hist[HIST_W * (size_t)(k - 1)];
   h->last.l2norm = last[0];
   const bool mixed = is_mixed(h);
   h->last.rel_residual = mixed ? last[1] : 0.0;
   h->last.refinements = mixed ? (int)last[2] : 0;
   h->last.converged = mixed ? (int)last[3] : 1;
+  h->last.fp64_residuals = mixed ? (int)last[4] : 0;
   for (int i = 0; i < k; ++i)
-    if (!std::isfinite(hist[4 * i])) return fail(h, ADS_ERR_NONFINITE, "non-finite l2norm");
+    if (!std::isfinite(hist[HIST_W * i])) return fail(h, ADS_ERR_NONFINITE, "non-finite l2norm");
   if (mixed) {
     for (int i = 0; i < k; ++i)
-      if (hist[4 * i + 3] == 0.0)
+      if (hist[HIST_W * i + 3] == 0.0)
         return fail(h, ADS_ERR_NOCONV, "iterative refinement did not reach refine_tol (relative residual " +
-                                          std::to_string(hist[4 * i + 1]) + ")");
+                                          std::to_string(hist[HIST_W * i + 1]) + ")");
   }
   return ADS_OK;
 }
@@ -865,6 +867,19 @@ int create_impl(ads_handle* h) {
     h->res_grid = h->res_nix * h->res_niy * h->res_niz;
     h->upd_niy = (g.N[1] + resid_update_rows() - 1) / resid_update_rows();
     h->upd_grid = h->res_nix * h->upd_niy * h->res_niz;
+    // k_residual streams its chunk plus a p-plane halo on each side: pick the
+    // chunk that fills whole waves of resident CTAs with the least halo work,
+    // min over zc of ceil(CTAs / resident) * (zc + 2p)
+    const int resident = nsm * std::max(1, residual_ctas_per_sm(h->P));
+    long long best = -1;
+    for (int zc = std::min(g.N[2], std::max(8, 2 * h->P)); zc <= std::min(g.N[2], 128); ++zc) {
+      const int niz = (g.N[2] + zc - 1) / zc;
+      const long long ctas = (long long)h->res_nix * h->res_niy * niz;
+      const long long cost = (ctas + resident - 1) / resident * (long long)(zc + 2 * h->P);
+      if (best < 0 || cost < best) { best = cost; h->rsd_zc = zc; }
+    }
+    h->rsd_niz = (g.N[2] + h->rsd_zc - 1) / h->rsd_zc;
+    h->rsd_grid = h->res_nix * h->res_niy * h->rsd_niz;
   }
   if (!h->general) {
     // spill-slab membership of each DOF index (the assembly's bricks spill the
@@ -884,7 +899,7 @@ int create_impl(ads_handle* h) {
     if (!xs.empty()) ADS_CUDA(h, cudaMemcpy(h->d_xslab, xs.data(), sizeof(int) * xs.size(), cudaMemcpyHostToDevice));
   }
   h->norm_parts = 4 * nsm;
-  h->npart = std::max(3 * std::max(h->res_grid, h->upd_grid), 2 * h->norm_parts);
+  h->npart = std::max(3 * std::max(std::max(h->res_grid, h->rsd_grid), h->upd_grid), 2 * h->norm_parts);
   if ((st = zalloc(&h->d_l2part, 3 * (size_t)h->asm_grid))) return st;
   if ((st = zalloc(&h->d_part, (size_t)h->npart))) return st;
   if ((st = zalloc(&h->d_scal, SC_COUNT))) return st;
@@ -1257,6 +1272,7 @@ int ads_multistep(ads_handle* h, const double mix[12], double* l2norm) {
   h->last.rel_residual = 0.0;
   h->last.refinements = 0;
   h->last.converged = 1;
+  h->last.fp64_residuals = 0;
   if (l2norm) *l2norm = l2;
   return ADS_OK;
 }
@@ -1365,6 +1381,7 @@ int ads_solve(ads_handle* h, const double* F, double* u_out) {
   h->last.rel_residual = mixed ? sc[SC_RELRES] : 0.0;
   h->last.refinements = mixed ? fl[FL_ITERS] : 0;
   h->last.converged = mixed ? fl[FL_CONV] : 1;
+  h->last.fp64_residuals = mixed ? fl[FL_RESID] : 0;
   if (mixed && !fl[FL_CONV]) return fail(h, ADS_ERR_NOCONV, "iterative refinement did not reach refine_tol");
   return ADS_OK;
 }
@@ -1712,9 +1729,11 @@ void handle_noalloc_view(ads_handle* h, NoallocView* v) {
   v->dev = h->dev;
   v->P = h->P;
   v->general = h->general;
-  v->grid = h->res_grid;
+  v->grid = h->res_grid;  // the 32-plane chunks: the scratch limit is stated in them
   v->stream = h->stream;
   v->args = residual_args(h, nullptr, nullptr, nullptr);
+  v->args.zc = h->res_zc;
+  v->args.niz = h->res_niz;
   v->args.g.PX = h->g.N[0];
   v->args.part = nullptr;
   v->args.err = nullptr;

@@ -219,15 +219,20 @@ enum ScalarSlot {
   SC_DRAINED_TOTAL, // oil form: drained summed over the steps since ads_set_oil
   SC_COUNT = 16
 };
+// doubles per step in the history the step kernels record
+constexpr int HIST_W = 5;
 enum FlagSlot {
   FL_ERR = 0,       // error bits (ERRF_*)
   FL_CONV,          // refinement converged
   FL_ITERS,         // corrections applied in the current solve
   FL_HIST,          // number of recorded steps
+  FL_RESID,         // FP64 residuals that ran in the current solve
   FL_COUNT = 8
 };
 
 cudaError_t launch_residual(int P, const ResidualArgs& a, int grid, cudaStream_t s);
+// resident k_residual CTAs per SM (1 if the query fails)
+int residual_ctas_per_sm(int P);
 // reduce residual partials; sets SC_RR, SC_RELRES, FL_CONV and
 // (if count_iter and not converged) FL_ITERS += 1.  Skipped when FL_CONV is set.
 // use_ff: take ||F||^2 from the partials (and store it) instead of SC_FF

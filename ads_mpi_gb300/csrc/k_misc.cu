@@ -156,6 +156,18 @@ __global__ void __launch_bounds__(RS_THREADS) k_residual(const ResidualArgs a) {
   }
 }
 
+int residual_ctas_per_sm(int P) {
+  int n = 0;
+  cudaError_t e = cudaErrorInvalidValue;
+  switch (P) {
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_residual<1>, RS_THREADS, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_residual<2>, RS_THREADS, 0); break;
+    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_residual<3>, RS_THREADS, 0); break;
+    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_residual<4>, RS_THREADS, 0); break;
+  }
+  return e == cudaSuccess ? n : 1;
+}
+
 cudaError_t launch_residual(int P, const ResidualArgs& a, int grid, cudaStream_t s) {
   switch (P) {
     case 1: k_residual<1><<<grid, RS_THREADS, 0, s>>>(a); break;
@@ -201,6 +213,7 @@ __global__ void k_decide(const double* part, int n, double tol, int count_iter, 
     const double rel = (ff > 0.0) ? sqrt(rr / ff) : (rr > 0.0 ? INFINITY : 0.0);
     scal[SC_RELRES] = rel;
     const bool conv = (rr <= tol * tol * ff);
+    flags[FL_RESID] += 1;  // an FP64 residual that did work
     if (conv) flags[FL_CONV] = 1;
     else if (count_iter) flags[FL_ITERS] += 1;
   }
@@ -667,6 +680,7 @@ __global__ void k_step_reset(double* scal, int* flags) {
   if (threadIdx.x == 0) {
     flags[FL_CONV] = 0;
     flags[FL_ITERS] = 0;
+    flags[FL_RESID] = 0;
     scal[SC_RELRES] = 0.0;
     scal[SC_RR] = 0.0;
   }
@@ -676,15 +690,17 @@ cudaError_t launch_step_reset(double* scal, int* flags, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// hist rows of 4 doubles: l2norm, relative residual, corrections, converged
+// hist rows of HIST_W doubles: l2norm, relative residual, corrections,
+// converged, FP64 residuals
 __global__ void k_record(double* scal, int* flags, double* hist, int cap) {
   if (threadIdx.x != 0) return;
   const int c = flags[FL_HIST];
   if (c < cap) {
-    hist[4 * c + 0] = scal[SC_L2];
-    hist[4 * c + 1] = scal[SC_RELRES];
-    hist[4 * c + 2] = (double)flags[FL_ITERS];
-    hist[4 * c + 3] = (double)flags[FL_CONV];
+    hist[HIST_W * c + 0] = scal[SC_L2];
+    hist[HIST_W * c + 1] = scal[SC_RELRES];
+    hist[HIST_W * c + 2] = (double)flags[FL_ITERS];
+    hist[HIST_W * c + 3] = (double)flags[FL_CONV];
+    hist[HIST_W * c + 4] = (double)flags[FL_RESID];
   }
   flags[FL_HIST] = c + 1;
   scal[SC_DRAINED_TOTAL] += scal[SC_DRAINED];  // oil form; 0 for the others

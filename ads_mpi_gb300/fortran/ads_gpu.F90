@@ -32,6 +32,7 @@ module ads_gpu
       real(c_double) :: rel_residual
       integer(c_int) :: refinements
       integer(c_int) :: converged
+      integer(c_int) :: fp64_residuals
    end type ads_stats
 
    type :: ads_gpu_handle

@@ -104,6 +104,9 @@ typedef struct ads_stats {
                            residual where that decided); 0 for FP64 */
   int refinements;      /* corrections applied in the last solve (mixed) */
   int converged;        /* 1 if the refinement reached refine_tol (mixed), 1 for FP64 */
+  int fp64_residuals;   /* FP64 residuals that ran in the last solve (mixed): one per
+                           correction, plus one more where the certified bound stayed
+                           above refine_tol and an FP64 residual decided; 0 for FP64 */
 } ads_stats;
 
 int ads_default_opts(ads_opts* opts);

@@ -148,19 +148,24 @@ def test_mixed_certified_bound_covers_true_residual(ads_mod, E, p, tol):
         assert true <= st["rel_residual"] + fp64_floor(ads_mod, E, p, F, u)
         if p == 2:
             assert st["refinements"] == 1
+            assert st["fp64_residuals"] == 1  # the bound decided, not a second FP64 residual
             assert st["rel_residual"] >= true + 1e-15
+        assert st["fp64_residuals"] in (st["refinements"], st["refinements"] + 1)
 
 
-def test_mixed_bound_above_tolerance_falls_back_to_fp64_residual(ads_mod):
-    """With refine_tol below what the certified bound can show after one
-    correction (it carries u ||r1||, ~2e-14 here), the next round's FP64
-    residual decides; the step still converges."""
+def test_mixed_tolerance_below_one_correction_takes_another_round(ads_mod):
+    """With refine_tol below what one correction reaches (~1.6e-14 here, and
+    its bound carries u ||r1||, ~2e-14 more), the next round's FP64 residual
+    finds the solve unconverged and a second correction follows, whose bound
+    certifies; the result meets the tolerance."""
     E, p, tol = (30, 33, 40), 2, 1e-14
     g, _ = make(ads_mod, E, p, prec=1, refine_tol=tol)
     F = np.random.default_rng(41).standard_normal(g.N)
     u = g.solve(F)
     st = g.stats()
     assert st["converged"] and st["rel_residual"] <= tol
+    assert st["refinements"] == 2
+    assert st["fp64_residuals"] in (st["refinements"], st["refinements"] + 1)
     assert true_rel_residual(ads_mod, E, p, F, u) <= 2 * tol
 
 
