@@ -43,7 +43,8 @@ class Opts(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [("l2norm", ctypes.c_double), ("rel_residual", ctypes.c_double),
-                ("refinements", ctypes.c_int), ("converged", ctypes.c_int), ("fp64_residuals", ctypes.c_int)]
+                ("refinements", ctypes.c_int), ("converged", ctypes.c_int), ("fp64_residuals", ctypes.c_int),
+                ("host_path", ctypes.c_int)]
 
 
 # (name, argtypes, restype) of every entry point declared in include/ads_gpu.h
@@ -64,6 +65,7 @@ ABI = [
     ("ads_set_coeffs", [ctypes.c_void_p, _dp], ctypes.c_int),
     ("ads_get_coeffs", [ctypes.c_void_p, _dp], ctypes.c_int),
     ("ads_step", [ctypes.c_void_p, _dp], ctypes.c_int),
+    ("ads_step_host", [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _dp], ctypes.c_int),
     ("ads_steps", [ctypes.c_void_p, ctypes.c_int, _dp], ctypes.c_int),
     ("ads_multistep", [ctypes.c_void_p, _dp, _dp], ctypes.c_int),
     ("ads_get_stats", [ctypes.c_void_p, ctypes.POINTER(Stats)], ctypes.c_int),
@@ -312,6 +314,23 @@ class ADS:
         self._check(self._L.ads_step(self.h, ctypes.byref(l2)))
         return l2.value
 
+    def step_host(self, u, out=None):
+        """One Step from the float64 array u into out (u itself when out is
+        None, the reference's in-place Step); returns l2norm.  Pinned (or, where
+        the device reads pageable memory, any) host arrays are read and written
+        in place by the step's kernels."""
+        out = u if out is None else out
+        for a in (u, out):
+            if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] \
+                    or a.size != self.N:
+                raise ValueError("u and out must be contiguous float64 arrays of ndof entries")
+        if not out.flags["WRITEABLE"]:
+            raise ValueError("out must be writeable")
+        l2 = ctypes.c_double(0.0)
+        self._check(self._L.ads_step_host(self.h, ctypes.c_void_p(u.ctypes.data), ctypes.c_void_p(out.ctypes.data),
+                                          ctypes.byref(l2)))
+        return l2.value
+
     def steps(self, k):
         out = np.zeros(max(k, 1))
         self._check(self._L.ads_steps(self.h, k, _ptr(out)))
@@ -330,7 +349,7 @@ class ADS:
         s = Stats()
         self._check(self._L.ads_get_stats(self.h, ctypes.byref(s)))
         return dict(l2norm=s.l2norm, rel_residual=s.rel_residual, refinements=s.refinements,
-                    converged=bool(s.converged), fp64_residuals=s.fp64_residuals)
+                    converged=bool(s.converged), fp64_residuals=s.fp64_residuals, host_path=s.host_path)
 
     def assemble(self):
         F = np.zeros(self.N)

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -54,6 +55,8 @@ struct ads_handle {
   int P = 0, Q = 0;
   ads_opts opts{};
   int dev = 0;
+  bool pageable = false;  // the device reads pageable host memory (cudaDevAttrPageableMemoryAccess)
+  bool uscale_set = false;  // SC_USCALE holds the scale of some coefficients (a uscale pass ran)
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   std::string err;
@@ -345,6 +348,7 @@ AssembleArgs assemble_args(const ads_handle* h, const double* u, double* F, bool
   a.dt = h->dt;
   a.kappa = h->kappa;
   a.u = u;
+  a.u_px = h->g.PX;
   a.F = F;
   a.shadow = h->d_shadow;
   a.shadow_stride = (long long)h->n0;
@@ -419,6 +423,13 @@ int enqueue_assemble_gen(ads_handle* h, const double* u, double* F, bool incr, b
   return ADS_OK;
 }
 
+DfTabs3 df_tabs(const ads_handle* h) {
+  DfTabs3 tb;
+  DfTab* t[3] = {&tb.x, &tb.y, &tb.z};
+  for (int d = 0; d < 3; ++d) { t[d]->nn = h->d_nndf[d]; t[d]->jw = h->d_jwdf[d]; }
+  return tb;
+}
+
 int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool incr, bool with_f,
                      const double* kqp_override = nullptr) {
   Phase ph(h, "Form 3D RHS");
@@ -432,15 +443,14 @@ int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool 
     t32[d].nn = h->d_nn32[d]; t32[d].jw = h->d_jw32[d]; t32[d].dd = h->d_dd32[d];
   }
   // the FP32 heat assembly works on coefficients scaled by a power of two
-  if (fp32 && (h->form == ADS_FORM_HEAT || h->form == ADS_FORM_OIL))
+  if (fp32 && (h->form == ADS_FORM_HEAT || h->form == ADS_FORM_OIL)) {
     RUN(h, "uscale", 2, launch_uscale(u, (long long)h->n0, h->d_part, h->norm_parts, h->d_scal, h->stream));
+    h->uscale_set = true;
+  }
   a.uscale = h->d_scal + SC_USCALE;
   int used = h->asm_grid;
   if (fp32 && incr && df_increment(h)) {
-    DfTabs3 tb;
-    DfTab* t[3] = {&tb.x, &tb.y, &tb.z};
-    for (int d = 0; d < 3; ++d) { t[d]->nn = h->d_nndf[d]; t[d]->jw = h->d_jwdf[d]; }
-    RUN(h, "assemble_df", 1, launch_assemble_df(a, tb, h->asm_grid, &used, h->stream));
+    RUN(h, "assemble_df", 1, launch_assemble_df(a, df_tabs(h), h->asm_grid, &used, h->stream));
   } else {
     const void* tx = fp32 ? (const void*)&t32[0] : (const void*)&t64[0];
     const void* ty = fp32 ? (const void*)&t32[1] : (const void*)&t64[1];
@@ -451,6 +461,33 @@ int enqueue_assemble(ads_handle* h, const double* u, double* F, bool fp32, bool 
   FixupArgs f = fixup_args(h, F);
   f.nl2 = used;
   if (fp32 && incr) f.g32 = h->d_g32;  // the heat increment also feeds the FP32 solve as float
+  RUN(h, "fixup", 2, launch_fixup(f, h->stream));
+  return ADS_OK;
+}
+
+// The double-float increment assembly of a step on a caller's array u
+// (unpadded rows of N[0], read in place), on the coefficient scale the last
+// assembly left in SC_USCALE instead of a pass over u: the fixup checks it
+// against the max |u| the assembly saw, sets FL_UMISS when it was off and
+// leaves the exact scale of u for the next step.
+int enqueue_assemble_host(ads_handle* h, const double* u) {
+  Phase ph(h, "Form 3D RHS");
+  if (!h->uscale_set) {
+    // no scale to start from yet: a pass over u (through the host link)
+    const long long n = (long long)h->g.N[0] * h->g.N[1] * h->g.N[2];
+    RUN(h, "uscale", 2, launch_uscale(u, n, h->d_part, h->norm_parts, h->d_scal, h->stream));
+    h->uscale_set = true;
+  }
+  AssembleArgs a = assemble_args(h, u, h->d_F, true);
+  a.u_px = h->g.N[0];
+  a.u_copy = h->d_u;  // u becomes the handle's coefficients on the way (HBM writes)
+  a.uscale = h->d_scal + SC_USCALE;
+  int used = h->asm_grid;
+  RUN(h, "assemble_df", 1, launch_assemble_df(a, df_tabs(h), h->asm_grid, &used, h->stream));
+  FixupArgs f = fixup_args(h, h->d_F);
+  f.nl2 = used;
+  f.g32 = h->d_g32;
+  f.umiss = h->d_flags + FL_UMISS;
   RUN(h, "fixup", 2, launch_fixup(f, h->stream));
   return ADS_OK;
 }
@@ -625,6 +662,23 @@ int enqueue_step(ads_handle* h) {
   return ADS_OK;
 }
 
+// The mixed heat step on a caller's arrays (device-addressable, unpadded):
+// the assembly reads u_in in place and copies it into d_u, the update writes
+// d_u + delta into d_u and u_out, unless the scale check failed (then the
+// update writes nothing).
+int enqueue_step_host(ads_handle* h, const double* u_in, double* u_out) {
+  RUN(h, "step_reset", 1, launch_step_reset(h->d_scal, h->d_flags, h->stream));
+  int st;
+  if ((st = enqueue_assemble_host(h, u_in))) return st;
+  if ((st = enqueue_solve_mixed(h, h->d_delta, true, true))) return st;
+  {
+    Phase ph(h, "Update");
+    RUN(h, "update_host", 1, launch_update_host(h->d_delta, h->d_u, u_out, h->g, h->d_flags + FL_UMISS, h->stream));
+  }
+  RUN(h, "record", 1, launch_record(h->d_scal, h->d_flags, h->d_hist, h->hist_cap, h->stream));
+  return ADS_OK;
+}
+
 int check_flags(ads_handle* h) {
   int fl[FL_COUNT];
   ADS_CUDA(h, cudaMemcpyAsync(fl, h->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, h->stream));
@@ -681,6 +735,7 @@ int finish_stats(ads_handle* h, int k, double* l2norms) {
   h->last.refinements = mixed ? (int)last[2] : 0;
   h->last.converged = mixed ? (int)last[3] : 1;
   h->last.fp64_residuals = mixed ? (int)last[4] : 0;
+  h->last.host_path = 0;
   for (int i = 0; i < k; ++i)
     if (!std::isfinite(hist[HIST_W * i])) return fail(h, ADS_ERR_NONFINITE, "non-finite l2norm");
   if (mixed) {
@@ -843,6 +898,9 @@ int create_impl(ads_handle* h) {
   ADS_CUDA(h, cudaGetDeviceProperties(&prop, h->dev));
   const int nsm = prop.multiProcessorCount;
   const size_t smem_max = prop.sharedMemPerMultiprocessor;
+  int pageable = 0;
+  ADS_CUDA(h, cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, h->dev));
+  h->pageable = pageable != 0;
   if (!h->general) {
     // expected residency of the step's assembly: the FP32 kernel 3 CTAs/SM at
     // p <= 2, else 2; the double-float and FP64 kernels 2 at p <= 2, else 1
@@ -900,7 +958,7 @@ int create_impl(ads_handle* h) {
   }
   h->norm_parts = 4 * nsm;
   h->npart = std::max(3 * std::max(std::max(h->res_grid, h->rsd_grid), h->upd_grid), 2 * h->norm_parts);
-  if ((st = zalloc(&h->d_l2part, 3 * (size_t)h->asm_grid))) return st;
+  if ((st = zalloc(&h->d_l2part, 4 * (size_t)h->asm_grid))) return st;
   if ((st = zalloc(&h->d_part, (size_t)h->npart))) return st;
   if ((st = zalloc(&h->d_scal, SC_COUNT))) return st;
   ADS_CUDA(h, cudaMalloc(&h->d_flags, sizeof(int) * FL_COUNT));
@@ -929,6 +987,22 @@ int ensure_stage(ads_handle* h) {
   ADS_CUDA(h, cudaMalloc((void**)&h->d_stage, sizeof(double) * n));
   return ADS_OK;
 }
+// A pointer the handle's device can dereference for a caller's buffer of
+// doubles: the device pointer of pinned or registered host memory mapped for
+// this device, device memory of this device, managed memory, or pageable host
+// memory itself where the device reads pageable memory; null otherwise.
+const double* device_view(const ads_handle* h, const void* p) {
+  if (reinterpret_cast<uintptr_t>(p) % alignof(double)) return nullptr;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type == cudaMemoryTypeUnregistered) return h->pageable ? static_cast<const double*>(p) : nullptr;
+  if (at.type == cudaMemoryTypeDevice && at.device != h->dev) return nullptr;
+  return static_cast<const double*>(at.devicePointer);
+}
+
 int copy_l0_in(ads_handle* h, double* d, const double* src, cudaMemcpyKind kind) {
   const size_t bytes = sizeof(double) * (size_t)h->g.N[0] * h->g.N[1] * h->g.N[2];
   if (kind == cudaMemcpyDeviceToDevice) {
@@ -1273,6 +1347,7 @@ int ads_multistep(ads_handle* h, const double mix[12], double* l2norm) {
   h->last.refinements = 0;
   h->last.converged = 1;
   h->last.fp64_residuals = 0;
+  h->last.host_path = 0;
   if (l2norm) *l2norm = l2;
   return ADS_OK;
 }
@@ -1341,6 +1416,44 @@ int ads_step(ads_handle* h, double* l2norm) {
   int st = ads_steps(h, 1, &l2);
   if (l2norm) *l2norm = l2;
   return st;
+}
+
+int ads_step_host(ads_handle* h, const double* u_in, double* u_out, double* l2norm) {
+  if (!h || !u_in || !u_out) return ADS_ERR_ARG;
+  if (!h->has_form) return fail(h, ADS_ERR_STATE, "ads_set_form must be called before stepping");
+  if (h->form == ADS_FORM_OIL && !h->has_oil) return fail(h, ADS_ERR_STATE, "ads_set_oil must be called before stepping the oil form");
+  ADS_CUDA(h, cudaSetDevice(h->dev));
+  auto staged = [&](int path) -> int {
+    int s = ads_set_coeffs(h, u_in);
+    if (!s) s = ads_step(h, l2norm);
+    if (!s) s = ads_get_coeffs(h, u_out);
+    h->last.host_path = path;
+    return s;
+  };
+  const double* din = nullptr;
+  double* dout = nullptr;
+  if (df_increment(h) && !h->general) {
+    din = device_view(h, u_in);
+    dout = const_cast<double*>(device_view(h, u_out));
+  }
+  if (!din || !dout) return staged(0);
+  int st = ensure_hist(h, 64);
+  if (st) return st;
+  ADS_CUDA(h, cudaMemsetAsync(h->d_flags + FL_HIST, 0, sizeof(int), h->stream));
+  if ((st = enqueue_step_host(h, din, dout))) return st;
+  int fl[FL_COUNT];
+  ADS_CUDA(h, cudaMemcpyAsync(fl, h->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, h->stream));
+  ADS_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (fl[FL_UMISS]) {
+    // u_out was not written (d_u holds u_in); errors of the discarded attempt are dropped
+    ADS_CUDA(h, cudaMemsetAsync(h->d_flags + FL_ERR, 0, sizeof(int), h->stream));
+    return staged(2);
+  }
+  double l2 = 0.0;
+  if ((st = finish_stats(h, 1, &l2))) return st;
+  if (l2norm) *l2norm = l2;
+  h->last.host_path = 1;
+  return ADS_OK;
 }
 
 int ads_get_stats(const ads_handle* h, ads_stats* s) {

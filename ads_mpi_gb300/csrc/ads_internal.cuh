@@ -82,6 +82,10 @@ struct AssembleArgs {
   int nix, niy, niz;   // items per axis
   double dt, kappa;
   const double* u;     // L0 coefficients (FP64)
+  long long u_px;      // row pitch of u in entries: g.PX for a device array, g.N[0] for a
+                       // caller's unpadded array read in place (the double-float assembly only)
+  double* u_copy;      // if set (double-float assembly): every coefficient read, once, into
+                       // this padded array (rows of g.PX)
   double* F;           // L0 output (owned DOFs)
   double* shadow;      // 7 spill classes, each an L0-sized array
   long long shadow_stride;
@@ -108,6 +112,10 @@ struct FixupArgs {
   const unsigned char* slab;  // 1 where a DOF index lies in a spill slab: x [Nx], then y [Ny], then z [Nz]
   const int* xslab;           // the x indices of the x slabs, ascending
   int nxslab;
+  int* umiss;                 // if set (double-float assembly on a guessed scale): the max |u| the
+                              // assembly saw (l2part segment 3) is checked against SC_USCALE and
+                              // *umiss set when the scale was off by more than USCALE_WINDOW binades
+                              // or F is not finite; SC_USCALE then becomes the exact scale
 };
 
 struct SweepArgs {
@@ -227,6 +235,7 @@ enum FlagSlot {
   FL_ITERS,         // corrections applied in the current solve
   FL_HIST,          // number of recorded steps
   FL_RESID,         // FP64 residuals that ran in the current solve
+  FL_UMISS,         // the step on a caller's buffers found its guessed coefficient scale off
   FL_COUNT = 8
 };
 
@@ -271,6 +280,14 @@ cudaError_t launch_grid_to_qp(const double* src, double* dst, const Geometry& g,
 // y = alpha*x + beta*y over n entries
 // y += x
 cudaError_t launch_add(double* y, const double* x, long long n, cudaStream_t s);
+// d_u += delta, also into u_out: d_u and delta padded (rows of PX), u_out an
+// unpadded array (rows of N[0]) a caller owns, written in place.  Writes
+// nothing when *skip is set.
+cudaError_t launch_update_host(const double* delta, double* d_u, double* u_out, const Geometry& g,
+                               const int* skip, cudaStream_t s);
+// binades by which the guessed coefficient scale of a step on a caller's
+// buffers may differ from the exact one
+constexpr int USCALE_WINDOW = 8;
 cudaError_t launch_axpby(double* y, const double* x, double alpha, double beta, long long n,
                          cudaStream_t s);
 // out = sum x*y over n entries (deterministic two-stage)

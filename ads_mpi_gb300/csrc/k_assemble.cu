@@ -62,6 +62,36 @@ __global__ void k_fixup_scale(const FixupArgs a) {
     a.scal[SC_OUT_SCALE] = ldexp(1.0, e);
     a.scal[SC_IN_SCALE] = ldexp(1.0, -e);
   }
+  if (a.umiss) {
+    // The assembly ran on coefficients scaled by a guessed 2^-eg.  A power of
+    // two commutes with every rounding of the double-float arithmetic while the
+    // intermediates stay normal and finite, so within a few binades of the
+    // exact scale (max |u| < 2^e) the increment is the one the exact scale
+    // gives; outside the window, or with a non-finite F, the step is redone.
+    unsigned long long mu = 0ull;
+    for (int i = lane; i < a.nl2; i += 32) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(a.l2part[3 * a.nl2 + i]);
+      mu = b > mu ? b : mu;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ob = __shfl_down_sync(0xffffffffu, mu, o);
+      mu = ob > mu ? ob : mu;
+    }
+    if (lane == 0) {
+      const double um = __longlong_as_double((long long)mu);
+      const double fm = __longlong_as_double((long long)m);
+      const int eg = -pow2_exp(a.scal[SC_USCALE]);
+      int eu = 0;
+      const bool ufin = um <= 1.7976931348623157e308;
+      if (um > 0.0 && ufin) (void)frexp(um, &eu);
+      const int off = eu - eg;
+      const bool miss = !ufin || !(fm <= 1.7976931348623157e308) ||
+                        (um > 0.0 && (off > USCALE_WINDOW || off < -USCALE_WINDOW));
+      if (miss) *a.umiss = 1;
+      a.scal[SC_USCALE] = ldexp(1.0, -eu);
+    }
+  }
 }
 
 // F += shadow contributions, in class order.  One CTA per (y, z) row.  FP64

@@ -64,17 +64,18 @@ struct AsmLayout {
 // One coefficient plane z of the brick's footprint (CY rows of 32 DOFs along
 // x, coalesced) into shared memory with 8-byte cp.async copies; entries
 // outside the mesh are zero-filled.  (The brick's x origin is a multiple of
-// 32 - p, odd for odd p, so 16-byte copies would not stay aligned.)
+// 32 - p, odd for odd p, so 16-byte copies would not stay aligned.)  upx is
+// the row pitch of u: g.PX, or g.N[0] for a caller's unpadded array.
 template <int P>
 __device__ __forceinline__ void issue_plane(double* ring_plane, const double* __restrict__ u,
-                                            const Geometry& g, int x0, int y0, int z) {
+                                            const Geometry& g, int x0, int y0, int z, long long upx) {
   constexpr int CX = 32, CY = AS_TY + P;
   const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
   for (int it = threadIdx.x; it < CX * CY; it += AS_THREADS) {
     const int cy = it / CX, cx = it % CX;
     const int x = x0 + cx, y = y0 + cy;
     const bool ok = (z < Nz) && (y < Ny) && (x < Nx);
-    const double* src = ok ? u + (size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * z) : u;
+    const double* src = ok ? u + (size_t)x + (size_t)upx * ((size_t)y + (size_t)Ny * z) : u;
     cp_async8(ring_plane + it, src, ok ? 8 : 0);
   }
 }
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
     // initial coefficient planes ez0 .. ez0+P
     if (HEAT) {
 #pragma unroll
-      for (int b = 0; b <= P; ++b) issue_plane<P>(cring + ((ez0 + b) % RC) * NCOL, a.u, g, x0, y0, ez0 + b);
+      for (int b = 0; b <= P; ++b) issue_plane<P>(cring + ((ez0 + b) % RC) * NCOL, a.u, g, x0, y0, ez0 + b, a.u_px);
     }
     cp_async_commit();
 
@@ -230,7 +231,7 @@ __global__ void __launch_bounds__(AS_THREADS, (sizeof(T) == 4 && P <= 2) ? 3 : (
       T l2_layer = T(0);
       T dr_layer = T(0);
       // prefetch the plane the next layer adds
-      if (HEAT && ez + 1 < ez1) issue_plane<P>(cring + ((ez + P + 1) % RC) * NCOL, a.u, g, x0, y0, ez + P + 1);
+      if (HEAT && ez + 1 < ez1) issue_plane<P>(cring + ((ez + P + 1) % RC) * NCOL, a.u, g, x0, y0, ez + P + 1, a.u_px);
       cp_async_commit();
       for (int i = tid; i < L::NT; i += AS_THREADS) NZs[i] = tb.z.nn[(size_t)ez * L::NT + i];
       for (int i = tid; i < Q; i += AS_THREADS) JWZs[i] = tb.z.jw[(size_t)ez * Q + i];

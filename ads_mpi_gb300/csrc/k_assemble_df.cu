@@ -105,6 +105,7 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
 
   double l2_thread = 0.0;
   unsigned long long amax_bits = 0ull;  // max |written value| as ordered bits
+  unsigned long long umax_bits = 0ull;  // max |u| over the coefficients read, as ordered bits
 
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
     const int ix = item % a.nix;
@@ -145,14 +146,14 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
 
     // initial coefficient planes ez0 .. ez0+P
 #pragma unroll
-    for (int b = 0; b <= P; ++b) issue_plane<P>(cring + ((ez0 + b) % RC) * NCOL, a.u, g, x0, y0, ez0 + b);
+    for (int b = 0; b <= P; ++b) issue_plane<P>(cring + ((ez0 + b) % RC) * NCOL, a.u, g, x0, y0, ez0 + b, a.u_px);
     cp_async_commit();
 
     float l2_item = 0.f, l2_lo = 0.f;
 
     for (int ez = ez0; ez < ez1; ++ez) {
       float l2_layer = 0.f;
-      if (ez + 1 < ez1) issue_plane<P>(cring + ((ez + P + 1) % RC) * NCOL, a.u, g, x0, y0, ez + P + 1);
+      if (ez + 1 < ez1) issue_plane<P>(cring + ((ez + P + 1) % RC) * NCOL, a.u, g, x0, y0, ez + P + 1, a.u_px);
       cp_async_commit();
       for (int i = tid; i < NT; i += AS_THREADS) NZs[i] = tb.z.nn[(size_t)ez * NT + i];
       for (int i = tid; i < Q; i += AS_THREADS) JWZs[i] = tb.z.jw[(size_t)ez * Q + i];
@@ -165,7 +166,20 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
         for (int z = zlo; z <= ez + P; ++z) {
           const double* src = cring + (z % RC) * NCOL;
           dfl* dst = tring + (z % RC) * NCOL;
-          for (int i = tid; i < NCOL; i += AS_THREADS) dst[i] = df_split(src[i], uexp);
+          // the brick's own DOFs (those the next brick along an axis does not start with)
+          const bool ownz = ((z < ez1) || lastz) && z < g.N[2];
+          for (int i = tid; i < NCOL; i += AS_THREADS) {
+            const double v = src[i];
+            const unsigned long long vb = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+            umax_bits = vb > umax_bits ? vb : umax_bits;
+            dst[i] = df_split(v, uexp);
+            if (a.u_copy && ownz) {
+              const int cy = i / CX, cx = i % CX;
+              const int x = x0 + cx, y = y0 + cy;
+              if ((cx < TX || lastx) && (cy < TY || lasty) && x < Nx && y < Ny)
+                a.u_copy[(size_t)x + (size_t)g.PX * ((size_t)y + (size_t)Ny * z)] = v;
+            }
+          }
         }
       }
       __syncthreads();
@@ -396,28 +410,33 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
 
   // deterministic block reduction of the l2 partial and of max |value|
   double v = l2_thread;
-  unsigned long long mb = amax_bits;
+  unsigned long long mb = amax_bits, ub = umax_bits;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     v += __shfl_down_sync(0xffffffffu, v, o);
     const unsigned long long ob = __shfl_down_sync(0xffffffffu, mb, o);
     mb = ob > mb ? ob : mb;
+    const unsigned long long oub = __shfl_down_sync(0xffffffffu, ub, o);
+    ub = oub > ub ? oub : ub;
   }
   __syncthreads();
   unsigned long long* redm = reinterpret_cast<unsigned long long*>(red + AS_THREADS / 32);
-  if (lane == 0) { red[warp] = v; redm[warp] = mb; }
+  unsigned long long* redu = redm + AS_THREADS / 32;
+  if (lane == 0) { red[warp] = v; redm[warp] = mb; redu[warp] = ub; }
   __syncthreads();
   if (tid == 0) {
     double t = 0.0;
-    unsigned long long m = 0ull;
+    unsigned long long m = 0ull, mu = 0ull;
     for (int w = 0; w < AS_THREADS / 32; ++w) {
       t += red[w];
       m = redm[w] > m ? redm[w] : m;
+      mu = redu[w] > mu ? redu[w] : mu;
     }
     // the high parts integrated (2^uexp u)^2
     a.l2part[blockIdx.x] = t * ldexp(1.0, -2 * uexp);
     a.l2part[gridDim.x + blockIdx.x] = __longlong_as_double((long long)m);
     a.l2part[2 * gridDim.x + blockIdx.x] = 0.0;
+    a.l2part[3 * gridDim.x + blockIdx.x] = __longlong_as_double((long long)mu);
   }
 }
 

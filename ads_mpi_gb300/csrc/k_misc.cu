@@ -681,6 +681,7 @@ __global__ void k_step_reset(double* scal, int* flags) {
     flags[FL_CONV] = 0;
     flags[FL_ITERS] = 0;
     flags[FL_RESID] = 0;
+    flags[FL_UMISS] = 0;
     scal[SC_RELRES] = 0.0;
     scal[SC_RR] = 0.0;
   }
@@ -870,6 +871,41 @@ __global__ void k_add(double* y, const double* x, int n2) {
 cudaError_t launch_add(double* y, const double* x, long long n, cudaStream_t s) {
   const int n2 = (int)(n / 2);
   k_add<<<blocks_for(n2), 256, 0, s>>>(y, x, n2);
+  return cudaGetLastError();
+}
+
+// The update of a step on a caller's buffer: entry j of the unpadded u_out
+// (row r = j / Nx) sits at j + r (PX - Nx) in the padded arrays.  Four entries
+// per thread and pass keep stores to the caller's memory in flight.
+__global__ void k_update_host(const double* __restrict__ delta, double* __restrict__ d_u, double* __restrict__ u_out,
+                              long long n, int Nx, long long pad, const int* skip) {
+  if (*skip) return;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += 4 * stride) {
+    double v[4];
+    long long o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const long long j = i + k * stride;
+      if (j < n) {
+        o[k] = j + (j / Nx) * pad;
+        v[k] = d_u[o[k]] + delta[o[k]];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const long long j = i + k * stride;
+      if (j < n) {
+        d_u[o[k]] = v[k];
+        u_out[j] = v[k];
+      }
+    }
+  }
+}
+cudaError_t launch_update_host(const double* delta, double* d_u, double* u_out, const Geometry& g,
+                               const int* skip, cudaStream_t s) {
+  const long long n = (long long)g.N[0] * g.N[1] * g.N[2];
+  k_update_host<<<blocks_for((n + 3) / 4), 256, 0, s>>>(delta, d_u, u_out, n, g.N[0], g.PX - g.N[0], skip);
   return cudaGetLastError();
 }
 

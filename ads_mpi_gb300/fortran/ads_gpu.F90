@@ -33,6 +33,7 @@ module ads_gpu
       integer(c_int) :: refinements
       integer(c_int) :: converged
       integer(c_int) :: fp64_residuals
+      integer(c_int) :: host_path
    end type ads_stats
 
    type :: ads_gpu_handle
@@ -111,6 +112,14 @@ module ads_gpu
       integer(c_int) function ads_step(h, l2norm) bind(c, name="ads_step")
          import :: c_int, c_ptr, c_double
          type(c_ptr), value :: h
+         real(c_double), intent(out) :: l2norm
+      end function
+      ! u_out may be u_in: both are passed as c_loc of the state array
+      integer(c_int) function ads_step_host(h, u_in, u_out, l2norm) bind(c, name="ads_step_host")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: h
+         type(c_ptr), value :: u_in
+         type(c_ptr), value :: u_out
          real(c_double), intent(out) :: l2norm
       end function
       integer(c_int) function ads_steps(h, k, l2norms) bind(c, name="ads_steps")
@@ -248,6 +257,16 @@ contains
       if (mierr /= ADS_OK) return
       mierr = ads_get_coeffs(g % h, F)
    end subroutine GpuStep
+
+   ! Step (src/ADS.F90:437) on the state array itself: u holds the coefficients
+   ! before the call and the new ones after it (ads_step_host with u_out = u_in).
+   subroutine GpuStepInPlace(g, u, l2norm, mierr)
+      type(ads_gpu_handle), intent(in) :: g
+      real(c_double), intent(inout), target, contiguous :: u(:)
+      real(c_double), intent(out) :: l2norm
+      integer(kind=4), intent(out) :: mierr
+      mierr = ads_step_host(g % h, c_loc(u), c_loc(u), l2norm)
+   end subroutine GpuStepInPlace
 
    ! MultiStep (src/ADS.F90:391): mix(4,3) as the reference's; F receives the solution.
    subroutine GpuMultiStep(iter, mix, g, F, l2norm, mierr)

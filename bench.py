@@ -270,13 +270,19 @@ def time_device_steps(torch, g, K):
     return e0.elapsed_time(e1) / 1e3
 
 
-def time_e2e(torch, g, K, host_in, host_out):
+def time_e2e(torch, g, K, host_in, host_out, three_calls=False):
+    """K steps from the pinned host state host_in into host_out through the
+    C-ABI: ads_step_host (the step's kernels read host_in and write host_out),
+    or ads_set_coeffs + ads_step + ads_get_coeffs."""
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(K):
-        g.set_coeffs(host_in)
-        g.step()
-        g.coeffs_into(host_out)
+        if three_calls:
+            g.set_coeffs(host_in)
+            g.step()
+            g.coeffs_into(host_out)
+        else:
+            g.step_host(host_in, host_out)
     torch.cuda.synchronize()
     return time.perf_counter() - t0
 
@@ -724,13 +730,20 @@ def run_ours(args, world, rank, local):
     host_in = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
     host_out = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
     host_in[:] = u0
-    e2e = {}
+    e2e, e2e_route = {}, {}
     for name, g in handles:
         time_e2e(torch, g, min(W, 2), host_in, host_out)
         barrier(world)
         secs = time_e2e(torch, g, K, host_in, host_out)
         secs = max_over_ranks(world, secs, f"cuda:{dev}")
         e2e[name] = world * N * K / secs
+        e2e_route[name] = g.stats()["host_path"]
+    # the same steps as three calls with staged copies, for comparison
+    gm = dict(handles)["mixed"]
+    time_e2e(torch, gm, min(W, 2), host_in, host_out, three_calls=True)
+    barrier(world)
+    secs = max_over_ranks(world, time_e2e(torch, gm, K, host_in, host_out, three_calls=True), f"cuda:{dev}")
+    e2e_three_calls = world * N * K / secs
 
     # per-kernel CUDA events (a separate pass over the same steps)
     prof = {}
@@ -855,6 +868,10 @@ def run_ours(args, world, rank, local):
                       "e2e": e2e["fp64"], "gpu_launches": res["fp64"]["launches"]},
         "mixed_over_fp64": res["fp64"]["secs"] / secs,
         "e2e_mixed_over_fp64": e2e["mixed"] / e2e["fp64"],
+        "e2e_route": {"call": "ads_step_host(h, u_in, u_out, &l2) with pinned u_in, u_out",
+                      "host_path": e2e_route,
+                      "mixed_three_calls": {"value": e2e_three_calls, "calls": "ads_set_coeffs + ads_step + "
+                                            "ads_get_coeffs (staged copies)"}},
         "mixed_rel_err_vs_fp64": {
             "one_step": err1, "steps_1_to_5_configured_dt": err_steps,
             "stable_dt_100_steps_max": c3.get("p2", {}).get("mixed_rel_err_per_step_stable_dt_max"),

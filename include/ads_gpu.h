@@ -107,6 +107,11 @@ typedef struct ads_stats {
   int fp64_residuals;   /* FP64 residuals that ran in the last solve (mixed): one per
                            correction, plus one more where the certified bound stayed
                            above refine_tol and an FP64 residual decided; 0 for FP64 */
+  int host_path;        /* the last ads_step_host: 1 = the step's kernels read u_in and wrote
+                           u_out in place, 2 = they did, found the coefficient scale guessed
+                           from the previous step off and the step was redone on staged
+                           copies, 0 = staged copies (ads_set_coeffs, ads_step,
+                           ads_get_coeffs); 0 after any other call that steps */
 } ads_stats;
 
 int ads_default_opts(ads_opts* opts);
@@ -170,6 +175,20 @@ int ads_get_coeffs(ads_handle* h, double* u);
  * Kronecker solve, store the solution as the new coefficients.  l2norm may be
  * NULL. */
 int ads_step(ads_handle* h, double* l2norm);
+/* One Step on a caller's state arrays, as Step (src/ADS.F90:437-461) updates
+ * the state it is given: u_out = the step from u_in (both host layout,
+ * x-fastest, ndof entries; u_out may be u_in), the handle's coefficients
+ * become u_out, l2norm as ads_step (may be NULL).  The results are those of
+ * ads_set_coeffs(u_in), ads_step, ads_get_coeffs(u_out).  With the mixed
+ * heat step on a regular geometry, and buffers the device can address
+ * (pinned or registered host memory, device memory of the handle's GPU, or
+ * any host memory where the device reads pageable memory), the increment
+ * assembly reads u_in in place (its transfer hidden behind the assembly's
+ * arithmetic) and keeps it as the handle's coefficients, and the final
+ * update writes u_out in place; the coefficient scale comes from the
+ * previous step and is checked, and a step whose scale was off is redone on
+ * staged copies (ads_stats.host_path). */
+int ads_step_host(ads_handle* h, const double* u_in, double* u_out, double* l2norm);
 /* MultiStep(iter, mix, RHS_fun, ...) (src/ADS.F90:391-429): three substeps,
  * substep s assembling with the form (u from the start of the step, grad u
  * from the current coefficients, as FormUn(s) provides them) and solving
