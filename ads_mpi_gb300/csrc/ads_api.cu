@@ -596,13 +596,16 @@ int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready, bool f32_in
   if (st) return st;
   const int* conv = h->d_flags + FL_CONV;
   Phase ph(h, "Refinement");
-  auto residual = [&](bool want_ff) -> int {
+  // launches of the first round keep the plain timer names; those of later
+  // rounds (which return at once once the refinement has converged) are
+  // timed as *_late, so a timer never mixes working and returning launches
+  auto residual = [&](bool want_ff, bool late) -> int {
     ResidualArgs ra = residual_args(h, x, h->d_F, h->d_r);
     ra.skip_flag = conv;
     ra.want_ff = want_ff;
     ra.r32 = h->d_g32;
     ra.r32_scale = in_s;
-    RUN(h, "residual_f64", 1, launch_residual(h->P, ra, h->rsd_grid, h->stream));
+    RUN(h, late ? "residual_f64_late" : "residual_f64", 1, launch_residual(h->P, ra, h->rsd_grid, h->stream));
     return ADS_OK;
   };
   UpdateArgs ua{};
@@ -618,16 +621,20 @@ int enqueue_solve_mixed(ads_handle* h, double* x, bool scales_ready, bool f32_in
   ua.skip_flag = conv;
   const long long ndof = (long long)h->g.N[0] * h->g.N[1] * h->g.N[2];
   for (int k = 0; k < h->opts.max_refine; ++k) {
-    if ((st = residual(k == 0))) return st;
-    RUN(h, "decide", 1, launch_decide(h->d_part, h->rsd_grid, h->opts.refine_tol, true, k == 0, h->d_scal, h->d_flags, h->stream));
-    if ((st = enqueue_solve32(h, h->d_g32, 1, nullptr, nullptr, 0, conv, "_corr", nullptr))) return st;
-    RUN(h, "resid_update", 1, launch_resid_update(h->P, ua, h->upd_grid, h->stream));
-    RUN(h, "certify", 1, launch_certify(h->d_part, h->upd_grid, h->P, ndof, h->opts.refine_tol, h->d_scal,
-                                        h->d_flags, h->stream));
+    const bool late = k > 0;
+    if ((st = residual(k == 0, late))) return st;
+    RUN(h, late ? "decide_late" : "decide", 1,
+        launch_decide(h->d_part, h->rsd_grid, h->opts.refine_tol, true, k == 0, h->d_scal, h->d_flags, h->stream));
+    if ((st = enqueue_solve32(h, h->d_g32, 1, nullptr, nullptr, 0, conv, late ? "_corr_late" : "_corr", nullptr)))
+      return st;
+    RUN(h, late ? "resid_update_late" : "resid_update", 1, launch_resid_update(h->P, ua, h->upd_grid, h->stream));
+    RUN(h, late ? "certify_late" : "certify", 1,
+        launch_certify(h->d_part, h->upd_grid, h->P, ndof, h->opts.refine_tol, h->d_scal, h->d_flags, h->stream));
   }
-  if ((st = residual(h->opts.max_refine == 0))) return st;
-  RUN(h, "decide", 1, launch_decide(h->d_part, h->rsd_grid, h->opts.refine_tol, false, h->opts.max_refine == 0,
-                                    h->d_scal, h->d_flags, h->stream));
+  const bool late = h->opts.max_refine > 0;
+  if ((st = residual(!late, late))) return st;
+  RUN(h, late ? "decide_late" : "decide", 1,
+      launch_decide(h->d_part, h->rsd_grid, h->opts.refine_tol, false, !late, h->d_scal, h->d_flags, h->stream));
   return ADS_OK;
 }
 

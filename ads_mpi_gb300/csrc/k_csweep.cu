@@ -43,6 +43,11 @@ __device__ __forceinline__ void cs_cp16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(cs_smem_u32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cs_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// bytes (a multiple of 16) from a 16-byte aligned global address into L2
+__device__ __forceinline__ void cs_prefetch_l2(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(__cvta_generic_to_global(p)), "r"(bytes)
+               : "memory");
+}
 template <int N>
 __device__ __forceinline__ void cs_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
@@ -355,209 +360,236 @@ __global__ void __launch_bounds__(CS_MAX_WARPS * 32) k_csweep(const CSweepArgs a
 }
 
 // ---------------------------------------------------------------------------
-// The FP32 x sweep in column form (k_xsweep).  Along x the positions of a line
-// are contiguous, so a tile of 32 lines (32 consecutive y) is staged LINE-major
-// by 16-byte cp.async copies (coalesced: consecutive lanes copy consecutive
-// chunks of a line) into rows whose pitch is an odd number of 16-byte chunks.
-// Lane j then reads its own line four positions at a time: the eight lanes of
-// a quarter-warp read the same chunk index of eight rows, which the odd pitch
-// puts on eight different bank quads, so the 128-bit loads and stores are
-// conflict-free.  The lanes run across the lines as in k_csweep (all at the
-// same position, the LU factors of a position one broadcast load), forward and
-// backward in place in the staged rows, and the finished rows leave by 16-byte
-// stores, coalesced again.  Positions are processed in software-pipelined
-// blocks of 16; the input is staged in four position groups (separate commit
-// groups) so the forward pass starts when the first group has landed.  No wait
-// spins: cp.async groups complete in hardware.
+// The FP32 x sweep (k_xsweep): the banded LU solve along x, where the
+// positions of a line are contiguous in memory.  A warp solves a tile of 32
+// lines (32 consecutive y at one z), lane j line j, in blocks of XS_BLK
+// positions.  Only a ring of XS_RING staged blocks and, per block, the P
+// forward values it starts from (a checkpoint) stay on chip, so an SM holds
+// two to three times the lines that staging whole lines allowed, and the line
+// length is not bounded by shared memory.  The tile's input is first
+// prefetched into L2 in bulk, a line per lane.
+//   forward   blocks 0..nb-1 are staged XS_RING-1 ahead by 16-byte cp.async
+//             copies (a copy instruction moves 64 contiguous bytes of each of
+//             eight lines) into rows of XS_PITCH floats, five 16-byte chunks,
+//             so the eight lines a quarter-warp touches sit on different bank
+//             quads; each lane runs y_i = b_i - sum_m f[m]_i y_{i-m} over the
+//             block from four 128-bit reads of its row, keeping only the block
+//             checkpoint;
+//   backward  block b, from the top down, re-derives its forward values from
+//             its checkpoint and staged input (the last XS_RING blocks are
+//             still staged, earlier ones are staged again, from L2, XS_RING
+//             blocks ahead), runs x_i = bs_i y_i - sum_m g[m]_i x_{i+m} into
+//             its row, and leaves by 16-byte stores the way it came.
+// Positions past L are zero in the factor tables and in the staged values,
+// so they neither feed nor take anything.  No wait spins: cp.async groups
+// complete in hardware.
 // ---------------------------------------------------------------------------
-constexpr int XS_MAX_WARPS = 8;
-constexpr int XS_GROUPS = 4;
-
-// staged row pitch in floats: round_up(L, 4) positions, as an odd number of
-// 16-byte chunks
-__host__ __device__ inline int xs_pitch(int L) {
-  int c = (L + 3) / 4;
-  if ((c & 1) == 0) ++c;
-  return 4 * c;
-}
-size_t xsweep_warp_bytes(int L) { return sizeof(float) * 32 * (size_t)xs_pitch(L); }
+constexpr int XS_BLK = 16;        // positions per block
+constexpr int XS_RING = 3;        // staged blocks per warp
+constexpr int XS_PITCH = 20;      // floats per line of a staged block: four chunks and a spare
+constexpr int XS_MAX_WARPS = 8;   // warps per CTA (the launch picks the count that fits most per SM)
 
 template <int P>
-__global__ void __launch_bounds__(XS_MAX_WARPS * 32) k_xsweep(const CSweepArgs a) {
+struct XsLayout {
+  __host__ __device__ static int blocks(int L) { return (L + XS_BLK - 1) / XS_BLK; }
+  // the CTA's factor tables, dense per position: forward f[1..P] at [i][P],
+  // backward (bs, g[1..P]) at [i][P + 1], nb * XS_BLK positions
+  __host__ __device__ static size_t tab_bytes(int L) {
+    return sizeof(float) * (size_t)(2 * P + 1) * blocks(L) * XS_BLK;
+  }
+  // per warp: the ring [XS_RING][32][XS_PITCH] and the checkpoints [nb][P][32]
+  __host__ __device__ static size_t warp_floats(int L) {
+    return (size_t)XS_RING * 32 * XS_PITCH + (size_t)blocks(L) * P * 32;
+  }
+};
+
+__device__ __forceinline__ void xs_load_row(float (&v)[XS_BLK], const float* row) {
+#pragma unroll
+  for (int q = 0; q < XS_BLK / 4; ++q) {
+    const float4 t = reinterpret_cast<const float4*>(row)[q];
+    v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
+  }
+}
+__device__ __forceinline__ void xs_store_row(float* row, const float (&v)[XS_BLK]) {
+#pragma unroll
+  for (int q = 0; q < XS_BLK / 4; ++q)
+    reinterpret_cast<float4*>(row)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+}
+// N floats (a multiple of 4) from a 16-byte aligned table, by 128-bit loads
+template <int N>
+__device__ __forceinline__ void xs_load_tab(float (&f)[N], const float* p) {
+#pragma unroll
+  for (int q = 0; q < N / 4; ++q) {
+    const float4 t = reinterpret_cast<const float4*>(p)[q];
+    f[4 * q] = t.x; f[4 * q + 1] = t.y; f[4 * q + 2] = t.z; f[4 * q + 3] = t.w;
+  }
+}
+// forward recurrence over one block in place; prev[m] = y_{i-1-m} on entry and exit
+template <int P>
+__device__ __forceinline__ void xs_forward(float (&v)[XS_BLK], float (&prev)[P], const float* fp) {
+  float f[XS_BLK * P];
+  xs_load_tab(f, fp);
+#pragma unroll
+  for (int t = 0; t < XS_BLK; ++t) {
+    float y = v[t];
+#pragma unroll
+    for (int m = P; m >= 1; --m) y -= f[t * P + m - 1] * prev[m - 1];
+#pragma unroll
+    for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
+    prev[0] = y;
+    v[t] = y;
+  }
+}
+// backward recurrence over one block in place, top down; nxt[m] = x_{i+1+m}
+template <int P>
+__device__ __forceinline__ void xs_backward(float (&v)[XS_BLK], float (&nxt)[P], const float* bp) {
+  float c[XS_BLK * (P + 1)];
+  xs_load_tab(c, bp);
+#pragma unroll
+  for (int t = XS_BLK - 1; t >= 0; --t) {
+    float x = c[t * (P + 1)] * v[t];
+#pragma unroll
+    for (int m = P; m >= 1; --m) x -= c[t * (P + 1) + m] * nxt[m - 1];
+#pragma unroll
+    for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
+    nxt[0] = x;
+    v[t] = x;
+  }
+}
+
+template <int P>
+__global__ void __launch_bounds__(XS_MAX_WARPS * 32, 2) k_xsweep(const CSweepArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   if (a.skip_flag != nullptr && *a.skip_flag != 0) return;
-  using Tab = CsTab<P>;
-  constexpr int VF = Tab::VF, VB = Tab::VB;
+  using Lay = XsLayout<P>;
+  constexpr int SLOT = 32 * XS_PITCH;  // floats per staged block
   const int L = a.L;
-  const int Lp = xs_pitch(L);
+  const int nb = Lay::blocks(L);
+  const int NP = nb * XS_BLK;
   const int nch = (L + 3) / 4;  // 16-byte chunks of a line
   const int j = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  float4* FT = reinterpret_cast<float4*>(smem);  // [L][VF]
-  float4* BT = FT + (size_t)VF * L;              // [L][VB]
-  float* S = reinterpret_cast<float*>(smem + Tab::bytes(L)) + (size_t)warp * 32 * Lp;
+  const int cq = j >> 3, cl = j & 7;  // copies: chunk cq of lines cl, cl + 8, cl + 16, cl + 24
+  float* FT = reinterpret_cast<float*>(smem);  // [NP][P]
+  float* BT = FT + (size_t)P * NP;             // [NP][P + 1]
+  float* ring = BT + (size_t)(P + 1) * NP + (size_t)warp * Lay::warp_floats(L);
+  float* ck = ring + XS_RING * SLOT;  // [nb][P][32]
 
-  // factor rows (global [row][L]): row 0 fs (1 here), 1..P f, P+1 bs, P+2.. g
-  for (int i = threadIdx.x; i < L; i += blockDim.x) {
-    float fw[4 * VF], bw[4 * VB];
+  // factor rows (global [row][L]): row 0 fs (1 here), 1..P f, P+1 bs, P+2.. g;
+  // zero past L
+  for (int i = threadIdx.x; i < NP; i += blockDim.x) {
+    const bool in = i < L;
 #pragma unroll
-    for (int m = 0; m < 4 * VF; ++m) fw[m] = (m < P) ? a.fac[(size_t)(1 + m) * L + i] : 0.f;
+    for (int m = 0; m < P; ++m) FT[(size_t)i * P + m] = in ? a.fac[(size_t)(1 + m) * L + i] : 0.f;
 #pragma unroll
-    for (int m = 0; m < 4 * VB; ++m) bw[m] = (m <= P) ? a.fac[(size_t)(P + 1 + m) * L + i] : 0.f;
-#pragma unroll
-    for (int v = 0; v < VF; ++v) FT[(size_t)i * VF + v] = make_float4(fw[4 * v], fw[4 * v + 1], fw[4 * v + 2], fw[4 * v + 3]);
-#pragma unroll
-    for (int v = 0; v < VB; ++v) BT[(size_t)i * VB + v] = make_float4(bw[4 * v], bw[4 * v + 1], bw[4 * v + 2], bw[4 * v + 3]);
+    for (int m = 0; m <= P; ++m) BT[(size_t)i * (P + 1) + m] = in ? a.fac[(size_t)(P + 1 + m) * L + i] : 0.f;
   }
   __syncthreads();
 
   float* out = static_cast<float*>(a.out);
   const int tiles_l = (a.nl + 31) / 32;
   const int ntiles = tiles_l * a.n3;
-  const int GP = ((L + XS_GROUPS - 1) / XS_GROUPS + CS_BLK - 1) / CS_BLK * CS_BLK;  // positions per group
-
   for (int tile = blockIdx.x * nwarps + warp; tile < ntiles; tile += gridDim.x * nwarps) {
     const int tl = tile % tiles_l, t3 = tile / tiles_l;
     const int l0 = tl * 32;
     const int nlv = min(32, a.nl - l0);
     const float* src = a.in + (size_t)t3 * a.in_ts + (size_t)l0 * a.in_ls;
+    float* dst = out + (size_t)t3 * a.out_ts + (size_t)l0 * a.out_ls;
 
-    __syncwarp();  // the previous tile is done with S
-    // ---- stage: group g holds chunks [g*GP/4, (g+1)*GP/4) of every line ----
-#pragma unroll 1
-    for (int g = 0; g < XS_GROUPS; ++g) {
-      const int c0 = g * (GP / 4), c1 = min(nch, (g + 1) * (GP / 4));
-      const int ncg = c1 - c0;
-      for (int idx = j; idx < nlv * ncg; idx += 32) {
-        const int l = idx / ncg, c = c0 + idx % ncg;
-        cs_cp16(S + (size_t)l * Lp + 4 * c, src + (size_t)l * a.in_ls + 4 * c);
+    // this lane's copies: chunk cq of lines cl + 8k; block b adds 16 b floats
+    const float* sp[4];
+    float* dp[4];
+    bool lv[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int l = cl + 8 * k;
+      lv[k] = l < nlv;
+      sp[k] = src + (size_t)l * a.in_ls + 4 * cq;
+      dp[k] = dst + (size_t)l * a.out_ls + 4 * cq;
+    }
+    const int so = cl * XS_PITCH + 4 * cq;  // slot offset of line cl, chunk cq (line cl + 8k: + 8k XS_PITCH)
+    // block b of the tile's lines into the ring slot at sl
+    auto stage = [&](int b, float* sl) {
+      if (4 * b + cq < nch) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (lv[k]) cs_cp16(sl + so + 8 * k * XS_PITCH, sp[k] + XS_BLK * b);
       }
+    };
+    // the solved block b out of its slot sl, then block b - XS_RING into the slot
+    auto flush = [&](int b, float* sl) {
+      __syncwarp();
+      if (4 * b + cq < nch) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (lv[k])
+            *reinterpret_cast<float4*>(dp[k] + XS_BLK * b) =
+                *reinterpret_cast<const float4*>(sl + so + 8 * k * XS_PITCH);
+      }
+      __syncwarp();
+      if (b >= XS_RING) stage(b - XS_RING, sl);
+      cs_commit();
+    };
+
+    // the tile's input into L2 at once (a line per lane), so that staging
+    // waits on L2 rather than DRAM latency; the backward pass's second
+    // staging finds it there too
+    if (j < nlv) cs_prefetch_l2(src + (size_t)j * a.in_ls, 16u * (unsigned)nch);
+
+    __syncwarp();  // the previous tile is done with the ring
+#pragma unroll 1
+    for (int b = 0; b < XS_RING - 1; ++b) {
+      if (b < nb) stage(b, ring + b * SLOT);
       cs_commit();
     }
 
-    float* Sj = S + (size_t)j * Lp;
-    // ---- forward: y_i = b_i - sum_m f[m]_i y_{i-m}, in place ----
-    float prev[P];
+    // ---- forward; the last block turns straight into the backward pass ----
+    float prev[P], nxt[P];
 #pragma unroll
-    for (int m = 0; m < P; ++m) prev[m] = 0.f;
-    {
-      int i = 0;
+    for (int m = 0; m < P; ++m) prev[m] = nxt[m] = 0.f;
+    int sb = 0;  // ring slot of block b
 #pragma unroll 1
-      for (int g = 0; g < XS_GROUPS; ++g) {
-        switch (g) {
-          case 0: cs_wait<XS_GROUPS - 1>(); break;
-          case 1: cs_wait<XS_GROUPS - 2>(); break;
-          case 2: cs_wait<XS_GROUPS - 3>(); break;
-          default: cs_wait<0>(); break;
-        }
-        __syncwarp();
-        const int ie = min(L, (g + 1) * GP);
-#pragma unroll 1
-        for (; i + CS_BLK <= ie; i += CS_BLK) {
-          float4* yp = reinterpret_cast<float4*>(Sj + i);
-          const float4* fp = FT + (size_t)i * VF;
-          float bv[CS_BLK];
-          float4 fv[CS_BLK][VF];
+    for (int b = 0; b < nb; ++b) {
+      __syncwarp();  // every lane is done with block b-1, whose slot block b+XS_RING-1 takes
+      const int sn = (sb == 0) ? XS_RING - 1 : sb - 1;
+      if (b + XS_RING - 1 < nb) stage(b + XS_RING - 1, ring + sn * SLOT);
+      cs_commit();
+      cs_wait<XS_RING - 1>();
+      __syncwarp();
+      float* row = ring + sb * SLOT + j * XS_PITCH;
+      float v[XS_BLK];
+      xs_load_row(v, row);
+      if (b < nb - 1) {
 #pragma unroll
-          for (int q = 0; q < CS_BLK / 4; ++q) {
-            const float4 v4 = yp[q];
-            bv[4 * q] = v4.x; bv[4 * q + 1] = v4.y; bv[4 * q + 2] = v4.z; bv[4 * q + 3] = v4.w;
-          }
+        for (int m = 0; m < P; ++m) ck[(b * P + m) * 32 + j] = prev[m];
+        xs_forward<P>(v, prev, FT + (size_t)b * XS_BLK * P);
+        sb = (sb == XS_RING - 1) ? 0 : sb + 1;
+      } else {
 #pragma unroll
-          for (int t = 0; t < CS_BLK; ++t)
-#pragma unroll
-            for (int v = 0; v < VF; ++v) fv[t][v] = fp[t * VF + v];
-#pragma unroll
-          for (int t = 0; t < CS_BLK; ++t) {
-            const float* f = reinterpret_cast<const float*>(fv[t]);
-            float y = bv[t];
-#pragma unroll
-            for (int m = P; m >= 1; --m) y -= f[m - 1] * prev[m - 1];
-#pragma unroll
-            for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
-            prev[0] = y;
-            bv[t] = y;
-          }
-#pragma unroll
-          for (int q = 0; q < CS_BLK / 4; ++q) yp[q] = make_float4(bv[4 * q], bv[4 * q + 1], bv[4 * q + 2], bv[4 * q + 3]);
-        }
-#pragma unroll 1
-        for (; i < ie; ++i) {
-          float4 fv[VF];
-#pragma unroll
-          for (int v = 0; v < VF; ++v) fv[v] = FT[(size_t)i * VF + v];
-          const float* f = reinterpret_cast<const float*>(fv);
-          float y = Sj[i];
-#pragma unroll
-          for (int m = P; m >= 1; --m) y -= f[m - 1] * prev[m - 1];
-#pragma unroll
-          for (int m = P - 1; m >= 1; --m) prev[m] = prev[m - 1];
-          prev[0] = y;
-          Sj[i] = y;
-        }
+        for (int t = 0; t < XS_BLK; ++t)
+          if (b * XS_BLK + t >= L) v[t] = 0.f;
+        xs_forward<P>(v, prev, FT + (size_t)b * XS_BLK * P);
+        xs_backward<P>(v, nxt, BT + (size_t)b * XS_BLK * (P + 1));
+        xs_store_row(row, v);
       }
     }
+    flush(nb - 1, ring + sb * SLOT);
 
-    // ---- backward: x_i = bs_i y_i - sum_m g[m]_i x_{i+m}, in place ----
-    {
-      float nxt[P];
-#pragma unroll
-      for (int m = 0; m < P; ++m) nxt[m] = 0.f;
-      int i = L;
-      const int rem = L % CS_BLK;
+    // ---- backward over the other blocks ----
 #pragma unroll 1
-      for (int r = 0; r < rem; ++r) {
-        --i;
-        float4 bw[VB];
+    for (int b = nb - 2; b >= 0; --b) {
+      sb = (sb == 0) ? XS_RING - 1 : sb - 1;
+      cs_wait<XS_RING - 1>();  // block b's staging (from flush(b + XS_RING)) has landed
+      __syncwarp();
+      float* sl = ring + sb * SLOT;
+      float* row = sl + j * XS_PITCH;
+      float v[XS_BLK], pv[P];
+      xs_load_row(v, row);
 #pragma unroll
-        for (int v = 0; v < VB; ++v) bw[v] = BT[(size_t)i * VB + v];
-        const float* c = reinterpret_cast<const float*>(bw);
-        float x = c[0] * Sj[i];
-#pragma unroll
-        for (int m = P; m >= 1; --m) x -= c[m] * nxt[m - 1];
-#pragma unroll
-        for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
-        nxt[0] = x;
-        Sj[i] = x;
-      }
-#pragma unroll 1
-      for (; i >= CS_BLK; i -= CS_BLK) {
-        const int ib = i - CS_BLK;  // block [ib, i), processed downwards
-        float4* yp = reinterpret_cast<float4*>(Sj + ib);
-        const float4* bp = BT + (size_t)ib * VB;
-        float yv[CS_BLK];
-        float4 bw[CS_BLK][VB];
-#pragma unroll
-        for (int q = 0; q < CS_BLK / 4; ++q) {
-          const float4 v4 = yp[q];
-          yv[4 * q] = v4.x; yv[4 * q + 1] = v4.y; yv[4 * q + 2] = v4.z; yv[4 * q + 3] = v4.w;
-        }
-#pragma unroll
-        for (int t = 0; t < CS_BLK; ++t)
-#pragma unroll
-          for (int v = 0; v < VB; ++v) bw[t][v] = bp[t * VB + v];
-#pragma unroll
-        for (int t = CS_BLK - 1; t >= 0; --t) {
-          const float* c = reinterpret_cast<const float*>(bw[t]);
-          float x = c[0] * yv[t];
-#pragma unroll
-          for (int m = P; m >= 1; --m) x -= c[m] * nxt[m - 1];
-#pragma unroll
-          for (int m = P - 1; m >= 1; --m) nxt[m] = nxt[m - 1];
-          nxt[0] = x;
-          yv[t] = x;
-        }
-#pragma unroll
-        for (int q = 0; q < CS_BLK / 4; ++q) yp[q] = make_float4(yv[4 * q], yv[4 * q + 1], yv[4 * q + 2], yv[4 * q + 3]);
-      }
-    }
-
-    // ---- the solved rows out, 16-byte coalesced stores ----
-    __syncwarp();
-    float* dst = out + (size_t)t3 * a.out_ts + (size_t)l0 * a.out_ls;
-    for (int idx = j; idx < nlv * nch; idx += 32) {
-      const int l = idx / nch, c = idx % nch;
-      *reinterpret_cast<float4*>(dst + (size_t)l * a.out_ls + 4 * c) =
-          *reinterpret_cast<const float4*>(S + (size_t)l * Lp + 4 * c);
+      for (int m = 0; m < P; ++m) pv[m] = ck[(b * P + m) * 32 + j];
+      xs_forward<P>(v, pv, FT + (size_t)b * XS_BLK * P);
+      xs_backward<P>(v, nxt, BT + (size_t)b * XS_BLK * (P + 1));
+      xs_store_row(row, v);
+      flush(b, sl);
     }
   }
   cs_wait<0>();
@@ -570,15 +602,25 @@ static cudaError_t launch_xs(const CSweepArgs& a, cudaStream_t s) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t tab = CsTab<P>::bytes(a.L), per = xsweep_warp_bytes(a.L);
+  const size_t tab = XsLayout<P>::tab_bytes(a.L), per = sizeof(float) * XsLayout<P>::warp_floats(a.L);
   if (tab + per > (size_t)smem_max) return cudaErrorInvalidValue;
-  const int nw = (int)std::min<size_t>(XS_MAX_WARPS, ((size_t)smem_max - tab) / per);
-  const size_t bytes = tab + per * nw;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
   if (e != cudaSuccess) return e;
+  // the warps per CTA that put the most warps on an SM (the factor tables are per CTA)
+  int best_w = 1, best_total = 0;
+  for (int w = XS_MAX_WARPS; w >= 1; --w) {
+    const size_t bytes = tab + per * w;
+    if (bytes > (size_t)smem_max) continue;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, w * 32, bytes);
+    if (e != cudaSuccess) return e;
+    if (per_sm * w > best_total) { best_total = per_sm * w; best_w = w; }
+  }
+  const size_t bytes = tab + per * best_w;
+  const int per_sm = std::max(1, best_total / best_w);
   const int tiles = (a.nl + 31) / 32 * a.n3;
-  const int grid = std::max(1, std::min(nsm, (tiles + nw - 1) / nw));
-  kern<<<grid, 32 * nw, bytes, s>>>(a);
+  const int grid = std::max(1, std::min(nsm * per_sm, (tiles + best_w - 1) / best_w));
+  kern<<<grid, best_w * 32, bytes, s>>>(a);
   return cudaGetLastError();
 }
 
