@@ -158,6 +158,13 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append((time.perf_counter(), line.strip()))
 
+    def wait_ready(self, timeout=5.0):
+        """Until the first sample is in: nvidia-smi's start-up (NVML
+        initialisation) then lies before, not inside, a timed region."""
+        t_end = time.perf_counter() + timeout
+        while self.proc is not None and not self.lines and time.perf_counter() < t_end:
+            time.sleep(0.01)
+
     def stop(self):
         if self.proc:
             self.proc.terminate()
@@ -691,6 +698,7 @@ def run_ours(args, world, rank, local):
 
     clocks = ClockSampler(dev)
     clocks.start()
+    clocks.wait_ready()
     res = {}
     for name, g in handles:
         g.set_coeffs(u0)
