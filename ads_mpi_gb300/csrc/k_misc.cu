@@ -4,6 +4,7 @@
 #include "df32.cuh"
 
 #include <cfloat>
+#include <cstdint>
 #include <type_traits>
 
 namespace ads {
@@ -635,13 +636,34 @@ cudaError_t launch_norm_f(const double* F, const Geometry& g, double* part, int 
   return cudaGetLastError();
 }
 
+__device__ __forceinline__ unsigned long long umax_bits(unsigned long long m, double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+  return b > m ? b : m;
+}
+// max |u| per block; a 16-byte aligned u is read as double2, four per thread
+// and pass, so that each thread keeps several loads in flight
 __global__ void k_umax_partial(const double* u, long long n, double* part) {
   __shared__ unsigned long long sm[256];
   unsigned long long m = 0ull;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(u[i]) & 0x7fffffffffffffffull;
-    m = b > m ? b : m;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nt = (long long)gridDim.x * blockDim.x;
+  long long tail = 0;
+  if ((reinterpret_cast<uintptr_t>(u) & 15) == 0) {
+    const double2* u2 = reinterpret_cast<const double2*>(u);
+    const long long n2 = n / 2;
+    long long i = t;
+    for (; i + 3 * nt < n2; i += 4 * nt) {
+      const double2 a = u2[i], b = u2[i + nt], c = u2[i + 2 * nt], d = u2[i + 3 * nt];
+      m = umax_bits(umax_bits(umax_bits(umax_bits(m, a.x), a.y), b.x), b.y);
+      m = umax_bits(umax_bits(umax_bits(umax_bits(m, c.x), c.y), d.x), d.y);
+    }
+    for (; i < n2; i += nt) {
+      const double2 a = u2[i];
+      m = umax_bits(umax_bits(m, a.x), a.y);
+    }
+    tail = 2 * n2;
   }
+  for (long long i = tail + t; i < n; i += nt) m = umax_bits(m, u[i]);
   sm[threadIdx.x] = m;
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
