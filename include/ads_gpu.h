@@ -59,7 +59,8 @@ extern "C" {
 #define ADS_ERR_ZERO_PIVOT 3   /* zero pivot in the banded LU factorisation */
 #define ADS_ERR_NONFINITE 4    /* non-finite value in an input or result */
 #define ADS_ERR_NOCONV 5       /* iterative refinement did not reach the tolerance */
-#define ADS_ERR_TIMEOUT 6      /* a bounded device-side wait gave up */
+#define ADS_ERR_TIMEOUT 6      /* reserved for a bounded device-side wait that gives up: no kernel of
+                                  this library spins on a device-side condition, so no call returns it */
 #define ADS_ERR_UNSUPPORTED 7  /* valid but not supported by the GPU path (e.g. p > 4) */
 #define ADS_ERR_STATE 8        /* call out of order (no form set, ...) */
 #define ADS_ERR_ALLOC 9        /* device or host allocation failed */
@@ -173,7 +174,11 @@ int ads_get_coeffs(ads_handle* h, double* u);
 
 /* One Step: assemble with the current form from the current coefficients,
  * Kronecker solve, store the solution as the new coefficients.  l2norm may be
- * NULL. */
+ * NULL; it is the step's sum of J W v u^2 over points and test functions,
+ * the integral of the input state squared: FP64 sums with ADS_PREC_FP64;
+ * with the mixed precisions it is accumulated from the coefficients' FP32
+ * high parts (relative error ~1e-7, while the new state itself matches the
+ * FP64 step to ~1e-13). */
 int ads_step(ads_handle* h, double* l2norm);
 /* One Step on a caller's state arrays, as Step (src/ADS.F90:437-461) updates
  * the state it is given: u_out = the step from u_in (both host layout,

@@ -137,3 +137,20 @@ def test_step_host_rejects_bad_arrays(ads_mod):
         g.step_host(np.zeros(g.N, dtype=np.float32))
     with pytest.raises(ValueError):
         g.step_host(np.zeros((g.N, 2))[:, 0])
+
+
+def test_step_host_general_geometry_staged(ads_mod):
+    """Unequal degrees per axis (general geometry, FP64) take the staged
+    copies, with the three calls' results."""
+    hs = []
+    for _ in range(2):
+        g = ads_mod.ADS((13, 12, 11), (2, 3, 1), precision=ads_mod.PREC_FP64)
+        g.set_form(ads_mod.FORM_HEAT, kappa=1.0, dt=DT)
+        hs.append(g)
+    ref, g = hs
+    u_in, out = _pinned(ads_mod, g.N), _pinned(ads_mod, g.N)
+    u_in[:] = _u0(g.N)
+    want, l2_want = _staged(ref, u_in.copy())
+    assert g.step_host(u_in, out) == l2_want
+    assert g.stats()["host_path"] == 0
+    assert np.array_equal(out, want)
