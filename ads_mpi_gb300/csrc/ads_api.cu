@@ -86,6 +86,8 @@ struct ads_handle {
   int* d_gpiv[3] = {nullptr, nullptr, nullptr};
   double* d_gpart = nullptr;  // l2 partials of the general assembly
   float2* d_jwdf[3] = {nullptr, nullptr, nullptr};
+  float2* d_symdf[3] = {nullptr, nullptr, nullptr};        // p = 2: even-odd coefficients per element
+  unsigned char* d_symf[3] = {nullptr, nullptr, nullptr};  // ... and which elements are symmetric
   float2* d_band32[3] = {nullptr, nullptr, nullptr};  // double-float copies for the updated residual
 
   // device buffers
@@ -279,6 +281,45 @@ int upload(ads_handle* h, T** d, const std::vector<T>& v) {
   return ADS_OK;
 }
 
+// p = 2, three Gauss points: the even-odd coefficients of each element's
+// value and derivative tables (DfTab::sym) and whether they may stand for the
+// tables.  An element qualifies when N[k][b] = N[2-k][2-b] and
+// dN[k][b] = -dN[2-k][2-b] hold to 4e-15 of the table's largest entry (about
+// the double-float tables' own precision): the elements of a knot vector that
+// is uniform in FP64, except the first and the last, whose basis the open
+// knot vector's end knots bend.
+void even_odd_tables(const AxisHost& a, std::vector<double>& sc, std::vector<unsigned char>& sf) {
+  const int E = a.E;
+  sc.assign((size_t)E * DF_SYM, 0.0);
+  sf.assign((size_t)E, 0);
+  for (int e = 0; e < E; ++e) {
+    auto N = [&](int k, int b, int d) { return a.NN[(((size_t)e * 3 + k) * 3 + b) * 2 + d]; };
+    double mn = 0.0, md = 0.0;
+    for (int k = 0; k < 3; ++k)
+      for (int b = 0; b < 3; ++b) {
+        mn = std::max(mn, std::fabs(N(k, b, 0)));
+        md = std::max(md, std::fabs(N(k, b, 1)));
+      }
+    double en = 0.0, ed = 0.0;  // largest departure from the symmetry
+    for (int k = 0; k < 3; ++k)
+      for (int b = 0; b < 3; ++b) {
+        en = std::max(en, std::fabs(N(k, b, 0) - N(2 - k, 2 - b, 0)));
+        ed = std::max(ed, std::fabs(N(k, b, 1) + N(2 - k, 2 - b, 1)));
+      }
+    double* c = &sc[(size_t)e * DF_SYM];
+    c[0] = 0.5 * (N(0, 0, 0) + N(0, 2, 0));
+    c[1] = 0.5 * (N(0, 0, 0) - N(0, 2, 0));
+    c[2] = N(0, 1, 0);
+    c[3] = N(1, 0, 0);
+    c[4] = N(1, 1, 0);
+    c[5] = 0.5 * (N(0, 0, 1) + N(0, 2, 1));
+    c[6] = 0.5 * (N(0, 0, 1) - N(0, 2, 1));
+    c[7] = N(0, 1, 1);
+    c[8] = N(1, 0, 1);
+    sf[e] = (en <= 4e-15 * mn && ed <= 4e-15 * md) ? 1 : 0;
+  }
+}
+
 bool encode(CUtensorMap* m, void* base, bool fp32, cuuint64_t d0, cuuint64_t d1, cuuint64_t d2,
             long long pitch, cuuint32_t b0, cuuint32_t b1, cuuint32_t b2) {
   PFN_encodeTiled fn = get_encode();
@@ -426,7 +467,12 @@ int enqueue_assemble_gen(ads_handle* h, const double* u, double* F, bool incr, b
 DfTabs3 df_tabs(const ads_handle* h) {
   DfTabs3 tb;
   DfTab* t[3] = {&tb.x, &tb.y, &tb.z};
-  for (int d = 0; d < 3; ++d) { t[d]->nn = h->d_nndf[d]; t[d]->jw = h->d_jwdf[d]; }
+  for (int d = 0; d < 3; ++d) {
+    t[d]->nn = h->d_nndf[d];
+    t[d]->jw = h->d_jwdf[d];
+    t[d]->sym = h->d_symdf[d];
+    t[d]->symf = h->d_symf[d];
+  }
   return tb;
 }
 
@@ -775,6 +821,7 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_dd64[d]); cudaFree(h->d_dd32[d]);
     cudaFree(h->d_fac64[d]); cudaFree(h->d_tfac64[d]); cudaFree(h->d_fac32[d]); cudaFree(h->d_band[d]);
     cudaFree(h->d_band32[d]); cudaFree(h->d_nndf[d]); cudaFree(h->d_jwdf[d]);
+    cudaFree(h->d_symdf[d]); cudaFree(h->d_symf[d]);
     cudaFree(h->d_gab[d]); cudaFree(h->d_gpiv[d]);
   }
   cudaFree(h->d_gpart);
@@ -871,6 +918,13 @@ int create_impl(ads_handle* h) {
     if (h->opts.precision == ADS_PREC_MIXED) {
       if ((st = upload(h, &h->d_nndf[d], split(a.NN)))) return st;
       if ((st = upload(h, &h->d_jwdf[d], split(a.JW)))) return st;
+      if (a.p == 2) {
+        std::vector<double> sc;
+        std::vector<unsigned char> sf;
+        even_odd_tables(a, sc, sf);
+        if ((st = upload(h, &h->d_symdf[d], split(sc)))) return st;
+        if ((st = upload(h, &h->d_symf[d], sf))) return st;
+      }
     }
   }
 

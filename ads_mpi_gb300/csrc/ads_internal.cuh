@@ -50,7 +50,14 @@ struct AxisTab {
 struct DfTab {
   const float2* nn;  // [E][Q][P+1][2]
   const float2* jw;  // [E][Q]
+  // p = 2: per element, the even-odd coefficients of its centro-symmetric
+  // tables (N[k][b] = N[2-k][2-b], dN[k][b] = -dN[2-k][2-b]):
+  //   [(N00+N02)/2, (N00-N02)/2, N01, N10, N11, (dN00+dN02)/2, (dN00-dN02)/2, dN01, dN10]
+  // and symf[e] = 1 where the element's tables are symmetric (null: none are)
+  const float2* sym;           // [E][DF_SYM]
+  const unsigned char* symf;   // [E]
 };
+constexpr int DF_SYM = 9;
 struct DfTabs3 {
   DfTab x, y, z;
 };

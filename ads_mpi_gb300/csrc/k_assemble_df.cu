@@ -55,7 +55,10 @@ struct DfLayout {
   static constexpr size_t o_jwy = o_ny + D * TY * NT;           // dfl [TY][Q]
   static constexpr size_t o_nz = o_jwy + D * TY * Q;            // dfl [NT]
   static constexpr size_t o_jwz = o_nz + D * NT;                // dfl [Q]
-  static constexpr size_t o_red = (o_jwz + D * Q + 15) / 16 * 16;
+  static constexpr size_t o_sy = o_jwz + D * Q;                 // dfl [TY][DF_SYM] (p = 2)
+  static constexpr size_t o_sz = o_sy + D * TY * DF_SYM;        // dfl [DF_SYM]
+  static constexpr size_t o_sf = o_sz + D * DF_SYM;             // int [TY + 1]: rows, then the layer
+  static constexpr size_t o_red = (o_sf + 4 * (TY + 1) + 15) / 16 * 16;
   static constexpr size_t bytes = o_red + 3 * sizeof(double) * (AS_THREADS / 32);
 };
 
@@ -64,6 +67,71 @@ __device__ __forceinline__ dfl df_split(double d, int sexp) {
   split_scaled(d, sexp, h, l);
   return df_make(h, l);
 }
+
+// ---- even-odd forms of an element's 3 x 3 contractions (p = 2) ----
+// For an element whose tables are centro-symmetric, N[k][b] = N[2-k][2-b]
+// and dN[k][b] = -dN[2-k][2-b] (Gauss points symmetric about the element's
+// centre, basis mirrored: every element of a uniform knot vector but the
+// first and the last), the sums over b of an interpolation pair the outputs k
+// and 2-k: with s = v0 + v2 and d = v0 - v2,
+//   sum_b N[k][b] v[b]:  out0,2 = (a s + N01 v1) +- c d,  out1 = N10 s + N11 v1
+//   sum_b dN[k][b] v[b]: out0,2 = a' s + dN01 v1 ... (signs below), out1 = dN10 d
+// with a = (N00 + N02)/2, c = (N00 - N02)/2 (a', c' the same for dN); the
+// test contractions (sums over k) are the transposes.  A double-float
+// multiply-add costs 12 FP32 operations and a sum 8, so the forms below take
+// 52-68 operations for what the direct sums do in 84.
+struct SymN { dfl a, c, n01, n10, n11; };
+struct SymD { dfl a, c, d01, d10; };
+
+__device__ __forceinline__ dfl df_sub(dfl a, dfl b) { return df_add(a, df_neg(b)); }
+
+// out[k] = sum_b N[k][b] v[b]
+__device__ __forceinline__ void eo_interp_n(dfl (&out)[3], const dfl (&v)[3], const SymN& n) {
+  const dfl sp = df_add(v[0], v[2]), dm = df_sub(v[0], v[2]);
+  const dfl e = df_mac(df_mul(n.a, sp), n.n01, v[1]), d = df_mul(n.c, dm);
+  out[0] = df_add(e, d);
+  out[2] = df_sub(e, d);
+  out[1] = df_mac(df_mul(n.n10, sp), n.n11, v[1]);
+}
+// on[k] = sum_b N[k][b] v[b], od[k] = sum_b dN[k][b] v[b] (s and d shared)
+__device__ __forceinline__ void eo_interp_nd(dfl (&on)[3], dfl (&od)[3], const dfl (&v)[3], const SymN& n,
+                                             const SymD& dn) {
+  const dfl sp = df_add(v[0], v[2]), dm = df_sub(v[0], v[2]);
+  const dfl e = df_mac(df_mul(n.a, sp), n.n01, v[1]), d = df_mul(n.c, dm);
+  on[0] = df_add(e, d);
+  on[2] = df_sub(e, d);
+  on[1] = df_mac(df_mul(n.n10, sp), n.n11, v[1]);
+  const dfl e2 = df_mac(df_mul(dn.a, sp), dn.d01, v[1]), d2 = df_mul(dn.c, dm);
+  od[0] = df_add(d2, e2);
+  od[2] = df_sub(d2, e2);
+  od[1] = df_mul(dn.d10, dm);
+}
+// out[k] = sum_b dN[k][b] v[b]
+__device__ __forceinline__ void eo_interp_d(dfl (&out)[3], const dfl (&v)[3], const SymD& dn) {
+  const dfl sp = df_add(v[0], v[2]), dm = df_sub(v[0], v[2]);
+  const dfl e = df_mac(df_mul(dn.a, sp), dn.d01, v[1]), d = df_mul(dn.c, dm);
+  out[0] = df_add(d, e);
+  out[2] = df_sub(d, e);
+  out[1] = df_mul(dn.d10, dm);
+}
+// h[b] = sum_k N[k][b] g[k]
+__device__ __forceinline__ void eo_test_n(dfl (&h)[3], const dfl (&g)[3], const SymN& n) {
+  const dfl sp = df_add(g[0], g[2]), dm = df_sub(g[0], g[2]);
+  const dfl e = df_mac(df_mul(n.a, sp), n.n10, g[1]), d = df_mul(n.c, dm);
+  h[0] = df_add(e, d);
+  h[2] = df_sub(e, d);
+  h[1] = df_mac(df_mul(n.n01, sp), n.n11, g[1]);
+}
+// h[b] = sum_k dN[k][b] g[k]
+__device__ __forceinline__ void eo_test_d(dfl (&h)[3], const dfl (&g)[3], const SymD& dn) {
+  const dfl sp = df_add(g[0], g[2]), dm = df_sub(g[0], g[2]);
+  const dfl e = df_mac(df_mul(dn.c, sp), dn.d10, g[1]), d = df_mul(dn.a, dm);
+  h[0] = df_add(e, d);
+  h[2] = df_sub(d, e);
+  h[1] = df_mul(dn.d01, dm);
+}
+__device__ __forceinline__ SymN sym_n(const dfl* t) { return SymN{t[0], t[1], t[2], t[3], t[4]}; }
+__device__ __forceinline__ SymD sym_d(const dfl* t) { return SymD{t[5], t[6], t[7], t[8]}; }
 
 template <int P, bool HAS_F, bool HAS_K>
 __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
@@ -88,6 +156,9 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
   dfl* JWYs = reinterpret_cast<dfl*>(smem + L::o_jwy);
   dfl* NZs = reinterpret_cast<dfl*>(smem + L::o_nz);
   dfl* JWZs = reinterpret_cast<dfl*>(smem + L::o_jwz);
+  dfl* SYs = reinterpret_cast<dfl*>(smem + L::o_sy);
+  dfl* SZs = reinterpret_cast<dfl*>(smem + L::o_sz);
+  int* SF = reinterpret_cast<int*>(smem + L::o_sf);
   double* red = reinterpret_cast<double*>(smem + L::o_red);
 
   const Geometry& g = a.g;
@@ -118,25 +189,50 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
 
     __syncthreads();  // previous item fully done with shared memory
 
-    // per-lane x tables (element x0 + lane; lanes >= TX have no element)
+    // per-lane x tables (element x0 + lane; lanes >= TX have no element).
+    // p = 2 bricks whose elements are all centro-symmetric run the x stage in
+    // even-odd form; the table registers then hold the lane's DF_SYM
+    // even-odd coefficients
     dfl nx[Q][P + 1][2];
     dfl jwx[Q];
     const bool lane_elem = (lane < TX) && (x0 + lane < Ex);
+    bool symx = false;
+    if constexpr (P == 2) {
+      if (tb.x.sym != nullptr) symx = __all_sync(0xffffffffu, !lane_elem || tb.x.symf[x0 + lane] != 0);
+    }
     {
       const int ex = x0 + lane;
 #pragma unroll
-      for (int k = 0; k < Q; ++k) {
-        jwx[k] = lane_elem ? tb.x.jw[(size_t)ex * Q + k] : df_zero();
+      for (int k = 0; k < Q; ++k) jwx[k] = lane_elem ? tb.x.jw[(size_t)ex * Q + k] : df_zero();
+      if (symx) {
+        dfl* t = &nx[0][0][0];
 #pragma unroll
-        for (int b = 0; b <= P; ++b) {
-          nx[k][b][0] = lane_elem ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 0] : df_zero();
-          nx[k][b][1] = lane_elem ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 1] : df_zero();
+        for (int i = 0; i < Q * (P + 1) * 2; ++i)
+          t[i] = (i < DF_SYM && lane_elem) ? tb.x.sym[(size_t)ex * DF_SYM + i] : df_zero();
+      } else {
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+#pragma unroll
+          for (int b = 0; b <= P; ++b) {
+            nx[k][b][0] = lane_elem ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 0] : df_zero();
+            nx[k][b][1] = lane_elem ? tb.x.nn[(((size_t)ex * Q + k) * (P + 1) + b) * 2 + 1] : df_zero();
+          }
         }
       }
     }
     for (int i = tid; i < TY * NT; i += AS_THREADS) {
       const int ey = y0 + i / NT;
       NYs[i] = (ey < Ey) ? tb.y.nn[(size_t)ey * NT + (i % NT)] : df_zero();
+    }
+    if constexpr (P == 2) {
+      // the element rows' even-odd coefficients and flags (the y stage of a
+      // row, one warp, takes the even-odd form where its element qualifies)
+      const bool ys = tb.y.sym != nullptr;
+      for (int i = tid; i < TY * DF_SYM; i += AS_THREADS) {
+        const int ey = y0 + i / DF_SYM;
+        SYs[i] = (ys && ey < Ey) ? tb.y.sym[(size_t)ey * DF_SYM + (i % DF_SYM)] : df_zero();
+      }
+      for (int i = tid; i < TY; i += AS_THREADS) SF[i] = (ys && y0 + i < Ey) ? (int)tb.y.symf[y0 + i] : 0;
     }
     for (int i = tid; i < TY * Q; i += AS_THREADS) {
       const int ey = y0 + i / Q;
@@ -157,8 +253,15 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
       cp_async_commit();
       for (int i = tid; i < NT; i += AS_THREADS) NZs[i] = tb.z.nn[(size_t)ez * NT + i];
       for (int i = tid; i < Q; i += AS_THREADS) JWZs[i] = tb.z.jw[(size_t)ez * Q + i];
+      if constexpr (P == 2) {
+        const bool zs = tb.z.sym != nullptr;
+        for (int i = tid; i < DF_SYM; i += AS_THREADS) SZs[i] = zs ? tb.z.sym[(size_t)ez * DF_SYM + i] : df_zero();
+        if (tid == 0) SF[TY] = zs ? (int)tb.z.symf[ez] : 0;
+      }
       cp_async_wait<1>();
       __syncthreads();
+      const bool symz = (P == 2) && SF[TY] != 0;
+      const bool symy = (P == 2) && SF[my_ey] != 0;  // warp-uniform: a warp is one element row
 
       // split each coefficient plane once, when it arrives
       {
@@ -185,7 +288,24 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
       __syncthreads();
 
       // ---- z interpolation per column: ZA = sum_b Nz C, ZB = sum_b dNz C ----
-      for (int col = tid; col < NCOL; col += AS_THREADS) {
+      if constexpr (P == 2) {
+        if (symz) {
+          const SymN sn = sym_n(SZs);
+          const SymD sd = sym_d(SZs);
+          for (int col = tid; col < NCOL; col += AS_THREADS) {
+            dfl c[3], za[3], zb[3];
+#pragma unroll
+            for (int b = 0; b < 3; ++b) c[b] = tring[((ez + b) % RC) * NCOL + col];
+            eo_interp_nd(za, zb, c, sn, sd);
+#pragma unroll
+            for (int kz = 0; kz < 3; ++kz) {
+              ZA[kz * NCOL + col] = za[kz];
+              ZB[kz * NCOL + col] = zb[kz];
+            }
+          }
+        }
+      }
+      for (int col = symz ? NCOL : tid; col < NCOL; col += AS_THREADS) {
         dfl c[P + 1];
 #pragma unroll
         for (int b = 0; b <= P; ++b) c[b] = tring[((ez + b) % RC) * NCOL + col];
@@ -221,22 +341,40 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
             za[b] = ZA[kz * NCOL + (my_ey + b) * CX + my_cx];
             zb[b] = ZB[kz * NCOL + (my_ey + b) * CX + my_cx];
           }
+          if constexpr (P == 2) {
+            if (symy) {
+              const SymN sn = sym_n(SYs + my_ey * DF_SYM);
+              const SymD sd = sym_d(SYs + my_ey * DF_SYM);
+              dfl y0v[3], y1v[3], y2v[3];
+              eo_interp_nd(y0v, y1v, za, sn, sd);
+              eo_interp_n(y2v, zb, sn);
 #pragma unroll
-          for (int ky = 0; ky < Q; ++ky) {
-            const dfl* ny = NYs + my_ey * NT + ky * (P + 1) * 2;
-            dfl y0v = df_mul(ny[0], za[0]);
-            dfl y1v = df_mul(ny[1], za[0]);
-            dfl y2v = df_mul(ny[0], zb[0]);
-#pragma unroll
-            for (int b = 1; b <= P; ++b) {
-              y0v = df_mac(y0v, ny[2 * b], za[b]);
-              y1v = df_mac(y1v, ny[2 * b + 1], za[b]);
-              y2v = df_mac(y2v, ny[2 * b], zb[b]);
+              for (int ky = 0; ky < 3; ++ky) {
+                const int qy = my_ey * Q + ky;
+                Y0[qy * CX + my_cx] = y0v[ky];
+                Y1[qy * CX + my_cx] = y1v[ky];
+                Y2[qy * CX + my_cx] = y2v[ky];
+              }
             }
-            const int qy = my_ey * Q + ky;
-            Y0[qy * CX + my_cx] = y0v;
-            Y1[qy * CX + my_cx] = y1v;
-            Y2[qy * CX + my_cx] = y2v;
+          }
+          if (!symy) {
+#pragma unroll
+            for (int ky = 0; ky < Q; ++ky) {
+              const dfl* ny = NYs + my_ey * NT + ky * (P + 1) * 2;
+              dfl y0v = df_mul(ny[0], za[0]);
+              dfl y1v = df_mul(ny[1], za[0]);
+              dfl y2v = df_mul(ny[0], zb[0]);
+#pragma unroll
+              for (int b = 1; b <= P; ++b) {
+                y0v = df_mac(y0v, ny[2 * b], za[b]);
+                y1v = df_mac(y1v, ny[2 * b + 1], za[b]);
+                y2v = df_mac(y2v, ny[2 * b], zb[b]);
+              }
+              const int qy = my_ey * Q + ky;
+              Y0[qy * CX + my_cx] = y0v;
+              Y1[qy * CX + my_cx] = y1v;
+              Y2[qy * CX + my_cx] = y2v;
+            }
           }
         }
         __syncthreads();
@@ -247,16 +385,79 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
           const bool elem_ok = lane_elem && (y0 + ey_l < Ey);
           const dfl jwyz = df_mul(JWYs[qy], JWZs[kz]);
           const dfl cyz = df_mul(ndtk, jwyz);
-          dfl yv0[P + 1], yv1[P + 1], yv2[P + 1];
+          // this lane's P + 1 values of a y-interpolated plane
+          auto yrow = [&](const dfl* Yp, dfl (&v)[P + 1]) {
 #pragma unroll
-          for (int b = 0; b <= P; ++b) {
-            yv0[b] = lane_elem ? Y0[qy * CX + lane + b] : df_zero();
-            yv1[b] = lane_elem ? Y1[qy * CX + lane + b] : df_zero();
-            yv2[b] = lane_elem ? Y2[qy * CX + lane + b] : df_zero();
-          }
+            for (int b = 0; b <= P; ++b) v[b] = lane_elem ? Yp[qy * CX + lane + b] : df_zero();
+          };
           const long long qyg = (long long)y0 * Q + qy;
           const long long qzg = (long long)ez * Q + kz;
           dfl h0[P + 1], h1[P + 1], h2[P + 1];
+          if constexpr (P == 2) {
+            if (symx) {
+              const SymN sn = sym_n(&nx[0][0][0]);
+              const SymD sd = sym_d(&nx[0][0][0]);
+              // the point weights, then one gradient component at a time:
+              // interpolate, weight, contract
+              dfl cw[3];
+              float sx[3];
+              dfl g0[3];
+#pragma unroll
+              for (int kx = 0; kx < 3; ++kx) {
+                const long long qidx = ((long long)(x0 + lane) * Q + kx) + QXt * (qyg + QYt * qzg);
+                const dfl s = df_mul(jwx[kx], jwyz);
+                sx[kx] = s.x;
+                if constexpr (HAS_K) cw[kx] = df_mul(df_mul(ndt, elem_ok ? df_split(a.kqp[qidx], 0) : df_zero()), s);
+                else cw[kx] = df_mul(jwx[kx], cyz);
+                if constexpr (HAS_F) g0[kx] = df_mul(df_mul(s, dtv), elem_ok ? df_split(a.fqp[qidx], uexp) : df_zero());
+              }
+              dfl yv0[3];
+              yrow(Y0, yv0);
+              {
+                // u at the points from the high parts (the l2norm), the same even-odd form
+                const float sp = yv0[0].x + yv0[2].x, dm = yv0[0].x - yv0[2].x;
+                const float e = fmaf(sn.n01.x, yv0[1].x, sn.a.x * sp), d = sn.c.x * dm;
+                const float u0 = e + d, u2 = e - d, u1 = fmaf(sn.n11.x, yv0[1].x, sn.n10.x * sp);
+                l2_layer = fmaf(sx[0] * u0, u0, l2_layer);
+                l2_layer = fmaf(sx[1] * u1, u1, l2_layer);
+                l2_layer = fmaf(sx[2] * u2, u2, l2_layer);
+              }
+              {
+                dfl du[3];
+                eo_interp_d(du, yv0, sd);
+#pragma unroll
+                for (int kx = 0; kx < 3; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
+                eo_test_d(h0, du, sd);
+              }
+              {
+                dfl du[3], yv1[3];
+                yrow(Y1, yv1);
+                eo_interp_n(du, yv1, sn);
+#pragma unroll
+                for (int kx = 0; kx < 3; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
+                eo_test_n(h1, du, sn);
+              }
+              {
+                dfl du[3], yv2[3];
+                yrow(Y2, yv2);
+                eo_interp_n(du, yv2, sn);
+#pragma unroll
+                for (int kx = 0; kx < 3; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
+                eo_test_n(h2, du, sn);
+              }
+              if constexpr (HAS_F) {
+                dfl hf[3];
+                eo_test_n(hf, g0, sn);
+#pragma unroll
+                for (int b = 0; b < 3; ++b) h0[b] = df_add(h0[b], hf[b]);
+              }
+            }
+          }
+          if (!symx) {
+          dfl yv0[P + 1], yv1[P + 1], yv2[P + 1];
+          yrow(Y0, yv0);
+          yrow(Y1, yv1);
+          yrow(Y2, yv2);
 #pragma unroll
           for (int kx = 0; kx < Q; ++kx) {
             dfl dux = df_mul(nx[kx][0][1], yv0[0]);
@@ -293,6 +494,7 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
               if constexpr (HAS_F) h0[b] = df_mac(h0[b], nx[kx][b][0], g0);
             }
           }
+          }  // !symx
           // column cx = lane receives local function b of element lane - b
           dfl v0 = h0[0], v1 = h1[0], v2 = h2[0];
 #pragma unroll
@@ -311,6 +513,26 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
         // ---- y test contraction of this thread's element row, then z ----
         {
           dfl i0[P + 1], i1[P + 1];
+          if constexpr (P == 2) {
+            if (symy) {
+              const SymN sn = sym_n(SYs + my_ey * DF_SYM);
+              const SymD sd = sym_d(SYs + my_ey * DF_SYM);
+              dfl hv0[3], hv1[3], hv2[3], ta[3], tb1[3];
+#pragma unroll
+              for (int ky = 0; ky < 3; ++ky) {
+                const int qy = my_ey * Q + ky;
+                hv0[ky] = H0[qy * CX + my_cx];
+                hv1[ky] = H1[qy * CX + my_cx];
+                hv2[ky] = H2[qy * CX + my_cx];
+              }
+              eo_test_n(ta, hv0, sn);
+              eo_test_d(tb1, hv1, sd);
+#pragma unroll
+              for (int by = 0; by < 3; ++by) i0[by] = df_add(ta[by], tb1[by]);
+              eo_test_n(i1, hv2, sn);
+            }
+          }
+          if (!symy) {
 #pragma unroll
           for (int ky = 0; ky < Q; ++ky) {
             const int qy = my_ey * Q + ky;
@@ -330,6 +552,7 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
               i0[by] = df_mac(i0[by], ny[2 * by + 1], hv1);
             }
           }
+          }  // !symy
 #pragma unroll
           for (int bz = 0; bz <= P; ++bz) {
             const dfl nz0 = NZs[(kz * (P + 1) + bz) * 2 + 0];

@@ -209,13 +209,16 @@ def algorithmic_assembly_flops(P, nelem):
 DF_MUL, DF_MAC, DF_ADD = 4, 12, 8
 
 
-def df_assembly_ops(P, nelem):
+def df_assembly_ops(P, nelem, sym=(0.0, 0.0, 0.0)):
     """FP32 operations (each FFMA, FADD or FMUL one operation) of the
     double-float heat increment assembly per launch, counted from the kernel's
     stages for the work each element needs (the brick halo's repeated columns
     are not counted): the z interpolation of one DOF column per element layer,
     the y interpolation and the y/z test contraction of one (element row, DOF
-    column) pair, the x stage of one element, and the DOF-plane accumulation."""
+    column) pair, the x stage of one element, and the DOF-plane accumulation.
+    At p = 2, sym = the fractions of the x stage, element rows and layers
+    that run the even-odd form (centro-symmetric elements), whose sums cost
+    less: an interpolation pair 52-68 operations where the direct sums take 84."""
     q = P + 1
     z = q * (2 * DF_MUL + 2 * P * DF_MAC)
     y = q * q * (3 * DF_MUL + 3 * P * DF_MAC)
@@ -223,8 +226,45 @@ def df_assembly_ops(P, nelem):
     contraction = 3 * (P + 1) * DF_MUL + (q - 1) * 3 * (P + 1) * DF_MAC
     x = q * q * (2 * DF_MUL + q * per_kx + contraction + 3 * P * DF_ADD)
     yz_kz = (P + 1) * (2 * DF_MUL + DF_MAC) + (q - 1) * (P + 1) * 3 * DF_MAC + (P + 1) ** 2 * 2 * DF_MAC
+    yz = q * yz_kz
     acc = (P + 1) ** 2 * DF_ADD
-    return (z + y + x + q * yz_kz + acc) * nelem
+    if P == 2:
+        fx, fy, fz = sym
+        # even-odd sums: s and d of the inputs (2 sums), per output pair a
+        # product and a multiply-add plus a product, the pair's 2 sums, the
+        # middle output a product and a multiply-add (N) or a product (dN)
+        eo_n = 2 * DF_ADD + (DF_MUL + DF_MAC) + DF_MUL + 2 * DF_ADD + (DF_MUL + DF_MAC)   # 68
+        eo_d = 2 * DF_ADD + (DF_MUL + DF_MAC) + DF_MUL + 2 * DF_ADD + DF_MUL               # 56
+        eo_nd = eo_n + eo_d - 2 * DF_ADD                                                   # 108: s, d shared
+        z_eo = eo_nd
+        y_eo = q * (eo_nd + eo_n)
+        x_eo = q * q * (2 * DF_MUL + q * 2 * DF_MUL + 15 + (eo_d + 3 * DF_MUL + eo_d)
+                        + 2 * (eo_n + 3 * DF_MUL + eo_n) + 3 * P * DF_ADD)
+        yz_eo = q * ((eo_n + eo_d + 3 * DF_ADD + eo_n) + (P + 1) ** 2 * 2 * DF_MAC)
+        z = fz * z_eo + (1 - fz) * z
+        y = fy * y_eo + (1 - fy) * y
+        x = fx * x_eo + (1 - fx) * x
+        yz = fy * yz_eo + (1 - fy) * yz
+    return (z + y + x + yz + acc) * nelem
+
+
+def even_odd_fractions(A, E, p):
+    """Fractions of the x stage (bricks of 32 - p elements, all of them
+    centro-symmetric), of element rows and of layers that the double-float
+    assembly runs in even-odd form at p = 2 (the library's criterion,
+    4e-15 of a table's largest entry)."""
+    import numpy as np
+    if p != 2:
+        return (0.0, 0.0, 0.0)
+    NN = A.axis_setup(E + p - 1, p)["NN"].reshape(E, 3, 3, 2)
+    N, D = NN[..., 0], NN[..., 1]
+    en = np.abs(N - N[:, ::-1, ::-1]).max(axis=(1, 2))
+    ed = np.abs(D + D[:, ::-1, ::-1]).max(axis=(1, 2))
+    sym = (en <= 4e-15 * np.abs(N).max(axis=(1, 2))) & (ed <= 4e-15 * np.abs(D).max(axis=(1, 2)))
+    tx = 32 - p
+    fx = sum(min(tx, E - x0) for x0 in range(0, E, tx) if sym[x0:x0 + tx].all()) / E
+    f = float(sym.mean())
+    return (fx, f, f)
 
 
 def run_reference(args, world, rank):
@@ -790,12 +830,14 @@ def run_ours(args, world, rank, local):
         if kname == "assemble_df":
             # FP32 operations of the double-float algorithm against the FP32
             # pipe's instruction rate (half the FMA flop rate)
-            ops = df_assembly_ops(p, nelem)
+            eo = even_odd_fractions(A, E, p)
+            ops = df_assembly_ops(p, nelem, eo)
             achieved = ops / avg / 1e12
             peak = fp32_peak / 2
             return {"kernel": kname, "bound": "fp32-pipe", "achieved": achieved, "peak": peak, "unit": "Top/s",
                     "frac": achieved / peak, "peak_source": peak_src + "; peak = FP32 instruction rate = flop rate / 2",
                     "traffic": traffic, "algorithmic_fp32_ops_per_launch": ops,
+                    "even_odd_fractions_x_rows_layers": eo,
                     "fp64_equivalent_tflops": algorithmic_assembly_flops(p, nelem) / avg / 1e12,
                     "fp64_pipe_peak_tflops": fp64_peak, "avg_launch_ms": avg * 1e3}
         if kname.startswith("assemble"):
