@@ -405,11 +405,15 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
 #pragma unroll
               for (int kx = 0; kx < 3; ++kx) {
                 const long long qidx = ((long long)(x0 + lane) * Q + kx) + QXt * (qyg + QYt * qzg);
-                const dfl s = df_mul(jwx[kx], jwyz);
-                sx[kx] = s.x;
-                if constexpr (HAS_K) cw[kx] = df_mul(df_mul(ndt, elem_ok ? df_split(a.kqp[qidx], 0) : df_zero()), s);
-                else cw[kx] = df_mul(jwx[kx], cyz);
-                if constexpr (HAS_F) g0[kx] = df_mul(df_mul(s, dtv), elem_ok ? df_split(a.fqp[qidx], uexp) : df_zero());
+                if constexpr (HAS_K || HAS_F) {
+                  const dfl s = df_mul(jwx[kx], jwyz);
+                  sx[kx] = s.x;
+                  if constexpr (HAS_K) cw[kx] = df_mul(df_mul(ndt, elem_ok ? df_split(a.kqp[qidx], 0) : df_zero()), s);
+                  if constexpr (HAS_F) g0[kx] = df_mul(df_mul(s, dtv), elem_ok ? df_split(a.fqp[qidx], uexp) : df_zero());
+                } else {
+                  sx[kx] = jwx[kx].x * jwyz.x;  // the l2norm's weight: high parts suffice
+                }
+                if constexpr (!HAS_K) cw[kx] = df_mul(jwx[kx], cyz);
               }
               dfl yv0[3];
               yrow(Y0, yv0);

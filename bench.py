@@ -238,7 +238,7 @@ def df_assembly_ops(P, nelem, sym=(0.0, 0.0, 0.0)):
         eo_nd = eo_n + eo_d - 2 * DF_ADD                                                   # 108: s, d shared
         z_eo = eo_nd
         y_eo = q * (eo_nd + eo_n)
-        x_eo = q * q * (2 * DF_MUL + q * 2 * DF_MUL + 15 + (eo_d + 3 * DF_MUL + eo_d)
+        x_eo = q * q * (2 * DF_MUL + q * (DF_MUL + 1) + 15 + (eo_d + 3 * DF_MUL + eo_d)
                         + 2 * (eo_n + 3 * DF_MUL + eo_n) + 3 * P * DF_ADD)
         yz_eo = q * ((eo_n + eo_d + 3 * DF_ADD + eo_n) + (P + 1) ** 2 * 2 * DF_MAC)
         z = fz * z_eo + (1 - fz) * z
