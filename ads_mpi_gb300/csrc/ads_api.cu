@@ -281,41 +281,46 @@ int upload(ads_handle* h, T** d, const std::vector<T>& v) {
   return ADS_OK;
 }
 
-// p = 2, three Gauss points: the even-odd coefficients of each element's
-// value and derivative tables (DfTab::sym) and whether they may stand for the
-// tables.  An element qualifies when N[k][b] = N[2-k][2-b] and
-// dN[k][b] = -dN[2-k][2-b] hold to 4e-15 of the table's largest entry (about
+// p = 2 and 3 (p + 1 Gauss points): the even-odd coefficients of each
+// element's value and derivative tables (DfTab::sym) and whether they may
+// stand for the tables.  An element qualifies when N[k][b] = N[p-k][p-b] and
+// dN[k][b] = -dN[p-k][p-b] hold to 4e-15 of the table's largest entry (about
 // the double-float tables' own precision): the elements of a knot vector that
-// is uniform in FP64, except the first and the last, whose basis the open
-// knot vector's end knots bend.
+// is uniform in FP64, except the first and last p - 1, whose basis the open
+// knot vector's repeated end knots bend.
 void even_odd_tables(const AxisHost& a, std::vector<double>& sc, std::vector<unsigned char>& sf) {
-  const int E = a.E;
-  sc.assign((size_t)E * DF_SYM, 0.0);
+  const int E = a.E, p = a.p, q = p + 1, ns = df_sym_count(p);
+  sc.assign((size_t)E * ns, 0.0);
   sf.assign((size_t)E, 0);
   for (int e = 0; e < E; ++e) {
-    auto N = [&](int k, int b, int d) { return a.NN[(((size_t)e * 3 + k) * 3 + b) * 2 + d]; };
-    double mn = 0.0, md = 0.0;
-    for (int k = 0; k < 3; ++k)
-      for (int b = 0; b < 3; ++b) {
+    auto N = [&](int k, int b, int d) { return a.NN[(((size_t)e * q + k) * (p + 1) + b) * 2 + d]; };
+    double mn = 0.0, md = 0.0, en = 0.0, ed = 0.0;  // largest entries, largest departures from the symmetry
+    for (int k = 0; k < q; ++k)
+      for (int b = 0; b <= p; ++b) {
         mn = std::max(mn, std::fabs(N(k, b, 0)));
         md = std::max(md, std::fabs(N(k, b, 1)));
+        en = std::max(en, std::fabs(N(k, b, 0) - N(p - k, p - b, 0)));
+        ed = std::max(ed, std::fabs(N(k, b, 1) + N(p - k, p - b, 1)));
       }
-    double en = 0.0, ed = 0.0;  // largest departure from the symmetry
-    for (int k = 0; k < 3; ++k)
-      for (int b = 0; b < 3; ++b) {
-        en = std::max(en, std::fabs(N(k, b, 0) - N(2 - k, 2 - b, 0)));
-        ed = std::max(ed, std::fabs(N(k, b, 1) + N(2 - k, 2 - b, 1)));
-      }
-    double* c = &sc[(size_t)e * DF_SYM];
-    c[0] = 0.5 * (N(0, 0, 0) + N(0, 2, 0));
-    c[1] = 0.5 * (N(0, 0, 0) - N(0, 2, 0));
-    c[2] = N(0, 1, 0);
-    c[3] = N(1, 0, 0);
-    c[4] = N(1, 1, 0);
-    c[5] = 0.5 * (N(0, 0, 1) + N(0, 2, 1));
-    c[6] = 0.5 * (N(0, 0, 1) - N(0, 2, 1));
-    c[7] = N(0, 1, 1);
-    c[8] = N(1, 0, 1);
+    double* c = &sc[(size_t)e * ns];
+    if (p == 2) {
+      c[0] = 0.5 * (N(0, 0, 0) + N(0, 2, 0));
+      c[1] = 0.5 * (N(0, 0, 0) - N(0, 2, 0));
+      c[2] = N(0, 1, 0);
+      c[3] = N(1, 0, 0);
+      c[4] = N(1, 1, 0);
+      c[5] = 0.5 * (N(0, 0, 1) + N(0, 2, 1));
+      c[6] = 0.5 * (N(0, 0, 1) - N(0, 2, 1));
+      c[7] = N(0, 1, 1);
+      c[8] = N(1, 0, 1);
+    } else {
+      for (int d = 0; d < 2; ++d)
+        for (int k = 0; k < 2; ++k)
+          for (int j = 0; j < 2; ++j) {
+            c[8 * d + 2 * k + j] = 0.5 * (N(k, j, d) + N(k, 3 - j, d));
+            c[8 * d + 4 + 2 * k + j] = 0.5 * (N(k, j, d) - N(k, 3 - j, d));
+          }
+    }
     sf[e] = (en <= 4e-15 * mn && ed <= 4e-15 * md) ? 1 : 0;
   }
 }
@@ -918,7 +923,7 @@ int create_impl(ads_handle* h) {
     if (h->opts.precision == ADS_PREC_MIXED) {
       if ((st = upload(h, &h->d_nndf[d], split(a.NN)))) return st;
       if ((st = upload(h, &h->d_jwdf[d], split(a.JW)))) return st;
-      if (a.p == 2) {
+      if (df_sym_count(a.p) > 0) {
         std::vector<double> sc;
         std::vector<unsigned char> sf;
         even_odd_tables(a, sc, sf);

@@ -50,14 +50,16 @@ struct AxisTab {
 struct DfTab {
   const float2* nn;  // [E][Q][P+1][2]
   const float2* jw;  // [E][Q]
-  // p = 2: per element, the even-odd coefficients of its centro-symmetric
-  // tables (N[k][b] = N[2-k][2-b], dN[k][b] = -dN[2-k][2-b]):
-  //   [(N00+N02)/2, (N00-N02)/2, N01, N10, N11, (dN00+dN02)/2, (dN00-dN02)/2, dN01, dN10]
+  // p = 2 and 3: per element, the even-odd coefficients of its
+  // centro-symmetric tables (N[k][b] = N[p-k][p-b], dN[k][b] = -dN[p-k][p-b]),
+  //   p = 2: [(N00+N02)/2, (N00-N02)/2, N01, N10, N11, (dN00+dN02)/2, (dN00-dN02)/2, dN01, dN10]
+  //   p = 3: a[k][j] = (N[k][j] + N[k][3-j])/2, c[k][j] = (N[k][j] - N[k][3-j])/2 (k, j < 2),
+  //          then the same for dN: [a00 a01 a10 a11 c00 c01 c10 c11 a' c']
   // and symf[e] = 1 where the element's tables are symmetric (null: none are)
-  const float2* sym;           // [E][DF_SYM]
+  const float2* sym;           // [E][df_sym_count(p)]
   const unsigned char* symf;   // [E]
 };
-constexpr int DF_SYM = 9;
+constexpr int df_sym_count(int p) { return p == 2 ? 9 : (p == 3 ? 16 : 0); }
 struct DfTabs3 {
   DfTab x, y, z;
 };

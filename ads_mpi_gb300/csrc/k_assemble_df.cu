@@ -32,6 +32,191 @@
 
 namespace ads {
 
+// ---- even-odd forms of an element's contractions (p = 2 and 3) ----
+// For an element whose tables are centro-symmetric, N[k][b] = N[p-k][p-b]
+// and dN[k][b] = -dN[p-k][p-b] (Gauss points symmetric about the element's
+// centre, basis mirrored: every element of a uniform knot vector but the
+// first and last p - 1), the sums over b of an interpolation pair the outputs
+// k and p-k.  With s_j = v_j + v_{p-j} and d_j = v_j - v_{p-j},
+//   sum_b N[k][b] v[b]:  out_k, out_{p-k} = X_k +- Y_k, X_k = sum_j a_kj s_j, Y_k = sum_j c_kj d_j
+//   sum_b dN[k][b] v[b]: out_k, out_{p-k} = X_k +- Y_k, X_k = sum_j c'_kj d_j, Y_k = sum_j a'_kj s_j
+// with a_kj, c_kj = (N[k][j] +- N[k][p-j]) / 2 (a', c' the same for dN) and,
+// at p = 2, the middle output and middle input folded in; the test
+// contractions (sums over k) are the transposes.  A double-float
+// multiply-add costs 12 FP32 operations and a sum 8: at p = 2 the forms take
+// 52-68 operations for the direct sums' 84, at p = 3 96 for 160.
+template <int P>
+struct EO {
+  static constexpr bool on = false;
+  static constexpr int NS = 1;
+};
+
+__device__ __forceinline__ dfl df_sub(dfl a, dfl b) { return df_add(a, df_neg(b)); }
+
+template <>
+struct EO<2> {
+  static constexpr bool on = true;
+  static constexpr int NS = 9;  // [a, c, N01, N10, N11, a', c', dN01, dN10]
+  struct N { dfl a, c, n01, n10, n11; };
+  struct D { dfl a, c, d01, d10; };
+  static __device__ __forceinline__ N n(const dfl* t) { return N{t[0], t[1], t[2], t[3], t[4]}; }
+  static __device__ __forceinline__ D d(const dfl* t) { return D{t[5], t[6], t[7], t[8]}; }
+  // out[k] = sum_b N[k][b] v[b]
+  static __device__ __forceinline__ void interp_n(dfl (&out)[3], const dfl (&v)[3], const N& n) {
+    const dfl sp = df_add(v[0], v[2]), dm = df_sub(v[0], v[2]);
+    const dfl e = df_mac(df_mul(n.a, sp), n.n01, v[1]), d = df_mul(n.c, dm);
+    out[0] = df_add(e, d);
+    out[2] = df_sub(e, d);
+    out[1] = df_mac(df_mul(n.n10, sp), n.n11, v[1]);
+  }
+  // out[k] = sum_b dN[k][b] v[b]
+  static __device__ __forceinline__ void interp_d(dfl (&out)[3], const dfl (&v)[3], const D& dn) {
+    const dfl sp = df_add(v[0], v[2]), dm = df_sub(v[0], v[2]);
+    const dfl e = df_mac(df_mul(dn.a, sp), dn.d01, v[1]), d = df_mul(dn.c, dm);
+    out[0] = df_add(d, e);
+    out[2] = df_sub(d, e);
+    out[1] = df_mul(dn.d10, dm);
+  }
+  // both, sharing s and d
+  static __device__ __forceinline__ void interp_nd(dfl (&on)[3], dfl (&od)[3], const dfl (&v)[3], const N& n,
+                                                   const D& dn) {
+    const dfl sp = df_add(v[0], v[2]), dm = df_sub(v[0], v[2]);
+    const dfl e = df_mac(df_mul(n.a, sp), n.n01, v[1]), d = df_mul(n.c, dm);
+    on[0] = df_add(e, d);
+    on[2] = df_sub(e, d);
+    on[1] = df_mac(df_mul(n.n10, sp), n.n11, v[1]);
+    const dfl e2 = df_mac(df_mul(dn.a, sp), dn.d01, v[1]), d2 = df_mul(dn.c, dm);
+    od[0] = df_add(d2, e2);
+    od[2] = df_sub(d2, e2);
+    od[1] = df_mul(dn.d10, dm);
+  }
+  // h[b] = sum_k N[k][b] g[k]
+  static __device__ __forceinline__ void test_n(dfl (&h)[3], const dfl (&g)[3], const N& n) {
+    const dfl sp = df_add(g[0], g[2]), dm = df_sub(g[0], g[2]);
+    const dfl e = df_mac(df_mul(n.a, sp), n.n10, g[1]), d = df_mul(n.c, dm);
+    h[0] = df_add(e, d);
+    h[2] = df_sub(e, d);
+    h[1] = df_mac(df_mul(n.n01, sp), n.n11, g[1]);
+  }
+  // h[b] = sum_k dN[k][b] g[k]
+  static __device__ __forceinline__ void test_d(dfl (&h)[3], const dfl (&g)[3], const D& dn) {
+    const dfl sp = df_add(g[0], g[2]), dm = df_sub(g[0], g[2]);
+    const dfl e = df_mac(df_mul(dn.c, sp), dn.d10, g[1]), d = df_mul(dn.a, dm);
+    h[0] = df_add(e, d);
+    h[2] = df_sub(d, e);
+    h[1] = df_mul(dn.d01, dm);
+  }
+  // interp_n on the high parts, in FP32 (the l2norm's u at the points)
+  static __device__ __forceinline__ void uu(float (&u)[3], const dfl (&v)[3], const N& n) {
+    const float sp = v[0].x + v[2].x, dm = v[0].x - v[2].x;
+    const float e = fmaf(n.n01.x, v[1].x, n.a.x * sp), d = n.c.x * dm;
+    u[0] = e + d;
+    u[2] = e - d;
+    u[1] = fmaf(n.n11.x, v[1].x, n.n10.x * sp);
+  }
+};
+
+template <>
+struct EO<3> {
+  static constexpr bool on = true;
+  static constexpr int NS = 16;  // N: a[k][j] (4), c[k][j] (4); then dN: a', c'
+  struct C { dfl a[2][2], c[2][2]; };
+  using N = C;
+  using D = C;
+  static __device__ __forceinline__ C load(const dfl* t) {
+    C r;
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        r.a[k][j] = t[2 * k + j];
+        r.c[k][j] = t[4 + 2 * k + j];
+      }
+    return r;
+  }
+  static __device__ __forceinline__ C n(const dfl* t) { return load(t); }
+  static __device__ __forceinline__ C d(const dfl* t) { return load(t + 8); }
+  static __device__ __forceinline__ dfl dot2(dfl c0, dfl x0, dfl c1, dfl x1) { return df_mac(df_mul(c0, x0), c1, x1); }
+  static __device__ __forceinline__ void sd(dfl (&s)[2], dfl (&d)[2], const dfl (&v)[4]) {
+    s[0] = df_add(v[0], v[3]);
+    d[0] = df_sub(v[0], v[3]);
+    s[1] = df_add(v[1], v[2]);
+    d[1] = df_sub(v[1], v[2]);
+  }
+  static __device__ __forceinline__ void pairs(dfl (&out)[4], const dfl (&X)[2], const dfl (&Y)[2]) {
+    out[0] = df_add(X[0], Y[0]);
+    out[3] = df_sub(X[0], Y[0]);
+    out[1] = df_add(X[1], Y[1]);
+    out[2] = df_sub(X[1], Y[1]);
+  }
+  static __device__ __forceinline__ void interp_n_sd(dfl (&out)[4], const dfl (&s)[2], const dfl (&d)[2], const C& n) {
+    dfl X[2], Y[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      X[k] = dot2(n.a[k][0], s[0], n.a[k][1], s[1]);
+      Y[k] = dot2(n.c[k][0], d[0], n.c[k][1], d[1]);
+    }
+    pairs(out, X, Y);
+  }
+  static __device__ __forceinline__ void interp_d_sd(dfl (&out)[4], const dfl (&s)[2], const dfl (&d)[2], const C& dn) {
+    dfl X[2], Y[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      X[k] = dot2(dn.c[k][0], d[0], dn.c[k][1], d[1]);
+      Y[k] = dot2(dn.a[k][0], s[0], dn.a[k][1], s[1]);
+    }
+    pairs(out, X, Y);
+  }
+  static __device__ __forceinline__ void interp_n(dfl (&out)[4], const dfl (&v)[4], const C& n) {
+    dfl s[2], d[2];
+    sd(s, d, v);
+    interp_n_sd(out, s, d, n);
+  }
+  static __device__ __forceinline__ void interp_d(dfl (&out)[4], const dfl (&v)[4], const C& dn) {
+    dfl s[2], d[2];
+    sd(s, d, v);
+    interp_d_sd(out, s, d, dn);
+  }
+  static __device__ __forceinline__ void interp_nd(dfl (&on)[4], dfl (&od)[4], const dfl (&v)[4], const C& n,
+                                                   const C& dn) {
+    dfl s[2], d[2];
+    sd(s, d, v);
+    interp_n_sd(on, s, d, n);
+    interp_d_sd(od, s, d, dn);
+  }
+  // h[b] = sum_k N[k][b] g[k]: X_b = sum_k a_kb S_k, Y_b = sum_k c_kb D_k
+  static __device__ __forceinline__ void test_n(dfl (&h)[4], const dfl (&g)[4], const C& n) {
+    dfl S[2], D[2], X[2], Y[2];
+    sd(S, D, g);
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      X[b] = dot2(n.a[0][b], S[0], n.a[1][b], S[1]);
+      Y[b] = dot2(n.c[0][b], D[0], n.c[1][b], D[1]);
+    }
+    pairs(h, X, Y);
+  }
+  // h[b] = sum_k dN[k][b] g[k]: X_b = sum_k a'_kb D_k, Y_b = sum_k c'_kb S_k
+  static __device__ __forceinline__ void test_d(dfl (&h)[4], const dfl (&g)[4], const C& dn) {
+    dfl S[2], D[2], X[2], Y[2];
+    sd(S, D, g);
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      X[b] = dot2(dn.a[0][b], D[0], dn.a[1][b], D[1]);
+      Y[b] = dot2(dn.c[0][b], S[0], dn.c[1][b], S[1]);
+    }
+    pairs(h, X, Y);
+  }
+  static __device__ __forceinline__ void uu(float (&u)[4], const dfl (&v)[4], const C& n) {
+    const float s0 = v[0].x + v[3].x, d0 = v[0].x - v[3].x, s1 = v[1].x + v[2].x, d1 = v[1].x - v[2].x;
+    const float X0 = fmaf(n.a[0][1].x, s1, n.a[0][0].x * s0), Y0 = fmaf(n.c[0][1].x, d1, n.c[0][0].x * d0);
+    const float X1 = fmaf(n.a[1][1].x, s1, n.a[1][0].x * s0), Y1 = fmaf(n.c[1][1].x, d1, n.c[1][0].x * d0);
+    u[0] = X0 + Y0;
+    u[3] = X0 - Y0;
+    u[1] = X1 + Y1;
+    u[2] = X1 - Y1;
+  }
+};
+
 template <int P>
 struct DfLayout {
   static constexpr int Q = P + 1;
@@ -55,9 +240,10 @@ struct DfLayout {
   static constexpr size_t o_jwy = o_ny + D * TY * NT;           // dfl [TY][Q]
   static constexpr size_t o_nz = o_jwy + D * TY * Q;            // dfl [NT]
   static constexpr size_t o_jwz = o_nz + D * NT;                // dfl [Q]
-  static constexpr size_t o_sy = o_jwz + D * Q;                 // dfl [TY][DF_SYM] (p = 2)
-  static constexpr size_t o_sz = o_sy + D * TY * DF_SYM;        // dfl [DF_SYM]
-  static constexpr size_t o_sf = o_sz + D * DF_SYM;             // int [TY + 1]: rows, then the layer
+  static constexpr int NS = EO<P>::NS;                         // even-odd coefficients per element
+  static constexpr size_t o_sy = o_jwz + D * Q;                 // dfl [TY][NS]
+  static constexpr size_t o_sz = o_sy + D * TY * NS;            // dfl [NS]
+  static constexpr size_t o_sf = o_sz + D * NS;                 // int [TY + 1]: rows, then the layer
   static constexpr size_t o_red = (o_sf + 4 * (TY + 1) + 15) / 16 * 16;
   static constexpr size_t bytes = o_red + 3 * sizeof(double) * (AS_THREADS / 32);
 };
@@ -68,76 +254,13 @@ __device__ __forceinline__ dfl df_split(double d, int sexp) {
   return df_make(h, l);
 }
 
-// ---- even-odd forms of an element's 3 x 3 contractions (p = 2) ----
-// For an element whose tables are centro-symmetric, N[k][b] = N[2-k][2-b]
-// and dN[k][b] = -dN[2-k][2-b] (Gauss points symmetric about the element's
-// centre, basis mirrored: every element of a uniform knot vector but the
-// first and the last), the sums over b of an interpolation pair the outputs k
-// and 2-k: with s = v0 + v2 and d = v0 - v2,
-//   sum_b N[k][b] v[b]:  out0,2 = (a s + N01 v1) +- c d,  out1 = N10 s + N11 v1
-//   sum_b dN[k][b] v[b]: out0,2 = a' s + dN01 v1 ... (signs below), out1 = dN10 d
-// with a = (N00 + N02)/2, c = (N00 - N02)/2 (a', c' the same for dN); the
-// test contractions (sums over k) are the transposes.  A double-float
-// multiply-add costs 12 FP32 operations and a sum 8, so the forms below take
-// 52-68 operations for what the direct sums do in 84.
-struct SymN { dfl a, c, n01, n10, n11; };
-struct SymD { dfl a, c, d01, d10; };
-
-__device__ __forceinline__ dfl df_sub(dfl a, dfl b) { return df_add(a, df_neg(b)); }
-
-// out[k] = sum_b N[k][b] v[b]
-__device__ __forceinline__ void eo_interp_n(dfl (&out)[3], const dfl (&v)[3], const SymN& n) {
-  const dfl sp = df_add(v[0], v[2]), dm = df_sub(v[0], v[2]);
-  const dfl e = df_mac(df_mul(n.a, sp), n.n01, v[1]), d = df_mul(n.c, dm);
-  out[0] = df_add(e, d);
-  out[2] = df_sub(e, d);
-  out[1] = df_mac(df_mul(n.n10, sp), n.n11, v[1]);
-}
-// on[k] = sum_b N[k][b] v[b], od[k] = sum_b dN[k][b] v[b] (s and d shared)
-__device__ __forceinline__ void eo_interp_nd(dfl (&on)[3], dfl (&od)[3], const dfl (&v)[3], const SymN& n,
-                                             const SymD& dn) {
-  const dfl sp = df_add(v[0], v[2]), dm = df_sub(v[0], v[2]);
-  const dfl e = df_mac(df_mul(n.a, sp), n.n01, v[1]), d = df_mul(n.c, dm);
-  on[0] = df_add(e, d);
-  on[2] = df_sub(e, d);
-  on[1] = df_mac(df_mul(n.n10, sp), n.n11, v[1]);
-  const dfl e2 = df_mac(df_mul(dn.a, sp), dn.d01, v[1]), d2 = df_mul(dn.c, dm);
-  od[0] = df_add(d2, e2);
-  od[2] = df_sub(d2, e2);
-  od[1] = df_mul(dn.d10, dm);
-}
-// out[k] = sum_b dN[k][b] v[b]
-__device__ __forceinline__ void eo_interp_d(dfl (&out)[3], const dfl (&v)[3], const SymD& dn) {
-  const dfl sp = df_add(v[0], v[2]), dm = df_sub(v[0], v[2]);
-  const dfl e = df_mac(df_mul(dn.a, sp), dn.d01, v[1]), d = df_mul(dn.c, dm);
-  out[0] = df_add(d, e);
-  out[2] = df_sub(d, e);
-  out[1] = df_mul(dn.d10, dm);
-}
-// h[b] = sum_k N[k][b] g[k]
-__device__ __forceinline__ void eo_test_n(dfl (&h)[3], const dfl (&g)[3], const SymN& n) {
-  const dfl sp = df_add(g[0], g[2]), dm = df_sub(g[0], g[2]);
-  const dfl e = df_mac(df_mul(n.a, sp), n.n10, g[1]), d = df_mul(n.c, dm);
-  h[0] = df_add(e, d);
-  h[2] = df_sub(e, d);
-  h[1] = df_mac(df_mul(n.n01, sp), n.n11, g[1]);
-}
-// h[b] = sum_k dN[k][b] g[k]
-__device__ __forceinline__ void eo_test_d(dfl (&h)[3], const dfl (&g)[3], const SymD& dn) {
-  const dfl sp = df_add(g[0], g[2]), dm = df_sub(g[0], g[2]);
-  const dfl e = df_mac(df_mul(dn.c, sp), dn.d10, g[1]), d = df_mul(dn.a, dm);
-  h[0] = df_add(e, d);
-  h[2] = df_sub(d, e);
-  h[1] = df_mul(dn.d01, dm);
-}
-__device__ __forceinline__ SymN sym_n(const dfl* t) { return SymN{t[0], t[1], t[2], t[3], t[4]}; }
-__device__ __forceinline__ SymD sym_d(const dfl* t) { return SymD{t[5], t[6], t[7], t[8]}; }
-
 template <int P, bool HAS_F, bool HAS_K>
 __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
     k_assemble_df(const AssembleArgs a, const DfTabs3 tb) {
   using L = DfLayout<P>;
+  using E = EO<P>;
   constexpr int Q = L::Q, TX = L::TX, TY = L::TY, CX = L::CX;
+  constexpr int NS = L::NS;
   constexpr int NCOL = L::NCOL, QY = L::QY, RC = L::RC, RF = L::RF, NT = L::NT;
 
   extern __shared__ __align__(16) unsigned char smem[];
@@ -190,14 +313,14 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
     __syncthreads();  // previous item fully done with shared memory
 
     // per-lane x tables (element x0 + lane; lanes >= TX have no element).
-    // p = 2 bricks whose elements are all centro-symmetric run the x stage in
-    // even-odd form; the table registers then hold the lane's DF_SYM
+    // p = 2, 3: bricks whose elements are all centro-symmetric run the x
+    // stage in even-odd form; the table registers then hold the lane's NS
     // even-odd coefficients
     dfl nx[Q][P + 1][2];
     dfl jwx[Q];
     const bool lane_elem = (lane < TX) && (x0 + lane < Ex);
     bool symx = false;
-    if constexpr (P == 2) {
+    if constexpr (E::on) {
       if (tb.x.sym != nullptr) symx = __all_sync(0xffffffffu, !lane_elem || tb.x.symf[x0 + lane] != 0);
     }
     {
@@ -208,7 +331,7 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
         dfl* t = &nx[0][0][0];
 #pragma unroll
         for (int i = 0; i < Q * (P + 1) * 2; ++i)
-          t[i] = (i < DF_SYM && lane_elem) ? tb.x.sym[(size_t)ex * DF_SYM + i] : df_zero();
+          t[i] = (i < NS && lane_elem) ? tb.x.sym[(size_t)ex * NS + i] : df_zero();
       } else {
 #pragma unroll
         for (int k = 0; k < Q; ++k) {
@@ -224,13 +347,13 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
       const int ey = y0 + i / NT;
       NYs[i] = (ey < Ey) ? tb.y.nn[(size_t)ey * NT + (i % NT)] : df_zero();
     }
-    if constexpr (P == 2) {
+    if constexpr (E::on) {
       // the element rows' even-odd coefficients and flags (the y stage of a
       // row, one warp, takes the even-odd form where its element qualifies)
       const bool ys = tb.y.sym != nullptr;
-      for (int i = tid; i < TY * DF_SYM; i += AS_THREADS) {
-        const int ey = y0 + i / DF_SYM;
-        SYs[i] = (ys && ey < Ey) ? tb.y.sym[(size_t)ey * DF_SYM + (i % DF_SYM)] : df_zero();
+      for (int i = tid; i < TY * NS; i += AS_THREADS) {
+        const int ey = y0 + i / NS;
+        SYs[i] = (ys && ey < Ey) ? tb.y.sym[(size_t)ey * NS + (i % NS)] : df_zero();
       }
       for (int i = tid; i < TY; i += AS_THREADS) SF[i] = (ys && y0 + i < Ey) ? (int)tb.y.symf[y0 + i] : 0;
     }
@@ -253,15 +376,15 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
       cp_async_commit();
       for (int i = tid; i < NT; i += AS_THREADS) NZs[i] = tb.z.nn[(size_t)ez * NT + i];
       for (int i = tid; i < Q; i += AS_THREADS) JWZs[i] = tb.z.jw[(size_t)ez * Q + i];
-      if constexpr (P == 2) {
+      if constexpr (E::on) {
         const bool zs = tb.z.sym != nullptr;
-        for (int i = tid; i < DF_SYM; i += AS_THREADS) SZs[i] = zs ? tb.z.sym[(size_t)ez * DF_SYM + i] : df_zero();
+        for (int i = tid; i < NS; i += AS_THREADS) SZs[i] = zs ? tb.z.sym[(size_t)ez * NS + i] : df_zero();
         if (tid == 0) SF[TY] = zs ? (int)tb.z.symf[ez] : 0;
       }
       cp_async_wait<1>();
       __syncthreads();
-      const bool symz = (P == 2) && SF[TY] != 0;
-      const bool symy = (P == 2) && SF[my_ey] != 0;  // warp-uniform: a warp is one element row
+      const bool symz = E::on && SF[TY] != 0;
+      const bool symy = E::on && SF[my_ey] != 0;  // warp-uniform: a warp is one element row
 
       // split each coefficient plane once, when it arrives
       {
@@ -288,17 +411,17 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
       __syncthreads();
 
       // ---- z interpolation per column: ZA = sum_b Nz C, ZB = sum_b dNz C ----
-      if constexpr (P == 2) {
+      if constexpr (E::on) {
         if (symz) {
-          const SymN sn = sym_n(SZs);
-          const SymD sd = sym_d(SZs);
+          const typename E::N sn = E::n(SZs);
+          const typename E::D sd = E::d(SZs);
           for (int col = tid; col < NCOL; col += AS_THREADS) {
-            dfl c[3], za[3], zb[3];
+            dfl c[P + 1], za[Q], zb[Q];
 #pragma unroll
-            for (int b = 0; b < 3; ++b) c[b] = tring[((ez + b) % RC) * NCOL + col];
-            eo_interp_nd(za, zb, c, sn, sd);
+            for (int b = 0; b <= P; ++b) c[b] = tring[((ez + b) % RC) * NCOL + col];
+            E::interp_nd(za, zb, c, sn, sd);
 #pragma unroll
-            for (int kz = 0; kz < 3; ++kz) {
+            for (int kz = 0; kz < Q; ++kz) {
               ZA[kz * NCOL + col] = za[kz];
               ZB[kz * NCOL + col] = zb[kz];
             }
@@ -341,15 +464,15 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
             za[b] = ZA[kz * NCOL + (my_ey + b) * CX + my_cx];
             zb[b] = ZB[kz * NCOL + (my_ey + b) * CX + my_cx];
           }
-          if constexpr (P == 2) {
+          if constexpr (E::on) {
             if (symy) {
-              const SymN sn = sym_n(SYs + my_ey * DF_SYM);
-              const SymD sd = sym_d(SYs + my_ey * DF_SYM);
-              dfl y0v[3], y1v[3], y2v[3];
-              eo_interp_nd(y0v, y1v, za, sn, sd);
-              eo_interp_n(y2v, zb, sn);
+              const typename E::N sn = E::n(SYs + my_ey * NS);
+              const typename E::D sd = E::d(SYs + my_ey * NS);
+              dfl y0v[Q], y1v[Q], y2v[Q];
+              E::interp_nd(y0v, y1v, za, sn, sd);
+              E::interp_n(y2v, zb, sn);
 #pragma unroll
-              for (int ky = 0; ky < 3; ++ky) {
+              for (int ky = 0; ky < Q; ++ky) {
                 const int qy = my_ey * Q + ky;
                 Y0[qy * CX + my_cx] = y0v[ky];
                 Y1[qy * CX + my_cx] = y1v[ky];
@@ -393,17 +516,17 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
           const long long qyg = (long long)y0 * Q + qy;
           const long long qzg = (long long)ez * Q + kz;
           dfl h0[P + 1], h1[P + 1], h2[P + 1];
-          if constexpr (P == 2) {
+          if constexpr (E::on) {
             if (symx) {
-              const SymN sn = sym_n(&nx[0][0][0]);
-              const SymD sd = sym_d(&nx[0][0][0]);
+              const typename E::N sn = E::n(&nx[0][0][0]);
+              const typename E::D sd = E::d(&nx[0][0][0]);
               // the point weights, then one gradient component at a time:
               // interpolate, weight, contract
-              dfl cw[3];
-              float sx[3];
-              dfl g0[3];
+              dfl cw[Q];
+              float sx[Q];
+              dfl g0[Q];
 #pragma unroll
-              for (int kx = 0; kx < 3; ++kx) {
+              for (int kx = 0; kx < Q; ++kx) {
                 const long long qidx = ((long long)(x0 + lane) * Q + kx) + QXt * (qyg + QYt * qzg);
                 if constexpr (HAS_K || HAS_F) {
                   const dfl s = df_mul(jwx[kx], jwyz);
@@ -415,45 +538,43 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
                 }
                 if constexpr (!HAS_K) cw[kx] = df_mul(jwx[kx], cyz);
               }
-              dfl yv0[3];
+              dfl yv0[P + 1];
               yrow(Y0, yv0);
               {
                 // u at the points from the high parts (the l2norm), the same even-odd form
-                const float sp = yv0[0].x + yv0[2].x, dm = yv0[0].x - yv0[2].x;
-                const float e = fmaf(sn.n01.x, yv0[1].x, sn.a.x * sp), d = sn.c.x * dm;
-                const float u0 = e + d, u2 = e - d, u1 = fmaf(sn.n11.x, yv0[1].x, sn.n10.x * sp);
-                l2_layer = fmaf(sx[0] * u0, u0, l2_layer);
-                l2_layer = fmaf(sx[1] * u1, u1, l2_layer);
-                l2_layer = fmaf(sx[2] * u2, u2, l2_layer);
-              }
-              {
-                dfl du[3];
-                eo_interp_d(du, yv0, sd);
+                float u[Q];
+                E::uu(u, yv0, sn);
 #pragma unroll
-                for (int kx = 0; kx < 3; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
-                eo_test_d(h0, du, sd);
+                for (int kx = 0; kx < Q; ++kx) l2_layer = fmaf(sx[kx] * u[kx], u[kx], l2_layer);
               }
               {
-                dfl du[3], yv1[3];
+                dfl du[Q];
+                E::interp_d(du, yv0, sd);
+#pragma unroll
+                for (int kx = 0; kx < Q; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
+                E::test_d(h0, du, sd);
+              }
+              {
+                dfl du[Q], yv1[P + 1];
                 yrow(Y1, yv1);
-                eo_interp_n(du, yv1, sn);
+                E::interp_n(du, yv1, sn);
 #pragma unroll
-                for (int kx = 0; kx < 3; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
-                eo_test_n(h1, du, sn);
+                for (int kx = 0; kx < Q; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
+                E::test_n(h1, du, sn);
               }
               {
-                dfl du[3], yv2[3];
+                dfl du[Q], yv2[P + 1];
                 yrow(Y2, yv2);
-                eo_interp_n(du, yv2, sn);
+                E::interp_n(du, yv2, sn);
 #pragma unroll
-                for (int kx = 0; kx < 3; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
-                eo_test_n(h2, du, sn);
+                for (int kx = 0; kx < Q; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
+                E::test_n(h2, du, sn);
               }
               if constexpr (HAS_F) {
-                dfl hf[3];
-                eo_test_n(hf, g0, sn);
+                dfl hf[P + 1];
+                E::test_n(hf, g0, sn);
 #pragma unroll
-                for (int b = 0; b < 3; ++b) h0[b] = df_add(h0[b], hf[b]);
+                for (int b = 0; b <= P; ++b) h0[b] = df_add(h0[b], hf[b]);
               }
             }
           }
@@ -517,23 +638,23 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
         // ---- y test contraction of this thread's element row, then z ----
         {
           dfl i0[P + 1], i1[P + 1];
-          if constexpr (P == 2) {
+          if constexpr (E::on) {
             if (symy) {
-              const SymN sn = sym_n(SYs + my_ey * DF_SYM);
-              const SymD sd = sym_d(SYs + my_ey * DF_SYM);
-              dfl hv0[3], hv1[3], hv2[3], ta[3], tb1[3];
+              const typename E::N sn = E::n(SYs + my_ey * NS);
+              const typename E::D sd = E::d(SYs + my_ey * NS);
+              dfl hv0[Q], hv1[Q], hv2[Q], ta[P + 1], tb1[P + 1];
 #pragma unroll
-              for (int ky = 0; ky < 3; ++ky) {
+              for (int ky = 0; ky < Q; ++ky) {
                 const int qy = my_ey * Q + ky;
                 hv0[ky] = H0[qy * CX + my_cx];
                 hv1[ky] = H1[qy * CX + my_cx];
                 hv2[ky] = H2[qy * CX + my_cx];
               }
-              eo_test_n(ta, hv0, sn);
-              eo_test_d(tb1, hv1, sd);
+              E::test_n(ta, hv0, sn);
+              E::test_d(tb1, hv1, sd);
 #pragma unroll
-              for (int by = 0; by < 3; ++by) i0[by] = df_add(ta[by], tb1[by]);
-              eo_test_n(i1, hv2, sn);
+              for (int by = 0; by <= P; ++by) i0[by] = df_add(ta[by], tb1[by]);
+              E::test_n(i1, hv2, sn);
             }
           }
           if (!symy) {
