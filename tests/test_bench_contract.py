@@ -32,3 +32,21 @@ def test_reference_arm_prints_the_contract_line():
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
     # the DOFs of one step of the sample: (16 + 2)^3 at p = 2
     assert d["config"]["dofs_per_step"] == 18 ** 3
+
+
+def test_double_float_operation_model():
+    """The roofline's operation count of the double-float assembly: the
+    direct sums at p = 2 (8,187 FP32 operations per element), fewer with the
+    even-odd form, and the fractions of the work in that form at 256^3 (every
+    x brick but the two holding an end element, every row and layer but the
+    two end ones) and at 96^3 (FP32-rounded knots: no whole brick)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from ads_mpi_gb300 import ads as A
+    assert bench.df_assembly_ops(2, 1) == 8187
+    assert bench.df_assembly_ops(2, 1, (1.0, 1.0, 1.0)) < 0.81 * 8187
+    fx, fy, fz = bench.even_odd_fractions(A, 256, 2)
+    assert fx == (256 - 30 - 16) / 256 and fy == fz == 254 / 256
+    fx96, fy96, _ = bench.even_odd_fractions(A, 96, 2)
+    assert fx96 == 0.0 and 0.0 < fy96 < 1.0
+    assert bench.even_odd_fractions(A, 256, 3) == (0.0, 0.0, 0.0)
