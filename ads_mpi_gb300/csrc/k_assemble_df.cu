@@ -23,10 +23,15 @@
 //   integrand       g{1,2,3} = -dt kappa J W du/d{x,y,z},  g0 = dt J W f
 //   test functions  g --x--> H0,H1,H2 --y--> I0,I1 --z--> G (double-float planes)
 //
-// The coefficients are scaled by 2^-e (max |u| < 2^e, from the uscale pass)
-// so that FP32 never overflows, split once per plane into (high, low) floats,
-// and the finished DOF planes are scaled back by 2^e exactly.  The l2norm
-// (J W u^2) is accumulated from the high parts in compensated FP32.
+// The coefficients are scaled by 2^-e (max |u| < 2^e, from the uscale pass,
+// or the previous step's scale checked afterwards when a caller's array is
+// read in place) so that FP32 never overflows, split once per plane into
+// (high, low) floats, and the finished DOF planes are scaled back by 2^e
+// exactly.  The l2norm (J W u^2) is accumulated from the high parts in
+// compensated FP32.  At p = 2 and 3, elements whose tables are
+// centro-symmetric take the even-odd form of the sums (EO below): per layer
+// for the z interpolation, per element row for the y stages, per brick for the
+// x stage.
 #include "df32.cuh"
 #include "k_assemble.cuh"
 
