@@ -86,8 +86,10 @@ struct ads_handle {
   int* d_gpiv[3] = {nullptr, nullptr, nullptr};
   double* d_gpart = nullptr;  // l2 partials of the general assembly
   float2* d_jwdf[3] = {nullptr, nullptr, nullptr};
-  float2* d_symdf[3] = {nullptr, nullptr, nullptr};        // p = 2: even-odd coefficients per element
+  float2* d_symdf[3] = {nullptr, nullptr, nullptr};        // p = 2, 3: even-odd coefficients per element
   unsigned char* d_symf[3] = {nullptr, nullptr, nullptr};  // ... and which elements are symmetric
+  float2* d_nnwdf[3] = {nullptr, nullptr, nullptr};        // double-float tables times J W
+  float2* d_symwdf[3] = {nullptr, nullptr, nullptr};       // ... and their even-odd coefficients
   float2* d_band32[3] = {nullptr, nullptr, nullptr};  // double-float copies for the updated residual
 
   // device buffers
@@ -477,6 +479,8 @@ DfTabs3 df_tabs(const ads_handle* h) {
     t[d]->jw = h->d_jwdf[d];
     t[d]->sym = h->d_symdf[d];
     t[d]->symf = h->d_symf[d];
+    t[d]->nnw = h->d_nnwdf[d];
+    t[d]->symw = h->d_symwdf[d];
   }
   return tb;
 }
@@ -826,7 +830,7 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_dd64[d]); cudaFree(h->d_dd32[d]);
     cudaFree(h->d_fac64[d]); cudaFree(h->d_tfac64[d]); cudaFree(h->d_fac32[d]); cudaFree(h->d_band[d]);
     cudaFree(h->d_band32[d]); cudaFree(h->d_nndf[d]); cudaFree(h->d_jwdf[d]);
-    cudaFree(h->d_symdf[d]); cudaFree(h->d_symf[d]);
+    cudaFree(h->d_symdf[d]); cudaFree(h->d_symf[d]); cudaFree(h->d_nnwdf[d]); cudaFree(h->d_symwdf[d]);
     cudaFree(h->d_gab[d]); cudaFree(h->d_gpiv[d]);
   }
   cudaFree(h->d_gpart);
@@ -923,11 +927,20 @@ int create_impl(ads_handle* h) {
     if (h->opts.precision == ADS_PREC_MIXED) {
       if ((st = upload(h, &h->d_nndf[d], split(a.NN)))) return st;
       if ((st = upload(h, &h->d_jwdf[d], split(a.JW)))) return st;
+      // the tables with J W folded in: N[e][k][b] J(e) W(k)
+      AxisHost aw = a;
+      for (int e = 0; e < a.E; ++e)
+        for (int k = 0; k < a.q; ++k)
+          for (int i = 0; i < (a.p + 1) * 2; ++i) aw.NN[((size_t)e * a.q + k) * (a.p + 1) * 2 + i] *= a.JW[(size_t)e * a.q + k];
+      if ((st = upload(h, &h->d_nnwdf[d], split(aw.NN)))) return st;
       if (df_sym_count(a.p) > 0) {
-        std::vector<double> sc;
-        std::vector<unsigned char> sf;
+        std::vector<double> sc, scw;
+        std::vector<unsigned char> sf, sfw;
         even_odd_tables(a, sc, sf);
+        even_odd_tables(aw, scw, sfw);
+        for (size_t e = 0; e < sf.size(); ++e) sf[e] = sf[e] && sfw[e];
         if ((st = upload(h, &h->d_symdf[d], split(sc)))) return st;
+        if ((st = upload(h, &h->d_symwdf[d], split(scw)))) return st;
         if ((st = upload(h, &h->d_symf[d], sf))) return st;
       }
     }

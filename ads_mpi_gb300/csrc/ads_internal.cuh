@@ -58,6 +58,13 @@ struct DfTab {
   // and symf[e] = 1 where the element's tables are symmetric (null: none are)
   const float2* sym;           // [E][df_sym_count(p)]
   const unsigned char* symf;   // [E]
+  // the tables with the point weights J W folded in, nnw[e][k][b][d] =
+  // nn[e][k][b][d] J(e) W(k) (null: not built), and their even-odd
+  // coefficients (symw; the flags are symf's, W being symmetric): the
+  // constant-kappa heat increment interpolates with them along y and z and
+  // contracts with them along x, so that no per-point product remains
+  const float2* nnw;           // [E][Q][P+1][2]
+  const float2* symw;          // [E][df_sym_count(p)]
 };
 constexpr int df_sym_count(int p) { return p == 2 ? 9 : (p == 3 ? 16 : 0); }
 struct DfTabs3 {

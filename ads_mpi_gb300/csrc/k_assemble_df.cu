@@ -249,7 +249,12 @@ struct DfLayout {
   static constexpr size_t o_sy = o_jwz + D * Q;                 // dfl [TY][NS]
   static constexpr size_t o_sz = o_sy + D * TY * NS;            // dfl [NS]
   static constexpr size_t o_sf = o_sz + D * NS;                 // int [TY + 1]: rows, then the layer
-  static constexpr size_t o_red = (o_sf + 4 * (TY + 1) + 15) / 16 * 16;
+  // the J W-folded interpolation tables of the constant-kappa increment
+  static constexpr size_t o_nyw = (o_sf + 4 * (TY + 1) + 15) / 16 * 16;  // dfl [TY][NT]
+  static constexpr size_t o_syw = o_nyw + D * TY * NT;          // dfl [TY][NS]
+  static constexpr size_t o_nzw = o_syw + D * TY * NS;          // dfl [NT]
+  static constexpr size_t o_szw = o_nzw + D * NT;               // dfl [NS]
+  static constexpr size_t o_red = (o_szw + D * NS + 15) / 16 * 16;
   static constexpr size_t bytes = o_red + 3 * sizeof(double) * (AS_THREADS / 32);
 };
 
@@ -266,6 +271,11 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
   using E = EO<P>;
   constexpr int Q = L::Q, TX = L::TX, TY = L::TY, CX = L::CX;
   constexpr int NS = L::NS;
+  // constant conductivity, no source: the point weights J W = Jx Wx Jy Wy Jz Wz
+  // are folded into the y and z interpolation tables and the x test
+  // coefficients, and -dt kappa into the written DOFs, so the x stage has no
+  // per-point product
+  constexpr bool FOLD = !HAS_F && !HAS_K;
   constexpr int NCOL = L::NCOL, QY = L::QY, RC = L::RC, RF = L::RF, NT = L::NT;
 
   extern __shared__ __align__(16) unsigned char smem[];
@@ -287,6 +297,16 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
   dfl* SYs = reinterpret_cast<dfl*>(smem + L::o_sy);
   dfl* SZs = reinterpret_cast<dfl*>(smem + L::o_sz);
   int* SF = reinterpret_cast<int*>(smem + L::o_sf);
+  dfl* NYw = reinterpret_cast<dfl*>(smem + L::o_nyw);
+  dfl* SYw = reinterpret_cast<dfl*>(smem + L::o_syw);
+  dfl* NZw = reinterpret_cast<dfl*>(smem + L::o_nzw);
+  dfl* SZw = reinterpret_cast<dfl*>(smem + L::o_szw);
+  // the y and z interpolation tables (J W folded in under FOLD); the y and z
+  // test contractions keep NYs, SYs and NZs
+  const dfl* NYi = FOLD ? NYw : NYs;
+  const dfl* SYi = FOLD ? SYw : SYs;
+  const dfl* NZi = FOLD ? NZw : NZs;
+  const dfl* SZi = FOLD ? SZw : SZs;
   double* red = reinterpret_cast<double*>(smem + L::o_red);
 
   const Geometry& g = a.g;
@@ -333,10 +353,16 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
 #pragma unroll
       for (int k = 0; k < Q; ++k) jwx[k] = lane_elem ? tb.x.jw[(size_t)ex * Q + k] : df_zero();
       if (symx) {
+        // even-odd coefficients for the interpolation, then (under FOLD) those
+        // of the J W-folded tables for the test contraction
         dfl* t = &nx[0][0][0];
 #pragma unroll
-        for (int i = 0; i < Q * (P + 1) * 2; ++i)
-          t[i] = (i < NS && lane_elem) ? tb.x.sym[(size_t)ex * NS + i] : df_zero();
+        for (int i = 0; i < Q * (P + 1) * 2; ++i) {
+          dfl v = df_zero();
+          if (lane_elem && i < NS) v = tb.x.sym[(size_t)ex * NS + i];
+          if (FOLD && lane_elem && i >= NS && i < 2 * NS) v = tb.x.symw[(size_t)ex * NS + i - NS];
+          t[i] = v;
+        }
       } else {
 #pragma unroll
         for (int k = 0; k < Q; ++k) {
@@ -351,6 +377,7 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
     for (int i = tid; i < TY * NT; i += AS_THREADS) {
       const int ey = y0 + i / NT;
       NYs[i] = (ey < Ey) ? tb.y.nn[(size_t)ey * NT + (i % NT)] : df_zero();
+      if constexpr (FOLD) NYw[i] = (ey < Ey) ? tb.y.nnw[(size_t)ey * NT + (i % NT)] : df_zero();
     }
     if constexpr (E::on) {
       // the element rows' even-odd coefficients and flags (the y stage of a
@@ -359,6 +386,7 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
       for (int i = tid; i < TY * NS; i += AS_THREADS) {
         const int ey = y0 + i / NS;
         SYs[i] = (ys && ey < Ey) ? tb.y.sym[(size_t)ey * NS + (i % NS)] : df_zero();
+        if constexpr (FOLD) SYw[i] = (ys && ey < Ey) ? tb.y.symw[(size_t)ey * NS + (i % NS)] : df_zero();
       }
       for (int i = tid; i < TY; i += AS_THREADS) SF[i] = (ys && y0 + i < Ey) ? (int)tb.y.symf[y0 + i] : 0;
     }
@@ -379,11 +407,17 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
       float l2_layer = 0.f;
       if (ez + 1 < ez1) issue_plane<P>(cring + ((ez + P + 1) % RC) * NCOL, a.u, g, x0, y0, ez + P + 1, a.u_px);
       cp_async_commit();
-      for (int i = tid; i < NT; i += AS_THREADS) NZs[i] = tb.z.nn[(size_t)ez * NT + i];
+      for (int i = tid; i < NT; i += AS_THREADS) {
+        NZs[i] = tb.z.nn[(size_t)ez * NT + i];
+        if constexpr (FOLD) NZw[i] = tb.z.nnw[(size_t)ez * NT + i];
+      }
       for (int i = tid; i < Q; i += AS_THREADS) JWZs[i] = tb.z.jw[(size_t)ez * Q + i];
       if constexpr (E::on) {
         const bool zs = tb.z.sym != nullptr;
-        for (int i = tid; i < NS; i += AS_THREADS) SZs[i] = zs ? tb.z.sym[(size_t)ez * NS + i] : df_zero();
+        for (int i = tid; i < NS; i += AS_THREADS) {
+          SZs[i] = zs ? tb.z.sym[(size_t)ez * NS + i] : df_zero();
+          if constexpr (FOLD) SZw[i] = zs ? tb.z.symw[(size_t)ez * NS + i] : df_zero();
+        }
         if (tid == 0) SF[TY] = zs ? (int)tb.z.symf[ez] : 0;
       }
       cp_async_wait<1>();
@@ -418,8 +452,8 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
       // ---- z interpolation per column: ZA = sum_b Nz C, ZB = sum_b dNz C ----
       if constexpr (E::on) {
         if (symz) {
-          const typename E::N sn = E::n(SZs);
-          const typename E::D sd = E::d(SZs);
+          const typename E::N sn = E::n(SZi);
+          const typename E::D sd = E::d(SZi);
           for (int col = tid; col < NCOL; col += AS_THREADS) {
             dfl c[P + 1], za[Q], zb[Q];
 #pragma unroll
@@ -439,12 +473,12 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
         for (int b = 0; b <= P; ++b) c[b] = tring[((ez + b) % RC) * NCOL + col];
 #pragma unroll
         for (int kz = 0; kz < Q; ++kz) {
-          dfl za = df_mul(NZs[(kz * (P + 1)) * 2 + 0], c[0]);
-          dfl zb = df_mul(NZs[(kz * (P + 1)) * 2 + 1], c[0]);
+          dfl za = df_mul(NZi[(kz * (P + 1)) * 2 + 0], c[0]);
+          dfl zb = df_mul(NZi[(kz * (P + 1)) * 2 + 1], c[0]);
 #pragma unroll
           for (int b = 1; b <= P; ++b) {
-            za = df_mac(za, NZs[(kz * (P + 1) + b) * 2 + 0], c[b]);
-            zb = df_mac(zb, NZs[(kz * (P + 1) + b) * 2 + 1], c[b]);
+            za = df_mac(za, NZi[(kz * (P + 1) + b) * 2 + 0], c[b]);
+            zb = df_mac(zb, NZi[(kz * (P + 1) + b) * 2 + 1], c[b]);
           }
           ZA[kz * NCOL + col] = za;
           ZB[kz * NCOL + col] = zb;
@@ -471,8 +505,8 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
           }
           if constexpr (E::on) {
             if (symy) {
-              const typename E::N sn = E::n(SYs + my_ey * NS);
-              const typename E::D sd = E::d(SYs + my_ey * NS);
+              const typename E::N sn = E::n(SYi + my_ey * NS);
+              const typename E::D sd = E::d(SYi + my_ey * NS);
               dfl y0v[Q], y1v[Q], y2v[Q];
               E::interp_nd(y0v, y1v, za, sn, sd);
               E::interp_n(y2v, zb, sn);
@@ -488,7 +522,7 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
           if (!symy) {
 #pragma unroll
             for (int ky = 0; ky < Q; ++ky) {
-              const dfl* ny = NYs + my_ey * NT + ky * (P + 1) * 2;
+              const dfl* ny = NYi + my_ey * NT + ky * (P + 1) * 2;
               dfl y0v = df_mul(ny[0], za[0]);
               dfl y1v = df_mul(ny[1], za[0]);
               dfl y2v = df_mul(ny[0], zb[0]);
@@ -511,8 +545,12 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
         for (int qy = warp; qy < QY; qy += AS_THREADS / 32) {
           const int ey_l = qy / Q;
           const bool elem_ok = lane_elem && (y0 + ey_l < Ey);
-          const dfl jwyz = df_mul(JWYs[qy], JWZs[kz]);
-          const dfl cyz = df_mul(ndtk, jwyz);
+          const dfl jwyz = FOLD ? df_zero() : df_mul(JWYs[qy], JWZs[kz]);
+          const dfl cyz = FOLD ? df_zero() : df_mul(ndtk, jwyz);
+          // under FOLD the interpolated values carry Jy Wy Jz Wz: the l2norm's
+          // J W u^2 is Jx Wx u'^2 / (Jy Wy Jz Wz)
+          const float jyz = JWYs[qy].x * JWZs[kz].x;  // 0 on rows past the mesh
+          const float wr = (FOLD && jyz > 0.f) ? __frcp_rn(jyz) : 0.f;
           // this lane's P + 1 values of a y-interpolated plane
           auto yrow = [&](const dfl* Yp, dfl (&v)[P + 1]) {
 #pragma unroll
@@ -521,7 +559,42 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
           const long long qyg = (long long)y0 * Q + qy;
           const long long qzg = (long long)ez * Q + kz;
           dfl h0[P + 1], h1[P + 1], h2[P + 1];
-          if constexpr (E::on) {
+          if constexpr (E::on && FOLD) {
+            if (symx) {
+              // J W is in the y and z tables and in the test coefficients
+              // (the x table registers' second half): interpolate, contract
+              const typename E::N sn = E::n(&nx[0][0][0]);
+              const typename E::D sd = E::d(&nx[0][0][0]);
+              const typename E::N tn = E::n(&nx[0][0][0] + NS);
+              const typename E::D td = E::d(&nx[0][0][0] + NS);
+              dfl yv0[P + 1];
+              yrow(Y0, yv0);
+              {
+                float u[Q];
+                E::uu(u, yv0, sn);
+#pragma unroll
+                for (int kx = 0; kx < Q; ++kx) l2_layer = fmaf(jwx[kx].x * wr * u[kx], u[kx], l2_layer);
+              }
+              {
+                dfl du[Q];
+                E::interp_d(du, yv0, sd);
+                E::test_d(h0, du, td);
+              }
+              {
+                dfl du[Q], yv1[P + 1];
+                yrow(Y1, yv1);
+                E::interp_n(du, yv1, sn);
+                E::test_n(h1, du, tn);
+              }
+              {
+                dfl du[Q], yv2[P + 1];
+                yrow(Y2, yv2);
+                E::interp_n(du, yv2, sn);
+                E::test_n(h2, du, tn);
+              }
+            }
+          }
+          if constexpr (E::on && !FOLD) {
             if (symx) {
               const typename E::N sn = E::n(&nx[0][0][0]);
               const typename E::D sd = E::d(&nx[0][0][0]);
@@ -602,14 +675,20 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
               uu = fmaf(nx[kx][b][0].x, yv0[b].x, uu);
             }
             const long long qidx = ((long long)(x0 + lane) * Q + kx) + QXt * (qyg + QYt * qzg);
-            const dfl s = df_mul(jwx[kx], jwyz);
             dfl c;
-            if constexpr (HAS_K) c = df_mul(df_mul(ndt, elem_ok ? df_split(a.kqp[qidx], 0) : df_zero()), s);
-            else c = df_mul(jwx[kx], cyz);
-            const dfl g1 = df_mul(c, dux), g2 = df_mul(c, duy), g3 = df_mul(c, duz);
-            l2_layer = fmaf(s.x * uu, uu, l2_layer);
             dfl g0 = df_zero();
-            if constexpr (HAS_F) g0 = df_mul(df_mul(s, dtv), elem_ok ? df_split(a.fqp[qidx], uexp) : df_zero());
+            if constexpr (FOLD) {
+              // Jy Wy Jz Wz in the interpolated values, -dt kappa at the write
+              c = jwx[kx];
+              l2_layer = fmaf(jwx[kx].x * wr * uu, uu, l2_layer);
+            } else {
+              const dfl s = df_mul(jwx[kx], jwyz);
+              if constexpr (HAS_K) c = df_mul(df_mul(ndt, elem_ok ? df_split(a.kqp[qidx], 0) : df_zero()), s);
+              else c = df_mul(jwx[kx], cyz);
+              l2_layer = fmaf(s.x * uu, uu, l2_layer);
+              if constexpr (HAS_F) g0 = df_mul(df_mul(s, dtv), elem_ok ? df_split(a.fqp[qidx], uexp) : df_zero());
+            }
+            const dfl g1 = df_mul(c, dux), g2 = df_mul(c, duy), g3 = df_mul(c, duz);
 #pragma unroll
             for (int b = 0; b <= P; ++b) {
               if (kx == 0) {
@@ -722,8 +801,9 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
         for (int it = tid; it < NCOL; it += AS_THREADS) {
           const int cy = it / CX, cx = it % CX;
           const int x = x0 + cx, y = y0 + cy;
-          const dfl f = fring[slot + it];
+          dfl f = fring[slot + it];
           fring[slot + it] = df_zero();
+          if constexpr (FOLD) f = df_mul(f, ndtk);  // -dt kappa, kept out of the point sums
           if (x < Nx && y < Ny) {
             const double v = f2d_scaled(f.x, -uexp) + f2d_scaled(f.y, -uexp);
             const bool ownx = (cx < TX) || lastx, owny = (cy < TY) || lasty;
@@ -746,7 +826,8 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
         const int cy = it / CX, cx = it % CX;
         const int x = x0 + cx, y = y0 + cy;
         if (x < Nx && y < Ny && cz < g.N[2]) {
-          const dfl f = fring[slot + it];
+          dfl f = fring[slot + it];
+          if constexpr (FOLD) f = df_mul(f, ndtk);  // -dt kappa, kept out of the point sums
           const double v = f2d_scaled(f.x, -uexp) + f2d_scaled(f.y, -uexp);
           const bool ownx = (cx < TX) || lastx, owny = (cy < TY) || lasty;
           const int cls = (ownx ? 0 : 1) | (owny ? 0 : 2) | (ownz ? 0 : 4);

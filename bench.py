@@ -209,7 +209,7 @@ def algorithmic_assembly_flops(P, nelem):
 DF_MUL, DF_MAC, DF_ADD = 4, 12, 8
 
 
-def df_assembly_ops(P, nelem, sym=(0.0, 0.0, 0.0)):
+def df_assembly_ops(P, nelem, sym=(0.0, 0.0, 0.0), fold=False):
     """FP32 operations (each FFMA, FADD or FMUL one operation) of the
     double-float heat increment assembly per launch, counted from the kernel's
     stages for the work each element needs (the brick halo's repeated columns
@@ -218,16 +218,21 @@ def df_assembly_ops(P, nelem, sym=(0.0, 0.0, 0.0)):
     column) pair, the x stage of one element, and the DOF-plane accumulation.
     At p = 2, sym = the fractions of the x stage, element rows and layers
     that run the even-odd form (centro-symmetric elements), whose sums cost
-    less: an interpolation pair 52-68 operations where the direct sums take 84."""
+    less: an interpolation pair 52-68 operations where the direct sums take 84.
+    fold: constant conductivity and no source, where the point weights sit in
+    the tables and -dt kappa multiplies each written DOF, so the x stage has
+    no per-point product."""
     q = P + 1
     z = q * (2 * DF_MUL + 2 * P * DF_MAC)
     y = q * q * (3 * DF_MUL + 3 * P * DF_MAC)
-    per_kx = (3 * DF_MUL + 3 * P * DF_MAC) + (1 + P) + DF_MUL + DF_MUL + 3 * DF_MUL + 2
+    weights = 3 if fold else DF_MUL + DF_MUL + 2      # l2 weight (and c = Jx Wx Jy Wy Jz Wz (-dt kappa))
+    per_kx = (3 * DF_MUL + 3 * P * DF_MAC) + (1 + P) + weights + 3 * DF_MUL
     contraction = 3 * (P + 1) * DF_MUL + (q - 1) * 3 * (P + 1) * DF_MAC
-    x = q * q * (2 * DF_MUL + q * per_kx + contraction + 3 * P * DF_ADD)
+    row = 0 if fold else 2 * DF_MUL                    # Jy Wy Jz Wz and its -dt kappa per row
+    x = q * q * (row + q * per_kx + contraction + 3 * P * DF_ADD)
     yz_kz = (P + 1) * (2 * DF_MUL + DF_MAC) + (q - 1) * (P + 1) * 3 * DF_MAC + (P + 1) ** 2 * 2 * DF_MAC
     yz = q * yz_kz
-    acc = (P + 1) ** 2 * DF_ADD
+    acc = (P + 1) ** 2 * DF_ADD + (DF_MUL if fold else 0)
     if P == 2:
         fx, fy, fz = sym
         # even-odd sums: s and d of the inputs (2 sums), per output pair a
@@ -238,8 +243,13 @@ def df_assembly_ops(P, nelem, sym=(0.0, 0.0, 0.0)):
         eo_nd = eo_n + eo_d - 2 * DF_ADD                                                   # 108: s, d shared
         z_eo = eo_nd
         y_eo = q * (eo_nd + eo_n)
-        x_eo = q * q * (2 * DF_MUL + q * (DF_MUL + 1) + 15 + (eo_d + 3 * DF_MUL + eo_d)
-                        + 2 * (eo_n + 3 * DF_MUL + eo_n) + 3 * P * DF_ADD)
+        if fold:
+            # the reciprocal of Jy Wy Jz Wz, u at the points and the l2 terms, then
+            # per component an interpolation and a contraction
+            x_row = 3 + 18 + 2 * eo_d + 2 * (2 * eo_n)
+        else:
+            x_row = 2 * DF_MUL + q * (DF_MUL + 1) + 15 + (eo_d + 3 * DF_MUL + eo_d) + 2 * (eo_n + 3 * DF_MUL + eo_n)
+        x_eo = q * q * (x_row + 3 * P * DF_ADD)
         yz_eo = q * ((eo_n + eo_d + 3 * DF_ADD + eo_n) + (P + 1) ** 2 * 2 * DF_MAC)
         z = fz * z_eo + (1 - fz) * z
         y = fy * y_eo + (1 - fy) * y
@@ -831,7 +841,7 @@ def run_ours(args, world, rank, local):
             # FP32 operations of the double-float algorithm against the FP32
             # pipe's instruction rate (half the FMA flop rate)
             eo = even_odd_fractions(A, E, p)
-            ops = df_assembly_ops(p, nelem, eo)
+            ops = df_assembly_ops(p, nelem, eo, fold=True)  # the timed step: kappa = 1, no source
             achieved = ops / avg / 1e12
             peak = fp32_peak / 2
             return {"kernel": kname, "bound": "fp32-pipe", "achieved": achieved, "peak": peak, "unit": "Top/s",

@@ -45,6 +45,7 @@ def test_double_float_operation_model():
     from ads_mpi_gb300 import ads as A
     assert bench.df_assembly_ops(2, 1) == 8187
     assert bench.df_assembly_ops(2, 1, (1.0, 1.0, 1.0)) < 0.81 * 8187
+    assert bench.df_assembly_ops(2, 1, (1.0, 1.0, 1.0), fold=True) < bench.df_assembly_ops(2, 1, (1.0, 1.0, 1.0))
     fx, fy, fz = bench.even_odd_fractions(A, 256, 2)
     assert fx == (256 - 30 - 16) / 256 and fy == fz == 254 / 256
     fx96, fy96, _ = bench.even_odd_fractions(A, 96, 2)
