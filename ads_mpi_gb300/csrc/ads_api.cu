@@ -90,6 +90,7 @@ struct ads_handle {
   unsigned char* d_symf[3] = {nullptr, nullptr, nullptr};  // ... and which elements are symmetric
   float2* d_nnwdf[3] = {nullptr, nullptr, nullptr};        // double-float tables times J W
   float2* d_symwdf[3] = {nullptr, nullptr, nullptr};       // ... and their even-odd coefficients
+  float2* d_matdf = nullptr;   // x: element stiffness and mass matrices (double-float)
   float2* d_band32[3] = {nullptr, nullptr, nullptr};  // double-float copies for the updated residual
 
   // device buffers
@@ -327,6 +328,28 @@ void even_odd_tables(const AxisHost& a, std::vector<double>& sc, std::vector<uns
   }
 }
 
+// Each element's 1-D stiffness and mass matrices along an axis, K[b][b'] =
+// sum_k dN[k][b] dN[k][b'] J W(k), M[b][b'] = sum_k N[k][b] N[k][b'] J W(k)
+// (the same Gauss rule, in FP64; row-major, K then M: DfTab::mat).
+std::vector<double> element_matrices(const AxisHost& a) {
+  const int E = a.E, p = a.p, q = p + 1, nb = p + 1;
+  std::vector<double> m((size_t)E * 2 * nb * nb, 0.0);
+  for (int e = 0; e < E; ++e) {
+    auto N = [&](int k, int b, int d) { return a.NN[(((size_t)e * q + k) * (p + 1) + b) * 2 + d]; };
+    for (int t = 0; t < 2; ++t) {  // t = 0: stiffness (derivatives), 1: mass (values)
+      const int d = t == 0 ? 1 : 0;
+      double* M = &m[((size_t)e * 2 + t) * nb * nb];
+      for (int b = 0; b < nb; ++b)
+        for (int bb = 0; bb < nb; ++bb) {
+          double s = 0.0;
+          for (int k = 0; k < q; ++k) s += N(k, b, d) * N(k, bb, d) * a.JW[(size_t)e * q + k];
+          M[b * nb + bb] = s;
+        }
+    }
+  }
+  return m;
+}
+
 bool encode(CUtensorMap* m, void* base, bool fp32, cuuint64_t d0, cuuint64_t d1, cuuint64_t d2,
             long long pitch, cuuint32_t b0, cuuint32_t b1, cuuint32_t b2) {
   PFN_encodeTiled fn = get_encode();
@@ -481,6 +504,7 @@ DfTabs3 df_tabs(const ads_handle* h) {
     t[d]->symf = h->d_symf[d];
     t[d]->nnw = h->d_nnwdf[d];
     t[d]->symw = h->d_symwdf[d];
+    t[d]->mat = d == 0 ? h->d_matdf : nullptr;
   }
   return tb;
 }
@@ -831,6 +855,7 @@ void free_all(ads_handle* h) {
     cudaFree(h->d_fac64[d]); cudaFree(h->d_tfac64[d]); cudaFree(h->d_fac32[d]); cudaFree(h->d_band[d]);
     cudaFree(h->d_band32[d]); cudaFree(h->d_nndf[d]); cudaFree(h->d_jwdf[d]);
     cudaFree(h->d_symdf[d]); cudaFree(h->d_symf[d]); cudaFree(h->d_nnwdf[d]); cudaFree(h->d_symwdf[d]);
+    if (d == 0) cudaFree(h->d_matdf);
     cudaFree(h->d_gab[d]); cudaFree(h->d_gpiv[d]);
   }
   cudaFree(h->d_gpart);
@@ -933,6 +958,7 @@ int create_impl(ads_handle* h) {
         for (int k = 0; k < a.q; ++k)
           for (int i = 0; i < (a.p + 1) * 2; ++i) aw.NN[((size_t)e * a.q + k) * (a.p + 1) * 2 + i] *= a.JW[(size_t)e * a.q + k];
       if ((st = upload(h, &h->d_nnwdf[d], split(aw.NN)))) return st;
+      if (d == 0 && (st = upload(h, &h->d_matdf, split(element_matrices(a))))) return st;
       if (df_sym_count(a.p) > 0) {
         std::vector<double> sc, scw;
         std::vector<unsigned char> sf, sfw;

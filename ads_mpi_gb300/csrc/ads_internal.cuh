@@ -61,10 +61,14 @@ struct DfTab {
   // the tables with the point weights J W folded in, nnw[e][k][b][d] =
   // nn[e][k][b][d] J(e) W(k) (null: not built), and their even-odd
   // coefficients (symw; the flags are symf's, W being symmetric): the
-  // constant-kappa heat increment interpolates with them along y and z and
-  // contracts with them along x, so that no per-point product remains
+  // constant-kappa heat increment interpolates with them along y and z (x
+  // takes the element matrices below), so that no per-point product remains
   const float2* nnw;           // [E][Q][P+1][2]
   const float2* symw;          // [E][df_sym_count(p)]
+  // x only, for the same increment: each element's 1-D stiffness and mass
+  // matrices, K[b][b'] = sum_k dN[k][b] dN[k][b'] J W(k) and M[b][b'] =
+  // sum_k N[k][b] N[k][b'] J W(k) (row-major, K then M)
+  const float2* mat;           // [E][2][P+1][P+1]
 };
 constexpr int df_sym_count(int p) { return p == 2 ? 9 : (p == 3 ? 16 : 0); }
 struct DfTabs3 {

@@ -119,6 +119,29 @@ struct EO<2> {
     u[2] = e - d;
     u[1] = fmaf(n.n11.x, v[1].x, n.n10.x * sp);
   }
+  // the z test contraction h[b] += sum_k N[k][b] g0[k] + dN[k][b] g1[k],
+  // accumulated over the points in even-odd form: h[0] holds X, h[2] Y and
+  // h[1] the middle function until zt_finish sets h[0], h[2] = X +- Y.
+  // zt_pair takes the points (k, p - k) = (0, 2), zt_mid the middle point;
+  // t holds the even-odd coefficients (the N part, then the dN part)
+  static __device__ __forceinline__ void zt_pair(dfl (&h)[3], int, dfl g0a, dfl g0b, dfl g1a, dfl g1b,
+                                                 const dfl* t) {
+    const dfl s0 = df_add(g0a, g0b), d0 = df_sub(g0a, g0b);
+    const dfl s1 = df_add(g1a, g1b), d1 = df_sub(g1a, g1b);
+    h[0] = df_mac(df_mac(h[0], t[0], s0), t[5], d1);  // a S0 + a' D1
+    h[2] = df_mac(df_mac(h[2], t[1], d0), t[6], s1);  // c D0 + c' S1
+    h[1] = df_mac(df_mac(h[1], t[2], s0), t[7], d1);  // N01 S0 + dN01 D1
+  }
+  static __device__ __forceinline__ void zt_mid(dfl (&h)[3], dfl g0, dfl g1, const dfl* t) {
+    h[0] = df_mac(h[0], t[3], g0);  // N10
+    h[2] = df_mac(h[2], t[8], g1);  // dN10
+    h[1] = df_mac(h[1], t[4], g0);  // N11
+  }
+  static __device__ __forceinline__ void zt_finish(dfl (&h)[3]) {
+    const dfl x = h[0], y = h[2];
+    h[0] = df_add(x, y);
+    h[2] = df_sub(x, y);
+  }
 };
 
 template <>
@@ -220,6 +243,27 @@ struct EO<3> {
     u[1] = X1 + Y1;
     u[2] = X1 - Y1;
   }
+  // the z test contraction in even-odd form (as EO<2>): h[b] holds X_b and
+  // h[3-b] Y_b (b = 0, 1) until zt_finish; zt_pair takes the points (k, 3 - k)
+  static __device__ __forceinline__ void zt_pair(dfl (&h)[4], int k, dfl g0a, dfl g0b, dfl g1a, dfl g1b,
+                                                 const dfl* t) {
+    const dfl s0 = df_add(g0a, g0b), d0 = df_sub(g0a, g0b);
+    const dfl s1 = df_add(g1a, g1b), d1 = df_sub(g1a, g1b);
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      h[b] = df_mac(df_mac(h[b], t[2 * k + b], s0), t[8 + 2 * k + b], d1);              // a S0 + a' D1
+      h[3 - b] = df_mac(df_mac(h[3 - b], t[4 + 2 * k + b], d0), t[12 + 2 * k + b], s1);  // c D0 + c' S1
+    }
+  }
+  static __device__ __forceinline__ void zt_mid(dfl (&)[4], dfl, dfl, const dfl*) {}
+  static __device__ __forceinline__ void zt_finish(dfl (&h)[4]) {
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const dfl x = h[b], y = h[3 - b];
+      h[b] = df_add(x, y);
+      h[3 - b] = df_sub(x, y);
+    }
+  }
 };
 
 template <int P>
@@ -271,11 +315,16 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
   using E = EO<P>;
   constexpr int Q = L::Q, TX = L::TX, TY = L::TY, CX = L::CX;
   constexpr int NS = L::NS;
-  // constant conductivity, no source: the point weights J W = Jx Wx Jy Wy Jz Wz
-  // are folded into the y and z interpolation tables and the x test
-  // coefficients, and -dt kappa into the written DOFs, so the x stage has no
-  // per-point product
+  // constant conductivity, no source: the point weights Jy Wy and Jz Wz are
+  // folded into the y and z interpolation tables, the x quadrature into the
+  // brick's x stiffness and mass bands (per element sum_kx of the basis
+  // products times Jx Wx, the same Gauss sums in another order, then summed
+  // over the elements on a column), and -dt kappa into the written DOFs: the
+  // x stage is three banded products per row of points
   constexpr bool FOLD = !HAS_F && !HAS_K;
+  // the z test contraction of a symmetric layer in even-odd form (at p = 2
+  // with a per-point conductivity or a source its registers would spill)
+  constexpr bool ZEO = E::on && (FOLD || P == 3);
   constexpr int NCOL = L::NCOL, QY = L::QY, RC = L::RC, RF = L::RF, NT = L::NT;
 
   extern __shared__ __align__(16) unsigned char smem[];
@@ -316,6 +365,10 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
   const long long QXt = (long long)Ex * Q, QYt = (long long)Ey * Q;
   const int nitems = a.nix * a.niy * a.niz;
   const int my_ey = tid / CX, my_cx = tid % CX;
+  // FOLD: the columns lane - P .. lane + P of a row, clamped into the row
+  int xoff[2 * P + 1];
+#pragma unroll
+  for (int j = 0; j <= 2 * P; ++j) xoff[j] = min(max(lane + j - P, 0), CX - 1);
   // coefficients (and the source) are multiplied by 2^uexp
   const int uexp = pow2_exp(*a.uscale);
   const dfl ndtk = df_split(-a.dt * a.kappa, 0);  // constant conductivity
@@ -343,26 +396,39 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
     // even-odd coefficients
     dfl nx[Q][P + 1][2];
     dfl jwx[Q];
+    // FOLD: row lane of the brick's x stiffness and mass bands, column
+    // x0 + lane against columns x0 + lane - P .. x0 + lane + P: the sums of
+    // the element matrices' rows over the brick's elements on that column
+    dfl kb[2 * P + 1], mb[2 * P + 1];
     const bool lane_elem = (lane < TX) && (x0 + lane < Ex);
     bool symx = false;
-    if constexpr (E::on) {
+    if constexpr (E::on && !FOLD) {
       if (tb.x.sym != nullptr) symx = __all_sync(0xffffffffu, !lane_elem || tb.x.symf[x0 + lane] != 0);
     }
-    {
+    if constexpr (FOLD) {
+#pragma unroll
+      for (int j = 0; j <= 2 * P; ++j) kb[j] = mb[j] = df_zero();
+#pragma unroll
+      for (int b = 0; b <= P; ++b) {  // element x0 + lane - b, its local function b
+        const int e = x0 + lane - b;
+        if (lane - b >= 0 && lane - b < TX && e < Ex) {
+          const dfl* m = tb.x.mat + (size_t)e * 2 * (P + 1) * (P + 1) + b * (P + 1);
+#pragma unroll
+          for (int c = 0; c <= P; ++c) {
+            kb[c - b + P] = df_add(kb[c - b + P], m[c]);
+            mb[c - b + P] = df_add(mb[c - b + P], m[(P + 1) * (P + 1) + c]);
+          }
+        }
+      }
+    } else {
       const int ex = x0 + lane;
 #pragma unroll
       for (int k = 0; k < Q; ++k) jwx[k] = lane_elem ? tb.x.jw[(size_t)ex * Q + k] : df_zero();
       if (symx) {
-        // even-odd coefficients for the interpolation, then (under FOLD) those
-        // of the J W-folded tables for the test contraction
+        // even-odd coefficients for the interpolation and the test contraction
         dfl* t = &nx[0][0][0];
 #pragma unroll
-        for (int i = 0; i < Q * (P + 1) * 2; ++i) {
-          dfl v = df_zero();
-          if (lane_elem && i < NS) v = tb.x.sym[(size_t)ex * NS + i];
-          if (FOLD && lane_elem && i >= NS && i < 2 * NS) v = tb.x.symw[(size_t)ex * NS + i - NS];
-          t[i] = v;
-        }
+        for (int i = 0; i < Q * (P + 1) * 2; ++i) t[i] = (lane_elem && i < NS) ? tb.x.sym[(size_t)ex * NS + i] : df_zero();
       } else {
 #pragma unroll
         for (int k = 0; k < Q; ++k) {
@@ -493,8 +559,12 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
 #pragma unroll
         for (int bz = 0; bz <= P; ++bz) acc[by][bz] = df_zero();
 
+      // the layer's points in the order 0, P, 1, P - 1, ...: a symmetric layer
+      // contracts each pair (k, P - k) at once (i0p, i1p hold the first)
+      dfl i0p[P + 1], i1p[P + 1];
 #pragma unroll 1
-      for (int kz = 0; kz < Q; ++kz) {
+      for (int it = 0; it < Q; ++it) {
+        const int kz = (it & 1) ? P - (it >> 1) : (it >> 1);
         // ---- y interpolation, one (element row, column) per thread ----
         {
           dfl za[P + 1], zb[P + 1];
@@ -558,164 +628,151 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
           };
           const long long qyg = (long long)y0 * Q + qy;
           const long long qzg = (long long)ez * Q + kz;
-          dfl h0[P + 1], h1[P + 1], h2[P + 1];
-          if constexpr (E::on && FOLD) {
-            if (symx) {
-              // J W is in the y and z tables and in the test coefficients
-              // (the x table registers' second half): interpolate, contract
-              const typename E::N sn = E::n(&nx[0][0][0]);
-              const typename E::D sd = E::d(&nx[0][0][0]);
-              const typename E::N tn = E::n(&nx[0][0][0] + NS);
-              const typename E::D td = E::d(&nx[0][0][0] + NS);
-              dfl yv0[P + 1];
-              yrow(Y0, yv0);
-              {
-                float u[Q];
-                E::uu(u, yv0, sn);
+          if constexpr (FOLD) {
+            // H0 = Kx Y0, H1 = Mx Y1, H2 = Mx Y2 along the row with the brick's
+            // bands (column lane), and the l2norm's row term Y0' Mx Y0 from
+            // the high parts.  Columns outside the row carry zero coefficients:
+            // their reads are clamped into it.
+            const dfl* r0 = Y0 + qy * CX;
+            const dfl* r1 = Y1 + qy * CX;
+            const dfl* r2 = Y2 + qy * CX;
+            dfl a0 = df_mul(kb[0], r0[xoff[0]]);
+            dfl a1 = df_mul(mb[0], r1[xoff[0]]);
+            dfl a2 = df_mul(mb[0], r2[xoff[0]]);
+            float t = mb[0].x * r0[xoff[0]].x;
 #pragma unroll
-                for (int kx = 0; kx < Q; ++kx) l2_layer = fmaf(jwx[kx].x * wr * u[kx], u[kx], l2_layer);
-              }
-              {
-                dfl du[Q];
-                E::interp_d(du, yv0, sd);
-                E::test_d(h0, du, td);
-              }
-              {
-                dfl du[Q], yv1[P + 1];
-                yrow(Y1, yv1);
-                E::interp_n(du, yv1, sn);
-                E::test_n(h1, du, tn);
-              }
-              {
-                dfl du[Q], yv2[P + 1];
-                yrow(Y2, yv2);
-                E::interp_n(du, yv2, sn);
-                E::test_n(h2, du, tn);
-              }
+            for (int j = 1; j <= 2 * P; ++j) {
+              const dfl y0 = r0[xoff[j]];
+              a0 = df_mac(a0, kb[j], y0);
+              a1 = df_mac(a1, mb[j], r1[xoff[j]]);
+              a2 = df_mac(a2, mb[j], r2[xoff[j]]);
+              t = fmaf(mb[j].x, y0.x, t);
             }
-          }
-          if constexpr (E::on && !FOLD) {
-            if (symx) {
-              const typename E::N sn = E::n(&nx[0][0][0]);
-              const typename E::D sd = E::d(&nx[0][0][0]);
-              // the point weights, then one gradient component at a time:
-              // interpolate, weight, contract
-              dfl cw[Q];
-              float sx[Q];
-              dfl g0[Q];
+            l2_layer = fmaf(wr * r0[lane].x, t, l2_layer);
+            H0[qy * CX + lane] = a0;
+            H1[qy * CX + lane] = a1;
+            H2[qy * CX + lane] = a2;
+          } else {
+            dfl h0[P + 1], h1[P + 1], h2[P + 1];
+            if constexpr (E::on && !FOLD) {
+              if (symx) {
+                const typename E::N sn = E::n(&nx[0][0][0]);
+                const typename E::D sd = E::d(&nx[0][0][0]);
+                // the point weights, then one gradient component at a time:
+                // interpolate, weight, contract
+                dfl cw[Q];
+                float sx[Q];
+                dfl g0[Q];
 #pragma unroll
-              for (int kx = 0; kx < Q; ++kx) {
-                const long long qidx = ((long long)(x0 + lane) * Q + kx) + QXt * (qyg + QYt * qzg);
-                if constexpr (HAS_K || HAS_F) {
-                  const dfl s = df_mul(jwx[kx], jwyz);
-                  sx[kx] = s.x;
-                  if constexpr (HAS_K) cw[kx] = df_mul(df_mul(ndt, elem_ok ? df_split(a.kqp[qidx], 0) : df_zero()), s);
-                  if constexpr (HAS_F) g0[kx] = df_mul(df_mul(s, dtv), elem_ok ? df_split(a.fqp[qidx], uexp) : df_zero());
-                } else {
-                  sx[kx] = jwx[kx].x * jwyz.x;  // the l2norm's weight: high parts suffice
+                for (int kx = 0; kx < Q; ++kx) {
+                  const long long qidx = ((long long)(x0 + lane) * Q + kx) + QXt * (qyg + QYt * qzg);
+                  if constexpr (HAS_K || HAS_F) {
+                    const dfl s = df_mul(jwx[kx], jwyz);
+                    sx[kx] = s.x;
+                    if constexpr (HAS_K) cw[kx] = df_mul(df_mul(ndt, elem_ok ? df_split(a.kqp[qidx], 0) : df_zero()), s);
+                    if constexpr (HAS_F) g0[kx] = df_mul(df_mul(s, dtv), elem_ok ? df_split(a.fqp[qidx], uexp) : df_zero());
+                  } else {
+                    sx[kx] = jwx[kx].x * jwyz.x;  // the l2norm's weight: high parts suffice
+                  }
+                  if constexpr (!HAS_K) cw[kx] = df_mul(jwx[kx], cyz);
                 }
-                if constexpr (!HAS_K) cw[kx] = df_mul(jwx[kx], cyz);
-              }
-              dfl yv0[P + 1];
-              yrow(Y0, yv0);
-              {
-                // u at the points from the high parts (the l2norm), the same even-odd form
-                float u[Q];
-                E::uu(u, yv0, sn);
+                dfl yv0[P + 1];
+                yrow(Y0, yv0);
+                {
+                  // u at the points from the high parts (the l2norm), the same even-odd form
+                  float u[Q];
+                  E::uu(u, yv0, sn);
 #pragma unroll
-                for (int kx = 0; kx < Q; ++kx) l2_layer = fmaf(sx[kx] * u[kx], u[kx], l2_layer);
-              }
-              {
-                dfl du[Q];
-                E::interp_d(du, yv0, sd);
+                  for (int kx = 0; kx < Q; ++kx) l2_layer = fmaf(sx[kx] * u[kx], u[kx], l2_layer);
+                }
+                {
+                  dfl du[Q];
+                  E::interp_d(du, yv0, sd);
 #pragma unroll
-                for (int kx = 0; kx < Q; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
-                E::test_d(h0, du, sd);
-              }
-              {
-                dfl du[Q], yv1[P + 1];
-                yrow(Y1, yv1);
-                E::interp_n(du, yv1, sn);
+                  for (int kx = 0; kx < Q; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
+                  E::test_d(h0, du, sd);
+                }
+                {
+                  dfl du[Q], yv1[P + 1];
+                  yrow(Y1, yv1);
+                  E::interp_n(du, yv1, sn);
 #pragma unroll
-                for (int kx = 0; kx < Q; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
-                E::test_n(h1, du, sn);
-              }
-              {
-                dfl du[Q], yv2[P + 1];
-                yrow(Y2, yv2);
-                E::interp_n(du, yv2, sn);
+                  for (int kx = 0; kx < Q; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
+                  E::test_n(h1, du, sn);
+                }
+                {
+                  dfl du[Q], yv2[P + 1];
+                  yrow(Y2, yv2);
+                  E::interp_n(du, yv2, sn);
 #pragma unroll
-                for (int kx = 0; kx < Q; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
-                E::test_n(h2, du, sn);
-              }
-              if constexpr (HAS_F) {
-                dfl hf[P + 1];
-                E::test_n(hf, g0, sn);
+                  for (int kx = 0; kx < Q; ++kx) du[kx] = df_mul(cw[kx], du[kx]);
+                  E::test_n(h2, du, sn);
+                }
+                if constexpr (HAS_F) {
+                  dfl hf[P + 1];
+                  E::test_n(hf, g0, sn);
 #pragma unroll
-                for (int b = 0; b <= P; ++b) h0[b] = df_add(h0[b], hf[b]);
+                  for (int b = 0; b <= P; ++b) h0[b] = df_add(h0[b], hf[b]);
+                }
               }
             }
-          }
-          if (!symx) {
-          dfl yv0[P + 1], yv1[P + 1], yv2[P + 1];
-          yrow(Y0, yv0);
-          yrow(Y1, yv1);
-          yrow(Y2, yv2);
+            if (!symx && !FOLD) {
+            dfl yv0[P + 1], yv1[P + 1], yv2[P + 1];
+            yrow(Y0, yv0);
+            yrow(Y1, yv1);
+            yrow(Y2, yv2);
 #pragma unroll
-          for (int kx = 0; kx < Q; ++kx) {
-            dfl dux = df_mul(nx[kx][0][1], yv0[0]);
-            dfl duy = df_mul(nx[kx][0][0], yv1[0]);
-            dfl duz = df_mul(nx[kx][0][0], yv2[0]);
-            float uu = nx[kx][0][0].x * yv0[0].x;
+            for (int kx = 0; kx < Q; ++kx) {
+              dfl dux = df_mul(nx[kx][0][1], yv0[0]);
+              dfl duy = df_mul(nx[kx][0][0], yv1[0]);
+              dfl duz = df_mul(nx[kx][0][0], yv2[0]);
+              float uu = nx[kx][0][0].x * yv0[0].x;
+#pragma unroll
+              for (int b = 1; b <= P; ++b) {
+                dux = df_mac(dux, nx[kx][b][1], yv0[b]);
+                duy = df_mac(duy, nx[kx][b][0], yv1[b]);
+                duz = df_mac(duz, nx[kx][b][0], yv2[b]);
+                uu = fmaf(nx[kx][b][0].x, yv0[b].x, uu);
+              }
+              const long long qidx = ((long long)(x0 + lane) * Q + kx) + QXt * (qyg + QYt * qzg);
+              dfl c;
+              dfl g0 = df_zero();
+              {
+                const dfl s = df_mul(jwx[kx], jwyz);
+                if constexpr (HAS_K) c = df_mul(df_mul(ndt, elem_ok ? df_split(a.kqp[qidx], 0) : df_zero()), s);
+                else c = df_mul(jwx[kx], cyz);
+                l2_layer = fmaf(s.x * uu, uu, l2_layer);
+                if constexpr (HAS_F) g0 = df_mul(df_mul(s, dtv), elem_ok ? df_split(a.fqp[qidx], uexp) : df_zero());
+              }
+              const dfl g1 = df_mul(c, dux), g2 = df_mul(c, duy), g3 = df_mul(c, duz);
+#pragma unroll
+              for (int b = 0; b <= P; ++b) {
+                if (kx == 0) {
+                  h0[b] = df_mul(nx[kx][b][1], g1);
+                  h1[b] = df_mul(nx[kx][b][0], g2);
+                  h2[b] = df_mul(nx[kx][b][0], g3);
+                } else {
+                  h0[b] = df_mac(h0[b], nx[kx][b][1], g1);
+                  h1[b] = df_mac(h1[b], nx[kx][b][0], g2);
+                  h2[b] = df_mac(h2[b], nx[kx][b][0], g3);
+                }
+                if constexpr (HAS_F) h0[b] = df_mac(h0[b], nx[kx][b][0], g0);
+              }
+            }
+            }  // !symx && !FOLD
+            // column cx = lane receives local function b of element lane - b
+            dfl v0 = h0[0], v1 = h1[0], v2 = h2[0];
 #pragma unroll
             for (int b = 1; b <= P; ++b) {
-              dux = df_mac(dux, nx[kx][b][1], yv0[b]);
-              duy = df_mac(duy, nx[kx][b][0], yv1[b]);
-              duz = df_mac(duz, nx[kx][b][0], yv2[b]);
-              uu = fmaf(nx[kx][b][0].x, yv0[b].x, uu);
+              const dfl s0 = df_shfl_up(h0[b], b);
+              const dfl s1 = df_shfl_up(h1[b], b);
+              const dfl s2 = df_shfl_up(h2[b], b);
+              if (lane >= b) { v0 = df_add(v0, s0); v1 = df_add(v1, s1); v2 = df_add(v2, s2); }
             }
-            const long long qidx = ((long long)(x0 + lane) * Q + kx) + QXt * (qyg + QYt * qzg);
-            dfl c;
-            dfl g0 = df_zero();
-            if constexpr (FOLD) {
-              // Jy Wy Jz Wz in the interpolated values, -dt kappa at the write
-              c = jwx[kx];
-              l2_layer = fmaf(jwx[kx].x * wr * uu, uu, l2_layer);
-            } else {
-              const dfl s = df_mul(jwx[kx], jwyz);
-              if constexpr (HAS_K) c = df_mul(df_mul(ndt, elem_ok ? df_split(a.kqp[qidx], 0) : df_zero()), s);
-              else c = df_mul(jwx[kx], cyz);
-              l2_layer = fmaf(s.x * uu, uu, l2_layer);
-              if constexpr (HAS_F) g0 = df_mul(df_mul(s, dtv), elem_ok ? df_split(a.fqp[qidx], uexp) : df_zero());
-            }
-            const dfl g1 = df_mul(c, dux), g2 = df_mul(c, duy), g3 = df_mul(c, duz);
-#pragma unroll
-            for (int b = 0; b <= P; ++b) {
-              if (kx == 0) {
-                h0[b] = df_mul(nx[kx][b][1], g1);
-                h1[b] = df_mul(nx[kx][b][0], g2);
-                h2[b] = df_mul(nx[kx][b][0], g3);
-              } else {
-                h0[b] = df_mac(h0[b], nx[kx][b][1], g1);
-                h1[b] = df_mac(h1[b], nx[kx][b][0], g2);
-                h2[b] = df_mac(h2[b], nx[kx][b][0], g3);
-              }
-              if constexpr (HAS_F) h0[b] = df_mac(h0[b], nx[kx][b][0], g0);
-            }
+            H0[qy * CX + lane] = v0;
+            H1[qy * CX + lane] = v1;
+            H2[qy * CX + lane] = v2;
           }
-          }  // !symx
-          // column cx = lane receives local function b of element lane - b
-          dfl v0 = h0[0], v1 = h1[0], v2 = h2[0];
-#pragma unroll
-          for (int b = 1; b <= P; ++b) {
-            const dfl s0 = df_shfl_up(h0[b], b);
-            const dfl s1 = df_shfl_up(h1[b], b);
-            const dfl s2 = df_shfl_up(h2[b], b);
-            if (lane >= b) { v0 = df_add(v0, s0); v1 = df_add(v1, s1); v2 = df_add(v2, s2); }
-          }
-          H0[qy * CX + lane] = v0;
-          H1[qy * CX + lane] = v1;
-          H2[qy * CX + lane] = v2;
         }
         __syncthreads();
 
@@ -762,15 +819,37 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
             }
           }
           }  // !symy
+          if constexpr (ZEO) {
+            if (symz) {
+              if (it & 1) {
 #pragma unroll
-          for (int bz = 0; bz <= P; ++bz) {
-            const dfl nz0 = NZs[(kz * (P + 1) + bz) * 2 + 0];
-            const dfl nz1 = NZs[(kz * (P + 1) + bz) * 2 + 1];
+                for (int by = 0; by <= P; ++by) E::zt_pair(acc[by], it >> 1, i0p[by], i0[by], i1p[by], i1[by], SZs);
+              } else if (2 * kz == P) {
 #pragma unroll
-            for (int by = 0; by <= P; ++by) acc[by][bz] = df_mac(df_mac(acc[by][bz], nz0, i0[by]), nz1, i1[by]);
+                for (int by = 0; by <= P; ++by) E::zt_mid(acc[by], i0[by], i1[by], SZs);
+              } else {
+#pragma unroll
+                for (int by = 0; by <= P; ++by) { i0p[by] = i0[by]; i1p[by] = i1[by]; }
+              }
+            }
+          }
+          if (!ZEO || !symz) {
+#pragma unroll
+            for (int bz = 0; bz <= P; ++bz) {
+              const dfl nz0 = NZs[(kz * (P + 1) + bz) * 2 + 0];
+              const dfl nz1 = NZs[(kz * (P + 1) + bz) * 2 + 1];
+#pragma unroll
+              for (int by = 0; by <= P; ++by) acc[by][bz] = df_mac(df_mac(acc[by][bz], nz0, i0[by]), nz1, i1[by]);
+            }
           }
         }
       }  // kz
+      if constexpr (ZEO) {
+        if (symz) {
+#pragma unroll
+          for (int by = 0; by <= P; ++by) E::zt_finish(acc[by]);
+        }
+      }
 
       // compensated FP32 sum of the l2 layers
       {

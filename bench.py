@@ -219,9 +219,10 @@ def df_assembly_ops(P, nelem, sym=(0.0, 0.0, 0.0), fold=False):
     At p = 2, sym = the fractions of the x stage, element rows and layers
     that run the even-odd form (centro-symmetric elements), whose sums cost
     less: an interpolation pair 52-68 operations where the direct sums take 84.
-    fold: constant conductivity and no source, where the point weights sit in
-    the tables and -dt kappa multiplies each written DOF, so the x stage has
-    no per-point product."""
+    fold: constant conductivity and no source, where the y and z point weights
+    sit in the tables, the x quadrature in the brick's x stiffness and mass
+    bands, and -dt kappa multiplies each written DOF, so the x stage is three
+    banded products (2P + 1 wide) per row of points and DOF column."""
     q = P + 1
     z = q * (2 * DF_MUL + 2 * P * DF_MAC)
     y = q * q * (3 * DF_MUL + 3 * P * DF_MAC)
@@ -230,6 +231,10 @@ def df_assembly_ops(P, nelem, sym=(0.0, 0.0, 0.0), fold=False):
     contraction = 3 * (P + 1) * DF_MUL + (q - 1) * 3 * (P + 1) * DF_MAC
     row = 0 if fold else 2 * DF_MUL                    # Jy Wy Jz Wz and its -dt kappa per row
     x = q * q * (row + q * per_kx + contraction + 3 * P * DF_ADD)
+    if fold:
+        # per row and DOF column: the reciprocal of Jy Wy Jz Wz, the l2norm's
+        # Y0 (Mx Y0) in FP32, then Kx Y0, Mx Y1, Mx Y2 in double-float
+        x = q * q * (3 + (2 * P + 1) + 2 + 3 * (DF_MUL + 2 * P * DF_MAC))
     yz_kz = (P + 1) * (2 * DF_MUL + DF_MAC) + (q - 1) * (P + 1) * 3 * DF_MAC + (P + 1) ** 2 * 2 * DF_MAC
     yz = q * yz_kz
     acc = (P + 1) ** 2 * DF_ADD + (DF_MUL if fold else 0)
@@ -244,13 +249,16 @@ def df_assembly_ops(P, nelem, sym=(0.0, 0.0, 0.0), fold=False):
         z_eo = eo_nd
         y_eo = q * (eo_nd + eo_n)
         if fold:
-            # the reciprocal of Jy Wy Jz Wz, u at the points and the l2 terms, then
-            # per component an interpolation and a contraction
-            x_row = 3 + 18 + 2 * eo_d + 2 * (2 * eo_n)
+            x_row = None  # the banded x stage has no even-odd form
         else:
             x_row = 2 * DF_MUL + q * (DF_MUL + 1) + 15 + (eo_d + 3 * DF_MUL + eo_d) + 2 * (eo_n + 3 * DF_MUL + eo_n)
-        x_eo = q * q * (x_row + 3 * P * DF_ADD)
+        x_eo = x if fold else q * q * (x_row + 3 * P * DF_ADD)
         yz_eo = q * ((eo_n + eo_d + 3 * DF_ADD + eo_n) + (P + 1) ** 2 * 2 * DF_MAC)
+        if fold:
+            # the z test over the point pair (0, 2) and the middle point in
+            # even-odd form: per DOF row the pair's 4 sums and 6 multiply-adds,
+            # the middle's 3 multiply-adds, and the final 2 sums
+            yz_eo = q * (eo_n + eo_d + 3 * DF_ADD + eo_n) + (P + 1) * (4 * DF_ADD + 9 * DF_MAC + 2 * DF_ADD)
         z = fz * z_eo + (1 - fz) * z
         y = fy * y_eo + (1 - fy) * y
         x = fx * x_eo + (1 - fx) * x

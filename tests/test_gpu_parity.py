@@ -294,7 +294,7 @@ def test_mixed_heat_steps_error_bound(ads_mod, oracle_mod):
 
 
 @pytest.mark.parametrize("E,p,var", [(24, 2, False), ((30, 20, 26), 2, True), (20, 3, False), (14, 3, True),
-                                     (18, 1, True), (10, 4, False)])
+                                     (18, 1, True), (12, 1, False), (10, 4, False)])
 def test_mixed_step_matches_fp64_step(ads_mod, E, p, var):
     """Mixed against FP64 on the GPU, step by step at a stable dt, with a
     constant conductivity or per-point conductivity plus a source (every
