@@ -278,6 +278,7 @@ struct DfLayout {
   static constexpr int RF = P + 1;  // accumulator ring
   static constexpr int NT = Q * (P + 1) * 2;
   static_assert(CX == 32, "footprint must be one warp wide");
+  static_assert(TY == AS_THREADS / 32, "a warp per element row");
   static constexpr size_t D = sizeof(dfl);
   static constexpr size_t o_cring = 0;                          // double [RC][NCOL] (cp.async target)
   static constexpr size_t o_tring = o_cring + 8 * RC * NCOL;    // dfl [RC][NCOL] split planes
@@ -325,6 +326,10 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
   // the z test contraction of a symmetric layer in even-odd form (at p = 2
   // with a per-point conductivity or a source its registers would spill)
   constexpr bool ZEO = E::on && (FOLD || P == 3);
+  // the x stage's output kept in registers for the y test (constant
+  // conductivity at p <= 2; the per-point x stage, or p = 3 with its 4 x 3
+  // values a lane, would cost registers the kernel does not have)
+  constexpr bool HREG = FOLD && P <= 2;
   constexpr int NCOL = L::NCOL, QY = L::QY, RC = L::RC, RF = L::RF, NT = L::NT;
 
   extern __shared__ __align__(16) unsigned char smem[];
@@ -609,11 +614,19 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
             }
           }
         }
-        __syncthreads();
+        // warp w is element row w in all three stages of a point layer: it
+        // writes the Y rows of its Q points, runs the x stage on them and
+        // reads the H rows it wrote, so the stages meet at warp barriers
+        __syncwarp();
 
         // ---- x interpolation + integrand + x test contraction (warp per row) ----
-        for (int qy = warp; qy < QY; qy += AS_THREADS / 32) {
-          const int ey_l = qy / Q;
+        // HREG: this lane's column of the warp's H rows stays in registers for
+        // the y test; otherwise the rows go through shared memory
+        dfl hr0[Q], hr1[Q], hr2[Q];
+#pragma unroll (HREG ? Q : 1)
+        for (int kyr = 0; kyr < Q; ++kyr) {
+          const int qy = warp * Q + kyr;
+          const int ey_l = warp;
           const bool elem_ok = lane_elem && (y0 + ey_l < Ey);
           const dfl jwyz = FOLD ? df_zero() : df_mul(JWYs[qy], JWZs[kz]);
           const dfl cyz = FOLD ? df_zero() : df_mul(ndtk, jwyz);
@@ -649,9 +662,15 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
               t = fmaf(mb[j].x, y0.x, t);
             }
             l2_layer = fmaf(wr * r0[lane].x, t, l2_layer);
-            H0[qy * CX + lane] = a0;
-            H1[qy * CX + lane] = a1;
-            H2[qy * CX + lane] = a2;
+            if constexpr (HREG) {
+              hr0[kyr] = a0;
+              hr1[kyr] = a1;
+              hr2[kyr] = a2;
+            } else {
+              H0[qy * CX + lane] = a0;
+              H1[qy * CX + lane] = a1;
+              H2[qy * CX + lane] = a2;
+            }
           } else {
             dfl h0[P + 1], h1[P + 1], h2[P + 1];
             if constexpr (E::on && !FOLD) {
@@ -774,7 +793,7 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
             H2[qy * CX + lane] = v2;
           }
         }
-        __syncthreads();
+        __syncwarp();
 
         // ---- y test contraction of this thread's element row, then z ----
         {
@@ -787,9 +806,9 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
 #pragma unroll
               for (int ky = 0; ky < Q; ++ky) {
                 const int qy = my_ey * Q + ky;
-                hv0[ky] = H0[qy * CX + my_cx];
-                hv1[ky] = H1[qy * CX + my_cx];
-                hv2[ky] = H2[qy * CX + my_cx];
+                hv0[ky] = HREG ? hr0[ky] : H0[qy * CX + my_cx];
+                hv1[ky] = HREG ? hr1[ky] : H1[qy * CX + my_cx];
+                hv2[ky] = HREG ? hr2[ky] : H2[qy * CX + my_cx];
               }
               E::test_n(ta, hv0, sn);
               E::test_d(tb1, hv1, sd);
@@ -802,9 +821,9 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
 #pragma unroll
           for (int ky = 0; ky < Q; ++ky) {
             const int qy = my_ey * Q + ky;
-            const dfl hv0 = H0[qy * CX + my_cx];
-            const dfl hv1 = H1[qy * CX + my_cx];
-            const dfl hv2 = H2[qy * CX + my_cx];
+            const dfl hv0 = HREG ? hr0[ky] : H0[qy * CX + my_cx];
+            const dfl hv1 = HREG ? hr1[ky] : H1[qy * CX + my_cx];
+            const dfl hv2 = HREG ? hr2[ky] : H2[qy * CX + my_cx];
             const dfl* ny = NYs + my_ey * NT + ky * (P + 1) * 2;
 #pragma unroll
             for (int by = 0; by <= P; ++by) {
