@@ -30,8 +30,11 @@
 // exactly.  The l2norm (J W u^2) is accumulated from the high parts in
 // compensated FP32.  At p = 2 and 3, elements whose tables are
 // centro-symmetric take the even-odd form of the sums (EO below): per layer
-// for the z interpolation, per element row for the y stages, per brick for the
-// x stage.
+// for the z interpolation and test, per element row for the y stages, per
+// brick for the x stage.  With a constant conductivity and no source the x
+// quadrature is done on the host, per element (its 1-D stiffness and mass
+// matrices, the same Gauss sums), and the x stage applies the brick's bands
+// of those matrices to each row of points.
 #include "df32.cuh"
 #include "k_assemble.cuh"
 
