@@ -398,10 +398,10 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
 
     __syncthreads();  // previous item fully done with shared memory
 
-    // per-lane x tables (element x0 + lane; lanes >= TX have no element).
-    // p = 2, 3: bricks whose elements are all centro-symmetric run the x
-    // stage in even-odd form; the table registers then hold the lane's NS
-    // even-odd coefficients
+    // per-lane x tables for the pointwise x stage (per-point conductivity or
+    // a source; element x0 + lane, lanes >= TX have no element).  p = 2, 3:
+    // bricks whose elements are all centro-symmetric run it in even-odd form;
+    // the table registers then hold the lane's NS even-odd coefficients
     dfl nx[Q][P + 1][2];
     dfl jwx[Q];
     // FOLD: row lane of the brick's x stiffness and mass bands, column
@@ -622,7 +622,8 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
         // reads the H rows it wrote, so the stages meet at warp barriers
         __syncwarp();
 
-        // ---- x interpolation + integrand + x test contraction (warp per row) ----
+        // ---- x stage (warp per row): the bands' products under FOLD, else x
+        // interpolation + integrand + x test contraction ----
         // HREG: this lane's column of the warp's H rows stays in registers for
         // the y test; otherwise the rows go through shared memory
         dfl hr0[Q], hr1[Q], hr2[Q];
