@@ -46,6 +46,10 @@ def test_double_float_operation_model():
     assert bench.df_assembly_ops(2, 1) == 8187
     assert bench.df_assembly_ops(2, 1, (1.0, 1.0, 1.0)) < 0.81 * 8187
     assert bench.df_assembly_ops(2, 1, (1.0, 1.0, 1.0), fold=True) < bench.df_assembly_ops(2, 1, (1.0, 1.0, 1.0))
+    # constant conductivity: the x stage is three banded products per row of
+    # points and DOF column, whatever the symmetry (166 operations at p = 2)
+    assert bench.df_assembly_ops(2, 1, fold=True) - bench.df_assembly_ops(2, 1, (1.0, 0.0, 0.0), fold=True) == 0
+    assert bench.df_assembly_ops(2, 1, (1.0, 1.0, 1.0), fold=True) < 0.41 * 8187
     fx, fy, fz = bench.even_odd_fractions(A, 256, 2)
     assert fx == (256 - 30 - 16) / 256 and fy == fz == 254 / 256
     fx96, fy96, _ = bench.even_odd_fractions(A, 96, 2)
