@@ -94,3 +94,30 @@ def test_x_bands_assemble_the_element_matrices(E, p):
         for e in range(x0, min(x0 + tx, E)):
             want[e - x0:e - x0 + p + 1] += m[e] @ v[e - x0:e - x0 + p + 1]
         np.testing.assert_allclose(got, want, rtol=0, atol=1e-13 * np.abs(m).max())
+
+
+@pytest.mark.parametrize("E,p", [(40, 2), (40, 3), (45, 4)])
+def test_x_bands_equal_the_pointwise_x_stage(E, p):
+    """The banded x stage and the pointwise one it replaces give the same
+    H rows: interpolating a row's coefficients to each element's x points,
+    weighting by Jx Wx and contracting with the test functions (values for
+    the mass part, derivatives for the stiffness part), then adding the
+    elements' contributions per DOF column."""
+    t = A.axis_setup(E + p - 1, p)
+    NN = t["NN"].reshape(E, p + 1, p + 1, 2)
+    jw = t["J"][:, None] * t["W"][None, :]
+    K, M = element_matrices(t, p)
+    tx = 32 - p
+    rng = np.random.default_rng(11)
+    for x0 in range(0, E, tx):
+        v = rng.standard_normal(tx + p)
+        for d, m in ((1, K), (0, M)):
+            point = np.zeros(tx + p)
+            for e in range(x0, min(x0 + tx, E)):
+                c = v[e - x0:e - x0 + p + 1]
+                at_points = NN[e, :, :, d] @ c                      # interpolation to the x points
+                point[e - x0:e - x0 + p + 1] += NN[e, :, :, d].T @ (jw[e] * at_points)  # weighted test
+            bb = brick_bands(m, x0, tx, p)
+            band = np.array([sum(bb[c, j] * v[min(max(c + j - p, 0), tx + p - 1)] for j in range(2 * p + 1))
+                             for c in range(tx + p)])
+            np.testing.assert_allclose(band, point, rtol=0, atol=1e-13 * np.abs(point).max())
