@@ -235,8 +235,8 @@ def df_assembly_ops(P, nelem, sym=(0.0, 0.0, 0.0), fold=False):
         # per row and DOF column: the reciprocal of Jy Wy Jz Wz, the l2norm's
         # Y0 (Mx Y0) in FP32, then Kx Y0, Mx Y1, Mx Y2 in double-float
         x = q * q * (3 + (2 * P + 1) + 2 + 3 * (DF_MUL + 2 * P * DF_MAC))
-    yz_kz = (P + 1) * (2 * DF_MUL + DF_MAC) + (q - 1) * (P + 1) * 3 * DF_MAC + (P + 1) ** 2 * 2 * DF_MAC
-    yz = q * yz_kz
+    yt = q * ((P + 1) * (2 * DF_MUL + DF_MAC) + (q - 1) * (P + 1) * 3 * DF_MAC)   # y test
+    za = q * (P + 1) ** 2 * 2 * DF_MAC                                            # z test
     acc = (P + 1) ** 2 * DF_ADD + (DF_MUL if fold else 0)
     if P == 2:
         fx, fy, fz = sym
@@ -253,17 +253,17 @@ def df_assembly_ops(P, nelem, sym=(0.0, 0.0, 0.0), fold=False):
         else:
             x_row = 2 * DF_MUL + q * (DF_MUL + 1) + 15 + (eo_d + 3 * DF_MUL + eo_d) + 2 * (eo_n + 3 * DF_MUL + eo_n)
         x_eo = x if fold else q * q * (x_row + 3 * P * DF_ADD)
-        yz_eo = q * ((eo_n + eo_d + 3 * DF_ADD + eo_n) + (P + 1) ** 2 * 2 * DF_MAC)
-        if fold:
-            # the z test over the point pair (0, 2) and the middle point in
-            # even-odd form: per DOF row the pair's 4 sums and 6 multiply-adds,
-            # the middle's 3 multiply-adds, and the final 2 sums
-            yz_eo = q * (eo_n + eo_d + 3 * DF_ADD + eo_n) + (P + 1) * (4 * DF_ADD + 9 * DF_MAC + 2 * DF_ADD)
+        yt_eo = q * (eo_n + eo_d + 3 * DF_ADD + eo_n)
+        # fold: the z test over the point pair (0, 2) and the middle point in
+        # even-odd form: per DOF row the pair's 4 sums and 6 multiply-adds, the
+        # middle's 3 multiply-adds, and the final 2 sums
+        za_eo = (P + 1) * (4 * DF_ADD + 9 * DF_MAC + 2 * DF_ADD) if fold else za
         z = fz * z_eo + (1 - fz) * z
         y = fy * y_eo + (1 - fy) * y
         x = fx * x_eo + (1 - fx) * x
-        yz = fy * yz_eo + (1 - fy) * yz
-    return (z + y + x + yz + acc) * nelem
+        yt = fy * yt_eo + (1 - fy) * yt
+        za = fz * za_eo + (1 - fz) * za
+    return (z + y + x + yt + za + acc) * nelem
 
 
 def even_odd_fractions(A, E, p):
