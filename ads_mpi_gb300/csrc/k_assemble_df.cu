@@ -659,11 +659,11 @@ __global__ void __launch_bounds__(AS_THREADS, P <= 2 ? 2 : 1)
             float t = mb[0].x * r0[xoff[0]].x;
 #pragma unroll
             for (int j = 1; j <= 2 * P; ++j) {
-              const dfl y0 = r0[xoff[j]];
-              a0 = df_mac(a0, kb[j], y0);
+              const dfl v0 = r0[xoff[j]];
+              a0 = df_mac(a0, kb[j], v0);
               a1 = df_mac(a1, mb[j], r1[xoff[j]]);
               a2 = df_mac(a2, mb[j], r2[xoff[j]]);
-              t = fmaf(mb[j].x, y0.x, t);
+              t = fmaf(mb[j].x, v0.x, t);
             }
             l2_layer = fmaf(wr * r0[lane].x, t, l2_layer);
             if constexpr (HREG) {
